@@ -1,0 +1,185 @@
+/*
+ * nsfv1_gb300.h -- C ABI of the GB300-native FV1 incompressible Navier-Stokes
+ * assembly and Newton path (drop-in for the NavierStokesFV1 element disc of
+ * UG4 plugin_NavierStokes).
+ *
+ * Conventions
+ *  - Every function returns an int status (NSFV1_OK on success); the text of
+ *    the last error of a handle is returned by nsfv1_last_error(). No C++
+ *    exception crosses this boundary (the reference throws UG_THROW).
+ *  - Pointers documented as "device" are CUDA device pointers owned by the
+ *    caller; "host" pointers are read during the call only. Streams are
+ *    cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - One handle = one element disc; calls on one handle are not re-entrant
+ *    (the reference's disc is not re-entrant either, navier_stokes_fv1.cpp:259).
+ *  - Element-local layouts (the reference's LocalVector / LocalMatrix,
+ *    navier_stokes_fv1.h:128-140, fct-major):
+ *      local vector  u[fct * nsh + sh]
+ *      local matrix  J[((f1 * nsh + s1) * b + f2) * nsh + s2]
+ *    Global layouts: vector U[node * b + fct]; matrix block CSR with b x b
+ *    row-major blocks, rows sorted by column, b = dim + 1.
+ *  - Element type ids are ugcore ReferenceObjectID values.
+ */
+#ifndef NSFV1_GB300_H
+#define NSFV1_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define NSFV1_OK                0
+#define NSFV1_ERR_ARGUMENT      1   /* bad argument or unknown name (reference: UG_THROW)      */
+#define NSFV1_ERR_STATE         2   /* missing setup (e.g. no stabilisation, no mesh)           */
+#define NSFV1_ERR_CUDA          3   /* CUDA runtime error                                       */
+#define NSFV1_ERR_NOT_CONVERGED 4   /* Newton reached max iterations                            */
+#define NSFV1_ERR_BREAKDOWN     5   /* Krylov breakdown (rho = 0, omega = 0, singular block)    */
+#define NSFV1_ERR_NONFINITE     6   /* NaN / Inf in a defect or update                          */
+#define NSFV1_ERR_GEOMETRY      7   /* upwind ray found no element side (reference: UG_THROW)   */
+#define NSFV1_ERR_TIMEOUT       8   /* a bounded device wait ran out                            */
+
+/* element types (ugcore ReferenceObjectID) */
+#define NSFV1_TRIANGLE       2
+#define NSFV1_QUADRILATERAL  3
+#define NSFV1_TETRAHEDRON    4
+#define NSFV1_HEXAHEDRON     8
+
+/* Jacobian value precision */
+#define NSFV1_F64 0
+#define NSFV1_F32 1
+
+/* linear solvers of the Newton loop */
+#define NSFV1_BICGSTAB 0
+#define NSFV1_GMRES    1
+
+typedef struct nsfv1_disc nsfv1_disc;
+
+/* ---- element disc: construction and parameters ------------------------- */
+
+/* NavierStokesFV1(fcts, subsets) + init(): dim+1 P1 functions, density 1
+ * (navier_stokes_fv1.cpp:45-87); dim is 2 or 3. */
+int nsfv1_create(int dim, nsfv1_disc** out);
+int nsfv1_destroy(nsfv1_disc* h);
+/* text of the last error on this handle (never NULL) */
+const char* nsfv1_last_error(const nsfv1_disc* h);
+/* disc_type() == "fv1" (navier_stokes_fv1.h:241) */
+const char* nsfv1_disc_type(const nsfv1_disc* h);
+
+/* NavierStokesBase::set_kinematic_viscosity(number) (navier_stokes_base.cpp:72-77) */
+int nsfv1_set_kinematic_viscosity(nsfv1_disc* h, double nu);
+/* IncompressibleNavierStokesBase::set_density(number) (incompressible_navier_stokes_base.cpp:93-98) */
+int nsfv1_set_density(nsfv1_disc* h, double rho);
+/* NavierStokesBase::set_source(std::vector<number>) (navier_stokes_base.cpp:91-97); n == dim */
+int nsfv1_set_source(nsfv1_disc* h, const double* f, int n);
+/* NavierStokesBase::set_exact_jacobian(number) (navier_stokes_base.h:194-196); 0 = fixpoint */
+int nsfv1_set_exact_jacobian(nsfv1_disc* h, double factor);
+/* set_stokes / set_laplace / set_peclet_blend (incompressible_navier_stokes_base.h:206-225) */
+int nsfv1_set_stokes(nsfv1_disc* h, int on);
+int nsfv1_set_laplace(nsfv1_disc* h, int on);
+int nsfv1_set_peclet_blend(nsfv1_disc* h, int on);
+/* NavierStokesFV1::set_upwind(const std::string&) (navier_stokes_fv1.h:213-215,
+ * ids of CreateNavierStokesUpwind, upwind_interface.cpp:43-62): "no", "full",
+ * "skewed", "lps" / "linearprofileskewed" (case-insensitive, trimmed). The
+ * object is shared with a stabilisation that has no upwind yet. */
+int nsfv1_set_upwind(nsfv1_disc* h, const char* name);
+/* NavierStokesFV1::set_stabilization(name[, diffLength]) (navier_stokes_fv1.h:190-199,
+ * CreateNavierStokesStabilization stabilization.cpp:46-57, set_diffusion_length
+ * stabilization.cpp:86-100): "fields", "flow" (+ "without" for
+ * NavierStokesFV1WithoutStabilization); diff_length "raw" (NULL), "fivepoint", "cor". */
+int nsfv1_set_stabilization(nsfv1_disc* h, const char* name, const char* diff_length);
+/* INavierStokesFV1Stabilization::set_upwind with an upwind object of its own
+ * (stabilization.h:91-95, registered at register_fv1.cpp:246-249). */
+int nsfv1_set_stabilization_upwind(nsfv1_disc* h, const char* name);
+
+/* ---- mesh, sparsity pattern, colouring ---------------------------------- */
+
+/* Sets the element mesh (one element type; host arrays): coords[n_nodes*dim],
+ * conn[n_elems*nsh] (ugcore corner order). Builds the block-CSR pattern (all
+ * node pairs sharing an element; the sparsity of the reference's assembled
+ * matrix) and a greedy element colouring, and uploads them.
+ * Replaces prepare_setting / prep_elem_loop (navier_stokes_fv1.cpp:89-199)
+ * plus ugcore's DoF distribution and matrix-pattern setup. */
+int nsfv1_set_mesh(nsfv1_disc* h, int elem_type, int64_t n_nodes, const double* coords, int64_t n_elems, const int32_t* conn);
+int nsfv1_pattern_info(const nsfv1_disc* h, int64_t* n_rows, int64_t* nnz_blocks, int* block_size, int* n_colors);
+/* Host-only form of the same pattern / colouring build (no handle, no GPU):
+ * call with row_ptr == NULL to get *nnz_blocks and *n_colors, then again with
+ * row_ptr[n_nodes+1], col_idx[nnz_blocks], elem_color[n_elems] (each may be NULL). */
+int nsfv1_mesh_pattern(int elem_type, int64_t n_nodes, int64_t n_elems, const int32_t* conn, int64_t* nnz_blocks,
+                       int* n_colors, int32_t* row_ptr, int32_t* col_idx, int32_t* elem_color);
+/* host copies of the pattern (row_ptr[n_rows+1], col_idx[nnz_blocks]) and colouring */
+int nsfv1_get_pattern(const nsfv1_disc* h, int32_t* row_ptr, int32_t* col_idx);
+int nsfv1_get_coloring(const nsfv1_disc* h, int32_t* elem_color);
+/* device pointers of the pattern, owned by the handle (valid until the next set_mesh/destroy) */
+int nsfv1_device_pattern(const nsfv1_disc* h, const int32_t** row_ptr, const int32_t** col_idx);
+/* Dirichlet rows (host arrays): dofs[k] = node * b + fct, value g_k.
+ * Defect row = u - g, Jacobian row = identity (the reference's core
+ * DirichletBoundary semantics, bnd/wall_impl.h:57-69). */
+int nsfv1_set_dirichlet(nsfv1_disc* h, int64_t n, const int32_t* dofs, const double* values);
+
+/* ---- assembly (device pointers) ----------------------------------------- */
+
+/* Global defect d = A(u) - F (stationary, u_old == NULL) or
+ * d = M(u) - M(u_old) + dt (A(u) - F) (implicit Euler), FP64, with Dirichlet rows.
+ * Replaces the element loop over prep_elem + add_def_A_elem + add_def_M_elem +
+ * add_rhs_elem (navier_stokes_fv1.cpp:208-248, 597-869) and the scatter. */
+int nsfv1_assemble_defect(nsfv1_disc* h, const double* u, const double* u_old, double dt, double* d, void* stream);
+/* Global Jacobian values J = dA/du (or M + dt dA/du) in the handle's block CSR,
+ * vals[nnz_blocks * b * b] of double (NSFV1_F64) or float (NSFV1_F32).
+ * Replaces the element loop over add_jac_A_elem + add_jac_M_elem
+ * (navier_stokes_fv1.cpp:250-595, 781-808) and the matrix insertion. */
+int nsfv1_assemble_jacobian(nsfv1_disc* h, const double* u, const double* u_old, double dt, void* vals, int prec, void* stream);
+/* The reference's per-element callbacks, batched over n independent elements
+ * (device arrays): corners[n][nsh][dim], u/u_old[n][b*nsh] (local layout);
+ * outputs (each may be NULL) defA, defM, rhs [n][b*nsh] and jacA, jacM
+ * [n][(b*nsh)^2]: add_def_A_elem, add_def_M_elem, add_rhs_elem, add_jac_A_elem,
+ * add_jac_M_elem (navier_stokes_fv1.cpp:250-869), each output zeroed first. */
+int nsfv1_elem_batch(nsfv1_disc* h, int elem_type, int64_t n, const double* corners, const double* u, const double* u_old,
+                     double dt, double* defA, double* jacA, double* defM, double* jacM, double* rhs, void* stream);
+
+/* ---- linear algebra on the handle's pattern (device pointers) ------------ */
+
+/* y = J x with J in the handle's block CSR (prec as above; x, y FP64) */
+int nsfv1_bsr_mv(nsfv1_disc* h, const void* vals, int prec, const double* x, double* y, void* stream);
+
+/* ---- Newton solve (the plain method and the FP32-Jacobian mode) ---------- */
+
+typedef struct {
+    double rtol;            /* relative defect reduction (e.g. 1e-8)                      */
+    double atol;            /* absolute defect floor (0 to disable)                       */
+    int max_iter;           /* Newton iterations                                          */
+    double lin_rtol;        /* relative residual reduction of the linear solve            */
+    int lin_max_iter;       /* linear iterations per Newton step                          */
+    int line_search_steps;  /* backtracking halvings (0 = full steps)                     */
+    int jacobian_prec;      /* NSFV1_F64 (plain method) or NSFV1_F32 (FP32 Jacobian)      */
+    int linear_solver;      /* NSFV1_BICGSTAB or NSFV1_GMRES                              */
+    int gmres_restart;      /* GMRES restart length (<= 64)                               */
+} nsfv1_newton_params;
+
+typedef struct {
+    int iterations;
+    int linear_iterations;
+    double initial_defect;  /* ||d(u0)||_2 */
+    double final_defect;    /* ||d(u)||_2  */
+    int status;             /* NSFV1_OK, NSFV1_ERR_NOT_CONVERGED, ...                      */
+} nsfv1_newton_result;
+
+/* Newton from the given device vector u (overwritten with the solution): the
+ * Dirichlet values are set into u, then d = defect(u); loop { J(u) du = d
+ * (point-block-Jacobi preconditioned BiCGStab / GMRES in the Jacobian's
+ * precision); u -= lambda du with backtracking on ||d||_2 } until
+ * ||d|| <= rtol ||d0|| (ugcore's Newton, restated). Defect, norms, update and
+ * line search are FP64. u_old/dt as in nsfv1_assemble_defect. */
+int nsfv1_newton_solve(nsfv1_disc* h, double* u, const double* u_old, double dt, const nsfv1_newton_params* p,
+                       nsfv1_newton_result* r, void* stream);
+
+/* reference-element tables used by the kernels (for the table-consistency test):
+ * edges[2*nedge], sides[4*nside] (unused slots -1), side_nco[nside], edge_face[2*nedge] */
+int nsfv1_ref_tables(int elem_type, int* nco, int* nedge, int* edges, int* nside, int* side_nco, int* sides, int* edge_face);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NSFV1_GB300_H */

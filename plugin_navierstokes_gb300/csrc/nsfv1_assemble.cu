@@ -1,0 +1,294 @@
+// FV1 assembly kernels for sm_103a: one thread per element, elements of one
+// colour per launch (no two share a node), so the scatter into the global
+// defect / block-CSR Jacobian is a plain read-modify-write and the summation
+// order per entry is fixed (colour order, then SCVF order): runs are bitwise
+// reproducible.
+#include <type_traits>
+#include "nsfv1_internal.h"
+#include "nsfv1_elem.cuh"
+
+namespace nsfv1 {
+
+static constexpr int kThreads = 128;
+
+// ---- element gather --------------------------------------------------------
+
+// Corner coordinates; in float mode relative to corner 0 (all geometry used is
+// translation invariant) so that single precision keeps the local detail.
+template <int ROID, typename T>
+__device__ __forceinline__ void load_corners(const double* __restrict__ coords, const int32_t (&nodes)[Ref<ROID>::nsh], Elem<ROID, T>& E) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh;
+    if constexpr (std::is_same<T, double>::value) {
+#pragma unroll
+        for (int k = 0; k < nsh; ++k)
+#pragma unroll
+            for (int d = 0; d < dim; ++d) E.x[k][d] = __ldg(coords + (int64_t)nodes[k] * dim + d);
+    } else {
+        double x0[dim];
+#pragma unroll
+        for (int d = 0; d < dim; ++d) x0[d] = __ldg(coords + (int64_t)nodes[0] * dim + d);
+#pragma unroll
+        for (int k = 0; k < nsh; ++k)
+#pragma unroll
+            for (int d = 0; d < dim; ++d) E.x[k][d] = (T)(__ldg(coords + (int64_t)nodes[k] * dim + d) - x0[d]);
+    }
+}
+
+template <int ROID, typename T>
+__device__ __forceinline__ void load_u(const double* __restrict__ U, const int32_t (&nodes)[Ref<ROID>::nsh], T (&u)[Ref<ROID>::b][Ref<ROID>::nsh]) {
+    using R = Ref<ROID>;
+    constexpr int b = R::b, nsh = R::nsh;
+#pragma unroll
+    for (int k = 0; k < nsh; ++k) {
+        if constexpr (b == 4) {
+            const double2* p = reinterpret_cast<const double2*>(U + (int64_t)nodes[k] * 4);
+            const double2 a = __ldg(p), c = __ldg(p + 1);
+            u[0][k] = (T)a.x; u[1][k] = (T)a.y; u[2][k] = (T)c.x; u[3][k] = (T)c.y;
+        } else {
+#pragma unroll
+            for (int f = 0; f < b; ++f) u[f][k] = (T)__ldg(U + (int64_t)nodes[k] * b + f);
+        }
+    }
+}
+
+// ---- sinks for the local Jacobian blocks ------------------------------------
+
+template <typename VT, int nsh>
+struct GlobalJacSink {
+    VT* __restrict__ vals;
+    const int32_t* __restrict__ blk;   // this element's [nsh][nsh] block indices
+    template <int b, typename T>
+    __device__ __forceinline__ void add(const int i, const int k, const T (&B)[b][b], const bool plus) {
+        VT* p = vals + (int64_t)__ldg(blk + i * nsh + k) * (b * b);
+#pragma unroll
+        for (int r = 0; r < b; ++r)
+#pragma unroll
+            for (int c = 0; c < b; ++c) {
+                const VT v = (VT)B[r][c];
+                p[r * b + c] = plus ? p[r * b + c] + v : p[r * b + c] - v;
+            }
+    }
+};
+
+template <int nsh>
+struct LocalJacSink {
+    double* __restrict__ J;   // element-local [(f1 * nsh + s1) * b + f2] * nsh + s2
+    template <int b, typename T>
+    __device__ __forceinline__ void add(int i, int k, const T (&B)[b][b], bool plus) {
+#pragma unroll
+        for (int r = 0; r < b; ++r)
+#pragma unroll
+            for (int c = 0; c < b; ++c) {
+                double* q = J + ((r * nsh + i) * b + c) * nsh + k;
+                *q = plus ? *q + (double)B[r][c] : *q - (double)B[r][c];
+            }
+    }
+};
+
+// ---- global assembly kernels -------------------------------------------------
+
+template <int ROID>
+__global__ void __launch_bounds__(kThreads) k_defect(const DiscParams P, const AsmArgs A) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh, b = R::b;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.count) return;
+    const int32_t e = __ldg(A.elems + t);
+    int32_t nodes[nsh];
+#pragma unroll
+    for (int k = 0; k < nsh; ++k) nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
+    Elem<ROID, double> E;
+    load_corners<ROID, double>(A.coords, nodes, E);
+    elem_setup<ROID, double>(E);
+    double u[b][nsh], uo[b][nsh], dA[b][nsh];
+    load_u<ROID, double>(A.U, nodes, u);
+    if (P.transient) load_u<ROID, double>(A.Uold, nodes, uo);
+#pragma unroll
+    for (int f = 0; f < b; ++f)
+#pragma unroll
+        for (int k = 0; k < nsh; ++k) dA[f][k] = 0.0;
+    if (!elem_def_A<ROID, double>(P, E, u, uo, dA)) atomicOr(A.err, 1);
+    const double rho = P.rho;
+#pragma unroll
+    for (int k = 0; k < nsh; ++k) {
+        double loc[b];
+#pragma unroll
+        for (int f = 0; f < b; ++f) {
+            double v = dA[f][k];
+            if (f < dim && P.hasSource) v -= P.src[f] * E.vol[k] * rho;
+            if (P.transient) {
+                v = v * P.dt;
+                if (f < dim) v = (u[f][k] * E.vol[k] * rho - uo[f][k] * E.vol[k] * rho) + v;
+            }
+            loc[f] = v;
+        }
+        double* dp = A.D + (int64_t)nodes[k] * b;
+#pragma unroll
+        for (int f = 0; f < b; ++f) dp[f] += loc[f];
+    }
+}
+
+template <int ROID, typename T, typename VT>
+__global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const AsmArgs A) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh, b = R::b;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.count) return;
+    const int32_t e = __ldg(A.elems + t);
+    int32_t nodes[nsh];
+#pragma unroll
+    for (int k = 0; k < nsh; ++k) nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
+    Elem<ROID, T> E;
+    load_corners<ROID, T>(A.coords, nodes, E);
+    elem_setup<ROID, T>(E);
+    T u[b][nsh];
+    load_u<ROID, T>(A.U, nodes, u);
+    GlobalJacSink<VT, nsh> sink{reinterpret_cast<VT*>(A.vals), A.elemBlk + (int64_t)e * nsh * nsh};
+    const T scale = P.transient ? (T)P.dt : T(1);
+    if (!elem_jac_A<ROID, T>(P, E, u, scale, sink)) atomicOr(A.err, 1);
+    if (P.transient) {
+        // mass part: J(d, sh, d, sh) += |SCV| rho
+#pragma unroll
+        for (int k = 0; k < nsh; ++k) {
+            VT* p = sink.vals + (int64_t)__ldg(sink.blk + k * nsh + k) * (b * b);
+#pragma unroll
+            for (int d = 0; d < dim; ++d) p[d * b + d] += (VT)(E.vol[k] * T(P.rho));
+        }
+    }
+}
+
+// ---- batched element-local callbacks ----------------------------------------
+
+template <int ROID>
+__global__ void __launch_bounds__(kThreads) k_elem_batch(const DiscParams P, const ElemBatchArgs A) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh, b = R::b, n = b * nsh;
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= A.n) return;
+    Elem<ROID, double> E;
+#pragma unroll
+    for (int k = 0; k < nsh; ++k)
+#pragma unroll
+        for (int d = 0; d < dim; ++d) E.x[k][d] = A.corners[(e * nsh + k) * dim + d];
+    elem_setup<ROID, double>(E);
+    double u[b][nsh], uo[b][nsh];
+#pragma unroll
+    for (int f = 0; f < b; ++f)
+#pragma unroll
+        for (int k = 0; k < nsh; ++k) {
+            u[f][k] = A.u[e * n + f * nsh + k];
+            uo[f][k] = A.uold ? A.uold[e * n + f * nsh + k] : 0.0;
+        }
+    DiscParams Q = P;
+    Q.transient = A.uold != nullptr;
+    if (A.defA) {
+        double dA[b][nsh];
+#pragma unroll
+        for (int f = 0; f < b; ++f)
+#pragma unroll
+            for (int k = 0; k < nsh; ++k) dA[f][k] = 0.0;
+        if (!elem_def_A<ROID, double>(Q, E, u, uo, dA)) atomicOr(A.err, 1);
+#pragma unroll
+        for (int f = 0; f < b; ++f)
+#pragma unroll
+            for (int k = 0; k < nsh; ++k) A.defA[e * n + f * nsh + k] = dA[f][k];
+    }
+    if (A.jacA) {
+        double* J = A.jacA + e * n * n;
+        for (int q = 0; q < n * n; ++q) J[q] = 0.0;
+        LocalJacSink<nsh> sink{J};
+        if (!elem_jac_A<ROID, double>(Q, E, u, 1.0, sink)) atomicOr(A.err, 1);
+    }
+    if (A.defM) {
+        for (int q = 0; q < n; ++q) A.defM[e * n + q] = 0.0;
+#pragma unroll
+        for (int k = 0; k < nsh; ++k)
+#pragma unroll
+            for (int d = 0; d < dim; ++d) A.defM[e * n + d * nsh + k] = u[d][k] * E.vol[k] * P.rho;
+    }
+    if (A.jacM) {
+        double* J = A.jacM + e * n * n;
+        for (int q = 0; q < n * n; ++q) J[q] = 0.0;
+#pragma unroll
+        for (int k = 0; k < nsh; ++k)
+#pragma unroll
+            for (int d = 0; d < dim; ++d) J[((d * nsh + k) * b + d) * nsh + k] = E.vol[k] * P.rho;
+    }
+    if (A.rhs) {
+        for (int q = 0; q < n; ++q) A.rhs[e * n + q] = 0.0;
+        if (P.hasSource) {
+#pragma unroll
+            for (int k = 0; k < nsh; ++k)
+#pragma unroll
+                for (int d = 0; d < dim; ++d) A.rhs[e * n + d * nsh + k] = P.src[d] * E.vol[k] * P.rho;
+        }
+    }
+}
+
+// ---- Dirichlet rows ------------------------------------------------------------
+// defect = u - g ; Jacobian row = identity row (off-diagonal blocks stay in the pattern)
+template <typename VT>
+__global__ void k_dirichlet(int b, int64_t n, const int32_t* __restrict__ rows, const double* __restrict__ vals,
+                            const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx,
+                            const double* __restrict__ U, double* D, VT* J) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t dof = rows[i];
+    const int32_t node = dof / b, f = dof % b;
+    if (D) D[dof] = U[dof] - vals[i];
+    if (J) {
+        for (int32_t q = rowPtr[node]; q < rowPtr[node + 1]; ++q) {
+            VT* blk = J + (int64_t)q * b * b;
+            const bool diag = colIdx[q] == node;
+            for (int c = 0; c < b; ++c) blk[f * b + c] = (diag && c == f) ? VT(1) : VT(0);
+        }
+    }
+}
+
+// ---- launchers ------------------------------------------------------------------
+
+template <class F>
+static cudaError_t dispatch_roid(int roid, F&& f) {
+    switch (roid) {
+        case ROID_TRIANGLE: f(std::integral_constant<int, ROID_TRIANGLE>{}); break;
+        case ROID_QUADRILATERAL: f(std::integral_constant<int, ROID_QUADRILATERAL>{}); break;
+        case ROID_TETRAHEDRON: f(std::integral_constant<int, ROID_TETRAHEDRON>{}); break;
+        case ROID_HEXAHEDRON: f(std::integral_constant<int, ROID_HEXAHEDRON>{}); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_defect(int roid, const DiscParams& P, const AsmArgs& a, cudaStream_t s) {
+    if (a.count <= 0) return cudaSuccess;
+    const int grid = (a.count + kThreads - 1) / kThreads;
+    return dispatch_roid(roid, [&](auto r) { k_defect<decltype(r)::value><<<grid, kThreads, 0, s>>>(P, a); });
+}
+
+cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s) {
+    if (a.count <= 0) return cudaSuccess;
+    const int grid = (a.count + kThreads - 1) / kThreads;
+    return dispatch_roid(roid, [&](auto r) {
+        constexpr int RO = decltype(r)::value;
+        if (prec == 0) k_jacobian<RO, double, double><<<grid, kThreads, 0, s>>>(P, a);
+        else k_jacobian<RO, float, float><<<grid, kThreads, 0, s>>>(P, a);
+    });
+}
+
+cudaError_t launch_elem_batch(int roid, const DiscParams& P, const ElemBatchArgs& a, cudaStream_t s) {
+    if (a.n <= 0) return cudaSuccess;
+    const int grid = (int)((a.n + kThreads - 1) / kThreads);
+    return dispatch_roid(roid, [&](auto r) { k_elem_batch<decltype(r)::value><<<grid, kThreads, 0, s>>>(P, a); });
+}
+
+cudaError_t launch_dirichlet(int b, int64_t n, const int32_t* rows, const double* vals, const int32_t* rowPtr,
+                             const int32_t* colIdx, const double* U, double* D, void* J, int prec, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int grid = (int)((n + 255) / 256);
+    if (prec == 0) k_dirichlet<double><<<grid, 256, 0, s>>>(b, n, rows, vals, rowPtr, colIdx, U, D, (double*)J);
+    else k_dirichlet<float><<<grid, 256, 0, s>>>(b, n, rows, vals, rowPtr, colIdx, U, D, (float*)J);
+    return cudaGetLastError();
+}
+
+}  // namespace nsfv1

@@ -1,0 +1,488 @@
+// Host side of the C ABI (include/nsfv1_gb300.h): the element-disc handle,
+// its setters (same names, string ids and error behaviour as the reference's
+// NavierStokesFV1 / NavierStokesBase / IncompressibleNavierStokesBase), the
+// mesh set-up (block-CSR pattern, element colouring, device upload) and the
+// assembly dispatch.
+#include <algorithm>
+#include <cctype>
+#include <cstring>
+#include <exception>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#include "nsfv1_internal.h"
+#include "nsfv1_refelem.cuh"
+#include "nsfv1_host.h"
+#include "../../include/nsfv1_gb300.h"
+
+using namespace nsfv1;
+
+namespace nsfv1 {
+
+std::string lower_trim(const char* s) {
+    std::string n = s ? s : "";
+    const size_t a = n.find_first_not_of(" \t\n\r"), z = n.find_last_not_of(" \t\n\r");
+    n = (a == std::string::npos) ? std::string() : n.substr(a, z - a + 1);
+    std::transform(n.begin(), n.end(), n.begin(), [](unsigned char c) { return (char)std::tolower(c); });
+    return n;
+}
+
+// CreateNavierStokesUpwind (upwind_interface.cpp:43-62), FV1 upwinds of this path
+static int upwind_id(const char* name) {
+    const std::string n = lower_trim(name);
+    if (n == "no") return UPW_NO;
+    if (n == "full") return UPW_FULL;
+    if (n == "skewed") return UPW_SKEWED;
+    if (n == "linearprofileskewed" || n == "lps") return UPW_LPS;
+    return -1;
+}
+// CreateNavierStokesStabilization (stabilization.cpp:46-57) + the "without" variant
+static int stab_id(const char* name) {
+    const std::string n = lower_trim(name);
+    if (n == "fields") return STAB_FIELDS;
+    if (n == "flow") return STAB_FLOW;
+    if (n == "without" || n == "none") return STAB_WITHOUT;
+    return -1;
+}
+// set_diffusion_length (stabilization.cpp:86-100)
+static int difflen_id(const char* name) {
+    const std::string n = lower_trim(name);
+    if (n == "raw") return DL_RAW;
+    if (n == "fivepoint") return DL_FIVEPOINT;
+    if (n == "cor") return DL_COR;
+    return -1;
+}
+
+int ref_dim(int roid) { return (roid == ROID_TRIANGLE || roid == ROID_QUADRILATERAL) ? 2 : (roid == ROID_TETRAHEDRON || roid == ROID_HEXAHEDRON) ? 3 : 0; }
+int ref_nsh(int roid) {
+    switch (roid) {
+        case ROID_TRIANGLE: return 3;
+        case ROID_QUADRILATERAL: return 4;
+        case ROID_TETRAHEDRON: return 4;
+        case ROID_HEXAHEDRON: return 8;
+    }
+    return 0;
+}
+
+template <class T> static void dfree(T*& p) { if (p) cudaFree((void*)p); p = nullptr; }
+
+template <class T> static cudaError_t dupload(T*& dst, const T* src, size_t n) {
+    dfree(dst);
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void**)&dst, n * sizeof(T));
+    if (e != cudaSuccess) { dst = nullptr; return e; }
+    return cudaMemcpy((void*)dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+void Disc::free_mesh() {
+    dfree(d_coords); dfree(d_conn); dfree(d_elemBlk); dfree(d_colorElems); dfree(d_rowPtr); dfree(d_colIdx);
+    dfree(d_dirRow); dfree(d_dirVal);
+}
+
+Disc::~Disc() {
+    free_mesh();
+    free_workspace();
+    dfree(d_err);
+}
+
+// Disc parameters for a launch; validates like prep_elem_loop (navier_stokes_fv1.cpp:136-199)
+bool Disc::params(DiscParams& P, bool transient, double dt) {
+    if (!stabSet) return fail(NSFV1_ERR_STATE, "Stabilization has not been set.");
+    if (!stokes && !convUpwindSet) return fail(NSFV1_ERR_STATE, "Upwinding for convective Term in Momentum eq. not set.");
+    if (!viscoSet) return fail(NSFV1_ERR_STATE, "NavierStokes::prep_elem_loop: Kinematic Viscosity has not been set, but is required.");
+    if (!stokes && stabUpwindType < 0) return fail(NSFV1_ERR_STATE, "No upwind object");
+    std::memset(&P, 0, sizeof(P));
+    P.nu = nu; P.rho = rho; P.fullNewton = fullNewton; P.dt = dt;
+    for (int d = 0; d < 3; ++d) P.src[d] = src[d];
+    P.convUpwind = convUpwindType;
+    P.stabUpwind = stabUpwindType < 0 ? convUpwindType : stabUpwindType;
+    P.sameUpwind = stabSharesConv ? 1 : 0;
+    P.stab = stabType; P.diffLen = diffLen;
+    P.stokes = stokes; P.laplace = laplace; P.peclet = peclet; P.hasSource = hasSource; P.transient = transient ? 1 : 0;
+    return true;
+}
+
+bool Disc::fail(int code, const std::string& msg) {
+    status = code;
+    lastError = msg;
+    return false;
+}
+
+bool Disc::cuda_ok(cudaError_t e, const char* where) {
+    if (e == cudaSuccess) return true;
+    return fail(NSFV1_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+bool Disc::check_err_word(cudaStream_t s) {
+    int err = 0;
+    if (!cuda_ok(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "error word")) return false;
+    if (!cuda_ok(cudaStreamSynchronize(s), "sync")) return false;
+    if (err & 1) {
+        cudaMemsetAsync(d_err, 0, sizeof(int), s);
+        return fail(NSFV1_ERR_GEOMETRY, "GetLinearProfileSkewedUpwindShapes: Cannot find cut side.");
+    }
+    return true;
+}
+
+// block-CSR pattern: every node pair sharing an element, columns sorted
+static void build_pattern(int nsh, int64_t nNodes, int64_t nElems, const int32_t* conn, std::vector<int32_t>& rowPtr,
+                          std::vector<int32_t>& colIdx, std::vector<int32_t>& elemBlk) {
+    // node -> incident elements
+    std::vector<int64_t> nptr(nNodes + 1, 0);
+    for (int64_t k = 0; k < nElems * nsh; ++k) nptr[conn[k] + 1]++;
+    for (int64_t r = 0; r < nNodes; ++r) nptr[r + 1] += nptr[r];
+    std::vector<int32_t> nel(nptr[nNodes]);
+    {
+        std::vector<int64_t> fill(nptr.begin(), nptr.end() - 1);
+        for (int64_t e = 0; e < nElems; ++e)
+            for (int i = 0; i < nsh; ++i) nel[fill[conn[e * nsh + i]]++] = (int32_t)e;
+    }
+    rowPtr.assign(nNodes + 1, 0);
+    std::vector<int32_t> scratch;
+    colIdx.clear();
+    colIdx.reserve((size_t)nNodes * (nsh == 8 ? 27 : 9));
+    for (int64_t r = 0; r < nNodes; ++r) {
+        scratch.clear();
+        for (int64_t k = nptr[r]; k < nptr[r + 1]; ++k) {
+            const int64_t e = nel[k];
+            for (int j = 0; j < nsh; ++j) scratch.push_back(conn[e * nsh + j]);
+        }
+        std::sort(scratch.begin(), scratch.end());
+        scratch.erase(std::unique(scratch.begin(), scratch.end()), scratch.end());
+        colIdx.insert(colIdx.end(), scratch.begin(), scratch.end());
+        rowPtr[r + 1] = (int32_t)colIdx.size();
+    }
+    elemBlk.resize((size_t)nElems * nsh * nsh);
+    for (int64_t e = 0; e < nElems; ++e)
+        for (int i = 0; i < nsh; ++i) {
+            const int32_t r = conn[e * nsh + i];
+            const int32_t* b0 = colIdx.data() + rowPtr[r];
+            const int32_t* b1 = colIdx.data() + rowPtr[r + 1];
+            for (int j = 0; j < nsh; ++j)
+                elemBlk[(e * nsh + i) * nsh + j] = (int32_t)(std::lower_bound(b0, b1, conn[e * nsh + j]) - colIdx.data());
+        }
+}
+
+// greedy colouring in element order: the smallest colour not used by an
+// earlier element that shares a node
+static int build_coloring(int nsh, int64_t nNodes, int64_t nElems, const int32_t* conn, std::vector<int32_t>& color) {
+    std::vector<int64_t> nptr(nNodes + 1, 0);
+    for (int64_t k = 0; k < nElems * nsh; ++k) nptr[conn[k] + 1]++;
+    for (int64_t r = 0; r < nNodes; ++r) nptr[r + 1] += nptr[r];
+    std::vector<int32_t> nel(nptr[nNodes]);
+    {
+        std::vector<int64_t> fill(nptr.begin(), nptr.end() - 1);
+        for (int64_t e = 0; e < nElems; ++e)
+            for (int i = 0; i < nsh; ++i) nel[fill[conn[e * nsh + i]]++] = (int32_t)e;
+    }
+    color.assign(nElems, -1);
+    std::vector<int64_t> mark(256, -1);
+    int nc = 0;
+    for (int64_t e = 0; e < nElems; ++e) {
+        for (int i = 0; i < nsh; ++i) {
+            const int32_t n = conn[e * nsh + i];
+            for (int64_t k = nptr[n]; k < nptr[n + 1]; ++k) {
+                const int32_t o = nel[k];
+                if (o < e && color[o] >= 0) mark[color[o]] = e;
+            }
+        }
+        int c = 0;
+        while (mark[c] == e) ++c;
+        if (c >= 255) return -1;
+        color[e] = c;
+        nc = std::max(nc, c + 1);
+    }
+    return nc;
+}
+
+}  // namespace nsfv1
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+int nsfv1_create(int dim, nsfv1_disc** out) {
+    if (!out || (dim != 2 && dim != 3)) return NSFV1_ERR_ARGUMENT;
+    try {
+        Disc* h = new Disc();
+        h->dim = dim;
+        *out = reinterpret_cast<nsfv1_disc*>(h);
+        return NSFV1_OK;
+    } catch (...) { return NSFV1_ERR_ARGUMENT; }
+}
+
+int nsfv1_destroy(nsfv1_disc* h) {
+    delete reinterpret_cast<Disc*>(h);
+    return NSFV1_OK;
+}
+
+const char* nsfv1_last_error(const nsfv1_disc* h) {
+    return h ? reinterpret_cast<const Disc*>(h)->lastError.c_str() : "null handle";
+}
+
+const char* nsfv1_disc_type(const nsfv1_disc*) { return "fv1"; }
+
+#define NSFV1_H Disc* D = reinterpret_cast<Disc*>(h); if (!D) return NSFV1_ERR_ARGUMENT; D->status = NSFV1_OK
+
+int nsfv1_set_kinematic_viscosity(nsfv1_disc* h, double nu) { NSFV1_H; D->nu = nu; D->viscoSet = true; return NSFV1_OK; }
+int nsfv1_set_density(nsfv1_disc* h, double rho) { NSFV1_H; D->rho = rho; return NSFV1_OK; }
+int nsfv1_set_source(nsfv1_disc* h, const double* f, int n) {
+    NSFV1_H;
+    if (!f || n != D->dim) { D->fail(NSFV1_ERR_ARGUMENT, "set_source: need exactly dim components"); return D->status; }
+    D->hasSource = 1;
+    for (int d = 0; d < 3; ++d) D->src[d] = d < n ? f[d] : 0.0;
+    return NSFV1_OK;
+}
+int nsfv1_set_exact_jacobian(nsfv1_disc* h, double factor) { NSFV1_H; D->fullNewton = factor; return NSFV1_OK; }
+int nsfv1_set_stokes(nsfv1_disc* h, int on) { NSFV1_H; D->stokes = on ? 1 : 0; return NSFV1_OK; }
+int nsfv1_set_laplace(nsfv1_disc* h, int on) { NSFV1_H; D->laplace = on ? 1 : 0; return NSFV1_OK; }
+int nsfv1_set_peclet_blend(nsfv1_disc* h, int on) { NSFV1_H; D->peclet = on ? 1 : 0; return NSFV1_OK; }
+
+int nsfv1_set_upwind(nsfv1_disc* h, const char* name) {
+    NSFV1_H;
+    const int t = upwind_id(name);
+    if (t < 0) {
+        D->fail(NSFV1_ERR_ARGUMENT, std::string("NavierStokes: upwind type '") + (name ? name : "") +
+                "' not found. Options are: no, full, skewed, LinearProfileSkewed (lps)");
+        return D->status;
+    }
+    // navier_stokes_fv1.h:213-215: a new upwind object for the convection; a
+    // stabilisation without an upwind gets this object, one that already has an
+    // upwind keeps its (possibly previously shared) object and type
+    D->convUpwindType = t; D->convUpwindSet = true;
+    if (D->stabSet && D->stabUpwindType < 0) { D->stabUpwindType = t; D->stabSharesConv = true; }
+    else D->stabSharesConv = false;
+    return NSFV1_OK;
+}
+
+int nsfv1_set_stabilization(nsfv1_disc* h, const char* name, const char* diff_length) {
+    NSFV1_H;
+    const int t = stab_id(name);
+    if (t < 0) {
+        D->fail(NSFV1_ERR_ARGUMENT, std::string("NavierStokes: stabilization type '") + (name ? name : "") +
+                "' not a valid name of a Schneider-Raw stabilization. Options are: fields, flow");
+        return D->status;
+    }
+    const int dl = diff_length ? difflen_id(diff_length) : DL_RAW;
+    if (dl < 0) {
+        D->fail(NSFV1_ERR_ARGUMENT, "Diffusion Length calculation method not found. Use one of [Raw, Fivepoint, Cor].");
+        return D->status;
+    }
+    D->stabType = t; D->diffLen = dl; D->stabSet = true;
+    // a new stabilisation object: it takes the convection upwind if one is set (navier_stokes_fv1.h:192,199)
+    if (D->convUpwindSet) { D->stabUpwindType = D->convUpwindType; D->stabSharesConv = true; }
+    else { D->stabUpwindType = -1; D->stabSharesConv = false; }
+    return NSFV1_OK;
+}
+
+int nsfv1_set_stabilization_upwind(nsfv1_disc* h, const char* name) {
+    NSFV1_H;
+    const int t = upwind_id(name);
+    if (t < 0) { D->fail(NSFV1_ERR_ARGUMENT, std::string("NavierStokes: upwind type '") + (name ? name : "") + "' not found."); return D->status; }
+    if (!D->stabSet) { D->fail(NSFV1_ERR_STATE, "Stabilization has not been set."); return D->status; }
+    D->stabUpwindType = t; D->stabSharesConv = false;
+    return NSFV1_OK;
+}
+
+int nsfv1_set_mesh(nsfv1_disc* h, int elem_type, int64_t n_nodes, const double* coords, int64_t n_elems, const int32_t* conn) {
+    NSFV1_H;
+    try {
+        const int dim = ref_dim(elem_type), nsh = ref_nsh(elem_type);
+        if (dim == 0) { D->fail(NSFV1_ERR_ARGUMENT, "unsupported element type"); return D->status; }
+        if (dim != D->dim) { D->fail(NSFV1_ERR_ARGUMENT, "element dimension does not match the disc"); return D->status; }
+        if (n_nodes <= 0 || n_elems <= 0 || !coords || !conn) { D->fail(NSFV1_ERR_ARGUMENT, "empty mesh"); return D->status; }
+        if (n_nodes >= (int64_t(1) << 31) / 4 || n_elems * nsh * nsh >= (int64_t(1) << 31)) { D->fail(NSFV1_ERR_ARGUMENT, "mesh too large for 32-bit indices"); return D->status; }
+        for (int64_t k = 0; k < n_elems * nsh; ++k)
+            if (conn[k] < 0 || conn[k] >= n_nodes) { D->fail(NSFV1_ERR_ARGUMENT, "connectivity out of range"); return D->status; }
+        D->free_mesh();
+        D->hasMesh = false;
+        D->roid = elem_type; D->nsh = nsh; D->nNodes = n_nodes; D->nElems = n_elems;
+        build_pattern(nsh, n_nodes, n_elems, conn, D->rowPtr, D->colIdx, D->elemBlk);
+        D->nColors = build_coloring(nsh, n_nodes, n_elems, conn, D->color);
+        if (D->nColors < 0) { D->fail(NSFV1_ERR_ARGUMENT, "too many element colours"); return D->status; }
+        D->colorPtr.assign(D->nColors + 1, 0);
+        for (int64_t e = 0; e < n_elems; ++e) D->colorPtr[D->color[e] + 1]++;
+        for (int c = 0; c < D->nColors; ++c) D->colorPtr[c + 1] += D->colorPtr[c];
+        D->colorElems.resize(n_elems);
+        {
+            std::vector<int32_t> f(D->colorPtr.begin(), D->colorPtr.end() - 1);
+            for (int64_t e = 0; e < n_elems; ++e) D->colorElems[f[D->color[e]]++] = (int32_t)e;
+        }
+        if (!D->cuda_ok(dupload(D->d_coords, coords, (size_t)n_nodes * dim), "upload coords") ||
+            !D->cuda_ok(dupload(D->d_conn, conn, (size_t)n_elems * nsh), "upload conn") ||
+            !D->cuda_ok(dupload(D->d_elemBlk, D->elemBlk.data(), D->elemBlk.size()), "upload elemBlk") ||
+            !D->cuda_ok(dupload(D->d_colorElems, D->colorElems.data(), D->colorElems.size()), "upload colours") ||
+            !D->cuda_ok(dupload(D->d_rowPtr, D->rowPtr.data(), D->rowPtr.size()), "upload rowPtr") ||
+            !D->cuda_ok(dupload(D->d_colIdx, D->colIdx.data(), D->colIdx.size()), "upload colIdx"))
+            return D->status;
+        if (!D->d_err) {
+            if (!D->cuda_ok(cudaMalloc((void**)&D->d_err, sizeof(int)), "alloc err")) return D->status;
+        }
+        if (!D->cuda_ok(cudaMemset(D->d_err, 0, sizeof(int)), "memset err")) return D->status;
+        D->nDir = 0;
+        D->free_workspace();
+        D->hasMesh = true;
+        return NSFV1_OK;
+    } catch (std::exception& ex) {
+        D->fail(NSFV1_ERR_ARGUMENT, ex.what());
+        return D->status;
+    }
+}
+
+int nsfv1_pattern_info(const nsfv1_disc* h, int64_t* n_rows, int64_t* nnz_blocks, int* block_size, int* n_colors) {
+    const Disc* D = reinterpret_cast<const Disc*>(h);
+    if (!D || !D->hasMesh) return NSFV1_ERR_STATE;
+    if (n_rows) *n_rows = D->nNodes;
+    if (nnz_blocks) *nnz_blocks = (int64_t)D->colIdx.size();
+    if (block_size) *block_size = D->dim + 1;
+    if (n_colors) *n_colors = D->nColors;
+    return NSFV1_OK;
+}
+
+int nsfv1_mesh_pattern(int elem_type, int64_t n_nodes, int64_t n_elems, const int32_t* conn, int64_t* nnz_blocks,
+                       int* n_colors, int32_t* row_ptr, int32_t* col_idx, int32_t* elem_color) {
+    const int nsh = ref_nsh(elem_type);
+    if (nsh == 0 || n_nodes <= 0 || n_elems <= 0 || !conn) return NSFV1_ERR_ARGUMENT;
+    for (int64_t k = 0; k < n_elems * nsh; ++k)
+        if (conn[k] < 0 || conn[k] >= n_nodes) return NSFV1_ERR_ARGUMENT;
+    try {
+        std::vector<int32_t> rp, ci, eb, col;
+        build_pattern(nsh, n_nodes, n_elems, conn, rp, ci, eb);
+        const int nc = build_coloring(nsh, n_nodes, n_elems, conn, col);
+        if (nc < 0) return NSFV1_ERR_ARGUMENT;
+        if (nnz_blocks) *nnz_blocks = (int64_t)ci.size();
+        if (n_colors) *n_colors = nc;
+        if (row_ptr) std::copy(rp.begin(), rp.end(), row_ptr);
+        if (col_idx) std::copy(ci.begin(), ci.end(), col_idx);
+        if (elem_color) std::copy(col.begin(), col.end(), elem_color);
+        return NSFV1_OK;
+    } catch (...) { return NSFV1_ERR_ARGUMENT; }
+}
+
+int nsfv1_get_pattern(const nsfv1_disc* h, int32_t* row_ptr, int32_t* col_idx) {
+    const Disc* D = reinterpret_cast<const Disc*>(h);
+    if (!D || !D->hasMesh) return NSFV1_ERR_STATE;
+    if (row_ptr) std::copy(D->rowPtr.begin(), D->rowPtr.end(), row_ptr);
+    if (col_idx) std::copy(D->colIdx.begin(), D->colIdx.end(), col_idx);
+    return NSFV1_OK;
+}
+
+int nsfv1_get_coloring(const nsfv1_disc* h, int32_t* elem_color) {
+    const Disc* D = reinterpret_cast<const Disc*>(h);
+    if (!D || !D->hasMesh) return NSFV1_ERR_STATE;
+    std::copy(D->color.begin(), D->color.end(), elem_color);
+    return NSFV1_OK;
+}
+
+int nsfv1_device_pattern(const nsfv1_disc* h, const int32_t** row_ptr, const int32_t** col_idx) {
+    const Disc* D = reinterpret_cast<const Disc*>(h);
+    if (!D || !D->hasMesh) return NSFV1_ERR_STATE;
+    if (row_ptr) *row_ptr = D->d_rowPtr;
+    if (col_idx) *col_idx = D->d_colIdx;
+    return NSFV1_OK;
+}
+
+int nsfv1_set_dirichlet(nsfv1_disc* h, int64_t n, const int32_t* dofs, const double* values) {
+    NSFV1_H;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "set_dirichlet: no mesh"); return D->status; }
+    const int b = D->dim + 1;
+    for (int64_t k = 0; k < n; ++k)
+        if (dofs[k] < 0 || dofs[k] >= D->nNodes * b) { D->fail(NSFV1_ERR_ARGUMENT, "Dirichlet dof out of range"); return D->status; }
+    if (!D->cuda_ok(dupload(D->d_dirRow, dofs, (size_t)n), "upload dirichlet") ||
+        !D->cuda_ok(dupload(D->d_dirVal, values, (size_t)n), "upload dirichlet values"))
+        return D->status;
+    D->nDir = n;
+    return NSFV1_OK;
+}
+
+int nsfv1_assemble_defect(nsfv1_disc* h, const double* u, const double* u_old, double dt, double* d, void* stream) {
+    NSFV1_H;
+    return D->assemble_defect(u, u_old, dt, d, (cudaStream_t)stream) ? NSFV1_OK : D->status;
+}
+
+int nsfv1_assemble_jacobian(nsfv1_disc* h, const double* u, const double* u_old, double dt, void* vals, int prec, void* stream) {
+    NSFV1_H;
+    return D->assemble_jacobian(u, u_old, dt, vals, prec, (cudaStream_t)stream) ? NSFV1_OK : D->status;
+}
+
+int nsfv1_elem_batch(nsfv1_disc* h, int elem_type, int64_t n, const double* corners, const double* u, const double* u_old,
+                     double dt, double* defA, double* jacA, double* defM, double* jacM, double* rhs, void* stream) {
+    NSFV1_H;
+    if (ref_dim(elem_type) != D->dim) { D->fail(NSFV1_ERR_ARGUMENT, "element dimension does not match the disc"); return D->status; }
+    if (n < 0 || (n > 0 && (!corners || !u))) { D->fail(NSFV1_ERR_ARGUMENT, "elem_batch: bad arguments"); return D->status; }
+    DiscParams P;
+    if (!D->params(P, u_old != nullptr, dt)) return D->status;
+    if (!D->d_err) {
+        if (!D->cuda_ok(cudaMalloc((void**)&D->d_err, sizeof(int)), "alloc err")) return D->status;
+        cudaMemset(D->d_err, 0, sizeof(int));
+    }
+    ElemBatchArgs a{n, corners, u, u_old, defA, jacA, defM, jacM, rhs, D->d_err};
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!D->cuda_ok(launch_elem_batch(elem_type, P, a, s), "elem_batch")) return D->status;
+    return D->check_err_word(s) ? NSFV1_OK : D->status;
+}
+
+int nsfv1_ref_tables(int elem_type, int* nco, int* nedge, int* edges, int* nside, int* side_nco, int* sides, int* edge_face) {
+    auto fill = [&](auto r) {
+        using R = Ref<decltype(r)::value>;
+        *nco = R::nsh; *nedge = R::nip; *nside = R::nside;
+        for (int e = 0; e < R::nip; ++e) {
+            edges[2 * e] = R::edge(e, 0); edges[2 * e + 1] = R::edge(e, 1);
+            edge_face[2 * e] = R::dim == 3 ? R::edge_face(e, 0) : -1;
+            edge_face[2 * e + 1] = R::dim == 3 ? R::edge_face(e, 1) : -1;
+        }
+        for (int s = 0; s < R::nside; ++s) {
+            side_nco[s] = R::side_nco(s);
+            for (int j = 0; j < 4; ++j) sides[4 * s + j] = j < R::side_nco(s) ? R::side(s, j) : -1;
+        }
+    };
+    switch (elem_type) {
+        case ROID_TRIANGLE: fill(std::integral_constant<int, ROID_TRIANGLE>{}); return NSFV1_OK;
+        case ROID_QUADRILATERAL: fill(std::integral_constant<int, ROID_QUADRILATERAL>{}); return NSFV1_OK;
+        case ROID_TETRAHEDRON: fill(std::integral_constant<int, ROID_TETRAHEDRON>{}); return NSFV1_OK;
+        case ROID_HEXAHEDRON: fill(std::integral_constant<int, ROID_HEXAHEDRON>{}); return NSFV1_OK;
+    }
+    return NSFV1_ERR_ARGUMENT;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// assembly drivers
+// ============================================================================
+namespace nsfv1 {
+
+bool Disc::assemble_defect(const double* u, const double* u_old, double dt, double* d, cudaStream_t s) {
+    if (!hasMesh) return fail(NSFV1_ERR_STATE, "assemble_defect: no mesh set");
+    if (!u || !d) return fail(NSFV1_ERR_ARGUMENT, "assemble_defect: null vector");
+    DiscParams P;
+    if (!params(P, u_old != nullptr, dt)) return false;
+    const int b = dim + 1;
+    if (!cuda_ok(cudaMemsetAsync(d, 0, sizeof(double) * nNodes * b, s), "memset defect")) return false;
+    for (int c = 0; c < nColors; ++c) {
+        AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, d, nullptr};
+        if (!cuda_ok(launch_defect(roid, P, a, s), "defect kernel")) return false;
+    }
+    if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, d, nullptr, 0, s), "dirichlet")) return false;
+    return check_err_word(s);
+}
+
+bool Disc::assemble_jacobian(const double* u, const double* u_old, double dt, void* vals, int prec, cudaStream_t s, bool sync) {
+    if (!hasMesh) return fail(NSFV1_ERR_STATE, "assemble_jacobian: no mesh set");
+    if (!u || !vals) return fail(NSFV1_ERR_ARGUMENT, "assemble_jacobian: null pointer");
+    if (prec != NSFV1_F64 && prec != NSFV1_F32) return fail(NSFV1_ERR_ARGUMENT, "assemble_jacobian: precision must be NSFV1_F64 or NSFV1_F32");
+    DiscParams P;
+    if (!params(P, u_old != nullptr, dt)) return false;
+    const int b = dim + 1;
+    const size_t bytes = colIdx.size() * b * b * (prec == NSFV1_F64 ? sizeof(double) : sizeof(float));
+    if (!cuda_ok(cudaMemsetAsync(vals, 0, bytes, s), "memset jacobian")) return false;
+    for (int c = 0; c < nColors; ++c) {
+        AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, nullptr, vals};
+        if (!cuda_ok(launch_jacobian(roid, P, a, prec, s), "jacobian kernel")) return false;
+    }
+    if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, nullptr, vals, prec, s), "dirichlet")) return false;
+    return sync ? check_err_word(s) : true;
+}
+
+}  // namespace nsfv1

@@ -1,0 +1,853 @@
+// Per-element FV1 Navier-Stokes math for the sm_103a kernels: the SCVF/SCV
+// geometry, the convective upwind shapes, the stabilised velocity and the
+// local defect / Jacobian contributions, computed in registers by one thread
+// per element.
+//
+// Reference behaviour followed (file:line in UG4 plugin_NavierStokes):
+//   add_def_A_elem            incompressible/fv1/navier_stokes_fv1.cpp:597-778
+//   add_jac_A_elem            incompressible/fv1/navier_stokes_fv1.cpp:250-595
+//   add_def_M_elem/jac_M      incompressible/fv1/navier_stokes_fv1.cpp:781-838
+//   add_rhs_elem              incompressible/fv1/navier_stokes_fv1.cpp:841-869
+//   peclet_blend              incompressible/fv1/navier_stokes_fv1.cpp:871-892
+//   FIELDS / FLOW / without   incompressible/fv1/stabilization.cpp:122-241, 436-588, 805-850
+//   diffusion lengths         incompressible/fv1/diffusion_length.h:48-199
+//   no / full / skewed / LPS  upwind.cpp:52-80, 133-172, 337-430, 505-575
+//   upwind_vel, downwind      upwind_interface.h:150-165, 333-358
+//
+// The stabilised velocity and the continuity-row Jacobian are evaluated in a
+// regrouped but algebraically identical form: sum_k (a N_k + b U_k) u_k is
+// computed as a StdVel + b UpVel, and the FLOW cross terms collapse to
+// (S_k - V.g_k) n + (V.n) g_k. Results agree with the term-by-term reference
+// order to rounding (the parity tests hold them to 1e-12 relative in FP64).
+//
+// The SCVF loop runs over a warp-uniform runtime index: per-SCVF constants
+// (shapes and local gradients at the integration points, edge/face/side
+// tables) come from __constant__ tables (broadcast loads), corner data with a
+// runtime index is selected from registers without local-memory indexing.
+#pragma once
+#include <cstdint>
+#include "nsfv1_params.h"
+#include "nsfv1_refelem.cuh"
+
+namespace nsfv1 {
+
+// ---------------------------------------------------------------------------
+// per-element-type tables (generated at compile time from nsfv1_refelem.cuh)
+// ---------------------------------------------------------------------------
+struct ElemTab {
+    double ipShape[12][8];
+    double ipLGrad[12][8][3];
+    double refCo[8][3];
+    int edge[12][2];
+    int edgeFace[12][2];
+    int side[6][4];
+    int sideNco[6];
+    int sideMask[6];   // bit k set: corner k belongs to the side
+};
+
+template <int ROID> constexpr ElemTab make_tab() {
+    using R = Ref<ROID>;
+    ElemTab t{};
+    for (int ip = 0; ip < R::nip; ++ip) {
+        for (int k = 0; k < R::nsh; ++k) {
+            t.ipShape[ip][k] = ip_shape<ROID>(ip, k);
+            for (int d = 0; d < R::dim; ++d) t.ipLGrad[ip][k][d] = ip_lgrad<ROID>(ip, k, d);
+        }
+        t.edge[ip][0] = R::edge(ip, 0); t.edge[ip][1] = R::edge(ip, 1);
+        t.edgeFace[ip][0] = R::edge_face(ip, 0); t.edgeFace[ip][1] = R::edge_face(ip, 1);
+    }
+    for (int c = 0; c < R::nsh; ++c)
+        for (int d = 0; d < 3; ++d) t.refCo[c][d] = d < R::dim ? R::co(c, d) : 0.0;
+    for (int s = 0; s < R::nside; ++s) {
+        t.sideNco[s] = R::side_nco(s);
+        int m = 0;
+        for (int j = 0; j < 4; ++j) {
+            t.side[s][j] = j < R::side_nco(s) ? R::side(s, j) : R::side(s, 0);
+            if (j < R::side_nco(s)) m |= 1 << R::side(s, j);
+        }
+        t.sideMask[s] = m;
+    }
+    return t;
+}
+
+static __constant__ ElemTab c_tabTri = make_tab<ROID_TRIANGLE>();
+static __constant__ ElemTab c_tabQuad = make_tab<ROID_QUADRILATERAL>();
+static __constant__ ElemTab c_tabTet = make_tab<ROID_TETRAHEDRON>();
+static __constant__ ElemTab c_tabHex = make_tab<ROID_HEXAHEDRON>();
+
+template <int ROID> __device__ __forceinline__ const ElemTab& tab() {
+    if constexpr (ROID == ROID_TRIANGLE) return c_tabTri;
+    else if constexpr (ROID == ROID_QUADRILATERAL) return c_tabQuad;
+    else if constexpr (ROID == ROID_TETRAHEDRON) return c_tabTet;
+    else return c_tabHex;
+}
+
+template <typename T> struct Num;
+template <> struct Num<double> {
+    static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+    static __device__ __forceinline__ double abs_(double x) { return fabs(x); }
+};
+template <> struct Num<float> {
+    static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ float abs_(float x) { return fabsf(x); }
+};
+
+// ---------------------------------------------------------------------------
+// Element-level geometry shared by all SCVFs: corners, centre, face centres,
+// SCV volumes.
+// ---------------------------------------------------------------------------
+template <int ROID, typename T>
+struct Elem {
+    using R = Ref<ROID>;
+    static constexpr int dim = R::dim, nsh = R::nsh, nip = R::nip, b = R::b, nside = R::nside;
+    T x[nsh][dim];
+    T cen[dim];
+    T face[nside][dim];
+    T vol[nsh];
+};
+
+// corner 'i' (runtime index) of a register array, by selects (no local memory)
+template <int N, int D, typename T>
+__device__ __forceinline__ void pick(const T (&a)[N][D], const int i, T* out) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        T v = a[0][d];
+#pragma unroll
+        for (int k = 1; k < N; ++k) v = (k == i) ? a[k][d] : v;
+        out[d] = v;
+    }
+}
+
+template <typename T> __device__ __forceinline__ T tet6(const T* a, const T* b, const T* c, const T* d) {
+    T u[3], v[3], w[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { u[k] = b[k] - a[k]; v[k] = c[k] - a[k]; w[k] = d[k] - a[k]; }
+    const T x0 = v[1] * w[2] - v[2] * w[1];
+    const T x1 = v[2] * w[0] - v[0] * w[2];
+    const T x2 = v[0] * w[1] - v[1] * w[0];
+    return u[0] * x0 + u[1] * x1 + u[2] * x2;
+}
+
+template <int ROID, typename T>
+__device__ __forceinline__ void elem_setup(Elem<ROID, T>& E) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh;
+#pragma unroll
+    for (int d = 0; d < dim; ++d) {
+        T s = T(0);
+#pragma unroll
+        for (int c = 0; c < nsh; ++c) s += E.x[c][d];
+        E.cen[d] = s * T(1.0 / nsh);
+    }
+    if constexpr (dim == 3) {
+#pragma unroll
+        for (int f = 0; f < R::nside; ++f)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                T s = T(0);
+#pragma unroll
+                for (int j = 0; j < R::side_nco(f); ++j) s += E.x[R::side(f, j)][d];
+                E.face[f][d] = s * T(1.0 / R::side_nco(f));
+            }
+    }
+    // SCV volumes
+#pragma unroll
+    for (int a = 0; a < nsh; ++a) {
+        if constexpr (dim == 2) {
+            const int nxt = a;                    // edge a starts at corner a
+            const int prv = (a + nsh - 1) % nsh;  // edge a-1 ends at corner a
+            T p1[2], p3[2];
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                p1[d] = T(0.5) * (E.x[R::edge(nxt, 0)][d] + E.x[R::edge(nxt, 1)][d]);
+                p3[d] = T(0.5) * (E.x[R::edge(prv, 0)][d] + E.x[R::edge(prv, 1)][d]);
+            }
+            const T cr = (E.cen[0] - E.x[a][0]) * (p3[1] - p1[1]) - (E.cen[1] - E.x[a][1]) * (p3[0] - p1[0]);
+            E.vol[a] = T(0.5) * Num<T>::abs_(cr);
+        } else {
+            T q1[3], q2[3], q3[3], q4[3], q5[3], q7[3];
+            const int e0 = R::scv_tab(a, 0), f01 = R::scv_tab(a, 1), e1 = R::scv_tab(a, 2);
+            const int e2 = R::scv_tab(a, 3), f02 = R::scv_tab(a, 4), f12 = R::scv_tab(a, 5);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                q1[d] = T(0.5) * (E.x[R::edge(e0, 0)][d] + E.x[R::edge(e0, 1)][d]);
+                q3[d] = T(0.5) * (E.x[R::edge(e1, 0)][d] + E.x[R::edge(e1, 1)][d]);
+                q4[d] = T(0.5) * (E.x[R::edge(e2, 0)][d] + E.x[R::edge(e2, 1)][d]);
+                q2[d] = E.face[f01][d]; q5[d] = E.face[f02][d]; q7[d] = E.face[f12][d];
+            }
+            const T* q0 = E.x[a];
+            const T* q6 = E.cen;
+            const T s6 = tet6(q0, q1, q2, q6) + tet6(q0, q2, q3, q6) + tet6(q0, q3, q7, q6)
+                       + tet6(q0, q7, q4, q6) + tet6(q0, q4, q5, q6) + tet6(q0, q5, q1, q6);
+            E.vol[a] = Num<T>::abs_(s6) / T(6.0);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-SCVF geometry: normal, global ip, corners, J^-T at the local ip.
+// ---------------------------------------------------------------------------
+template <typename T> struct IpGeo {
+    int from, to;
+    T n[3], gip[3], em[3], xf[3], xt[3];
+    T JtInv[3][3];
+};
+
+template <int ROID, typename T>
+__device__ __forceinline__ void ip_geom(const Elem<ROID, T>& E, const int ip, IpGeo<T>& G) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh;
+    const ElemTab& tb = tab<ROID>();
+    G.from = tb.edge[ip][0]; G.to = tb.edge[ip][1];
+    pick(E.x, G.from, G.xf);
+    pick(E.x, G.to, G.xt);
+#pragma unroll
+    for (int d = 0; d < dim; ++d) G.em[d] = T(0.5) * (G.xf[d] + G.xt[d]);
+    if constexpr (dim == 2) {
+        const T dx = E.cen[0] - G.em[0], dy = E.cen[1] - G.em[1];
+        G.n[0] = dy; G.n[1] = -dx; G.n[2] = T(0);
+#pragma unroll
+        for (int d = 0; d < 2; ++d) G.gip[d] = (G.em[d] + E.cen[d]) * T(0.5);
+        G.gip[2] = T(0);
+    } else {
+        T f1[3], f2[3];
+        pick(E.face, tb.edgeFace[ip][0], f1);
+        pick(E.face, tb.edgeFace[ip][1], f2);
+        T a[3], c[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) { a[d] = E.cen[d] - G.em[d]; c[d] = f2[d] - f1[d]; }
+        G.n[0] = T(0.5) * (a[1] * c[2] - a[2] * c[1]);
+        G.n[1] = T(0.5) * (a[2] * c[0] - a[0] * c[2]);
+        G.n[2] = T(0.5) * (a[0] * c[1] - a[1] * c[0]);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) G.gip[d] = (G.em[d] + f1[d] + E.cen[d] + f2[d]) * T(0.25);
+    }
+    // Jacobian of the reference mapping at the local ip
+    T J[3][3];
+#pragma unroll
+    for (int r = 0; r < dim; ++r)
+#pragma unroll
+        for (int c = 0; c < dim; ++c) {
+            T s = T(0);
+#pragma unroll
+            for (int k = 0; k < nsh; ++k) s += E.x[k][r] * T(tb.ipLGrad[ip][k][c]);
+            J[r][c] = s;
+        }
+    if constexpr (dim == 2) {
+        const T det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        const T id = T(1) / det;
+        G.JtInv[0][0] = J[1][1] * id;  G.JtInv[0][1] = -J[1][0] * id;
+        G.JtInv[1][0] = -J[0][1] * id; G.JtInv[1][1] = J[0][0] * id;
+    } else {
+        T C[3][3];
+        C[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        C[0][1] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        C[0][2] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        C[1][0] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+        C[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+        C[1][2] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+        C[2][0] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+        C[2][1] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+        C[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        const T det = J[0][0] * C[0][0] + J[0][1] * C[0][1] + J[0][2] * C[0][2];
+        const T id = T(1) / det;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) G.JtInv[i][j] = C[i][j] * id;
+    }
+}
+
+// global gradient of shape k at the SCVF ip
+template <int ROID, typename T>
+__device__ __forceinline__ void ip_grad(const IpGeo<T>& G, const int ip, const int k, T g[3]) {
+    constexpr int dim = Ref<ROID>::dim;
+    const ElemTab& tb = tab<ROID>();
+#pragma unroll
+    for (int r = 0; r < dim; ++r) {
+        T s = T(0);
+#pragma unroll
+        for (int c = 0; c < dim; ++c) s += G.JtInv[r][c] * T(tb.ipLGrad[ip][k][c]);
+        g[r] = s;
+    }
+}
+
+template <int ROID, typename T>
+__device__ __forceinline__ T ipN(const int ip, const int k) { return T(tab<ROID>().ipShape[ip][k]); }
+
+// ---------------------------------------------------------------------------
+// Upwind shapes of one SCVF (INavierStokesUpwind::compute, upwind.cpp)
+// ---------------------------------------------------------------------------
+template <typename T, int dim> __device__ __forceinline__ T dist(const T* a, const T* b) {
+    T s = T(0);
+#pragma unroll
+    for (int d = 0; d < dim; ++d) { const T x = a[d] - b[d]; s += x * x; }
+    return Num<T>::sqrt_(s);
+}
+
+// Ray from 'from' along 'dir' against the element sides in reference order
+// (quadrilateral faces as triangles (0,1,2), (0,2,3)); the first side hit with
+// t <= 0 is the upwind side (ElementSideRayIntersection, restated). LPS takes
+// the element P1 shapes of the side corners at the local intersection, skewed
+// the side corner nearest to the intersection. Returns false when no side is
+// found (the reference throws).
+template <int ROID, typename T>
+__device__ __forceinline__ bool ray_upwind(const Elem<ROID, T>& E, const T* from, const T* dir, const bool lps,
+                                           T (&up)[Ref<ROID>::nsh], T& convLen) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh;
+    const ElemTab& tb = tab<ROID>();
+    const T tol = T(1e-12);
+    int hitSide = -1;
+    T gInt[3] = {T(0), T(0), T(0)}, lInt[3] = {T(0), T(0), T(0)};
+#pragma unroll 1
+    for (int s = 0; s < R::nside && hitSide < 0; ++s) {
+        constexpr int ntri = (dim == 3 && R::side_nco(0) == 4) ? 2 : 1;
+#pragma unroll
+        for (int tr = 0; tr < ntri; ++tr) {
+            if (hitSide >= 0) break;
+            if constexpr (dim == 2) {
+                const int i0 = tb.side[s][0], i1 = tb.side[s][1];
+                T p0[2], p1[2];
+                pick(E.x, i0, p0);
+                pick(E.x, i1, p1);
+                const T a00 = p1[0] - p0[0], a01 = -dir[0];
+                const T a10 = p1[1] - p0[1], a11 = -dir[1];
+                const T det = a00 * a11 - a01 * a10;
+                if (det != T(0)) {
+                    const T r0 = from[0] - p0[0], r1 = from[1] - p0[1];
+                    const T bc = (r0 * a11 - a01 * r1) / det;
+                    const T t = (a00 * r1 - r0 * a10) / det;
+                    if (!(bc < -tol || bc > T(1) + tol) && t <= T(0)) {
+                        hitSide = s;
+#pragma unroll
+                        for (int d = 0; d < 2; ++d) {
+                            gInt[d] = p0[d] + bc * (p1[d] - p0[d]);
+                            lInt[d] = T(tb.refCo[i0][d]) + bc * (T(tb.refCo[i1][d]) - T(tb.refCo[i0][d]));
+                        }
+                    }
+                }
+            } else {
+                const int i0 = tb.side[s][0];
+                const int i1 = tb.side[s][tr == 0 ? 1 : 2];
+                const int i2 = tb.side[s][tr == 0 ? 2 : 3];
+                T q0[3], q1[3], q2[3];
+                pick(E.x, i0, q0);
+                pick(E.x, i1, q1);
+                pick(E.x, i2, q2);
+                T e1[3], e2[3], nd[3], r[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) { e1[d] = q1[d] - q0[d]; e2[d] = q2[d] - q0[d]; nd[d] = -dir[d]; r[d] = from[d] - q0[d]; }
+                const T c0 = e2[1] * nd[2] - e2[2] * nd[1];
+                const T c1 = e2[2] * nd[0] - e2[0] * nd[2];
+                const T c2 = e2[0] * nd[1] - e2[1] * nd[0];
+                const T det = e1[0] * c0 + e1[1] * c1 + e1[2] * c2;
+                if (det != T(0)) {
+                    const T a = (r[0] * c0 + r[1] * c1 + r[2] * c2) / det;
+                    const T w0 = r[1] * nd[2] - r[2] * nd[1];
+                    const T w1 = r[2] * nd[0] - r[0] * nd[2];
+                    const T w2 = r[0] * nd[1] - r[1] * nd[0];
+                    const T bb = (e1[0] * w0 + e1[1] * w1 + e1[2] * w2) / det;
+                    const T v0 = e2[1] * r[2] - e2[2] * r[1];
+                    const T v1 = e2[2] * r[0] - e2[0] * r[2];
+                    const T v2 = e2[0] * r[1] - e2[1] * r[0];
+                    const T t = (e1[0] * v0 + e1[1] * v1 + e1[2] * v2) / det;
+                    if (!(a < -tol || bb < -tol || a + bb > T(1) + tol) && t <= T(0)) {
+                        hitSide = s;
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            gInt[d] = q0[d] + a * e1[d] + bb * e2[d];
+                            lInt[d] = T(tb.refCo[i0][d]) + a * (T(tb.refCo[i1][d]) - T(tb.refCo[i0][d]))
+                                    + bb * (T(tb.refCo[i2][d]) - T(tb.refCo[i0][d]));
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (hitSide < 0) return false;
+    const int mask = tb.sideMask[hitSide];
+    if (lps) {
+#pragma unroll
+        for (int k = 0; k < nsh; ++k) {
+            T v;
+            if constexpr (ROID == ROID_TRIANGLE) v = (k == 0) ? T(1) - lInt[0] - lInt[1] : (k == 1 ? lInt[0] : lInt[1]);
+            else if constexpr (ROID == ROID_TETRAHEDRON) v = (k == 0) ? T(1) - lInt[0] - lInt[1] - lInt[2] : lInt[k - 1];
+            else if constexpr (ROID == ROID_QUADRILATERAL) {
+                const T xa = (k == 1 || k == 2) ? lInt[0] : T(1) - lInt[0];
+                const T xb = (k == 2 || k == 3) ? lInt[1] : T(1) - lInt[1];
+                v = xa * xb;
+            } else {
+                const T xa = (k == 1 || k == 2 || k == 5 || k == 6) ? lInt[0] : T(1) - lInt[0];
+                const T xb = (k == 2 || k == 3 || k == 6 || k == 7) ? lInt[1] : T(1) - lInt[1];
+                const T xc = (k >= 4) ? lInt[2] : T(1) - lInt[2];
+                v = xa * xb * xc;
+            }
+            up[k] = ((mask >> k) & 1) ? v : T(0);
+        }
+        convLen = dist<T, dim>(from, gInt);
+    } else {
+        // nearest side corner (GetNodeNextToCut, strict '<' keeps the first in side order)
+        T mn = T(3.0e38);
+        int coOut = tb.side[hitSide][0];
+        const int nco = tb.sideNco[hitSide];
+#pragma unroll 1
+        for (int j = 0; j < nco; ++j) {
+            const int co = tb.side[hitSide][j];
+            T xc[3];
+            pick(E.x, co, xc);
+            T dd = T(0);
+#pragma unroll
+            for (int d = 0; d < dim; ++d) { const T x = gInt[d] - xc[d]; dd += x * x; }
+            if (dd < mn) { mn = dd; coOut = co; }
+        }
+#pragma unroll
+        for (int k = 0; k < nsh; ++k) up[k] = (k == coOut) ? T(1) : T(0);
+        T xo[3];
+        pick(E.x, coOut, xo);
+        convLen = dist<T, dim>(from, xo);
+    }
+    return true;
+}
+
+// Upwind shapes and convection length of SCVF 'ip' for IP velocity 'vel'.
+// Returns false if a skewed / LPS ray finds no side.
+template <int ROID, typename T>
+__device__ __forceinline__ bool upwind_shapes(const int type, const Elem<ROID, T>& E, const IpGeo<T>& G, const int ip,
+                                              const T* vel, T (&up)[Ref<ROID>::nsh], T& convLen) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh;
+    if (type == UPW_NO) {
+#pragma unroll
+        for (int k = 0; k < nsh; ++k) up[k] = ipN<ROID, T>(ip, k);
+        convLen = T(1);
+        return true;
+    }
+    if (type == UPW_FULL) {
+        T flux = T(0);
+#pragma unroll
+        for (int d = 0; d < dim; ++d) flux += G.n[d] * vel[d];
+        const bool f = flux > T(0);
+        const int co = f ? G.from : G.to;
+#pragma unroll
+        for (int k = 0; k < nsh; ++k) up[k] = (k == co) ? T(1) : T(0);
+        convLen = dist<T, dim>(G.gip, f ? G.xf : G.xt);
+        return true;
+    }
+    // skewed / LPS
+    T vv = T(0);
+#pragma unroll
+    for (int d = 0; d < dim; ++d) vv += vel[d] * vel[d];
+    if (Num<T>::sqrt_(vv) < T(1e-14)) {
+#pragma unroll
+        for (int k = 0; k < nsh; ++k) up[k] = T(0);
+        convLen = T(1);
+        return true;
+    }
+    return ray_upwind<ROID, T>(E, G.gip, vel, type == UPW_LPS, up, convLen);
+}
+
+// ---------------------------------------------------------------------------
+// Diffusion length 1/L^2 of one SCVF (RAW / FIVEPOINT; COR uses element-wide
+// minima, passed in).
+// ---------------------------------------------------------------------------
+template <int ROID, typename T>
+__device__ __forceinline__ T diff_len_sq_inv(const int type, const Elem<ROID, T>& E, const IpGeo<T>& G,
+                                            const T corMinN, const T corMinD, const T corAvgN) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh;
+    T nn = T(0);
+#pragma unroll
+    for (int d = 0; d < dim; ++d) nn += G.n[d] * G.n[d];
+    T vf = E.vol[0], vt = E.vol[0];
+#pragma unroll
+    for (int k = 1; k < nsh; ++k) { vf = (k == G.from) ? E.vol[k] : vf; vt = (k == G.to) ? E.vol[k] : vt; }
+    T area = T(0.5) * (vf + vt);
+    area *= area;
+    if (type == DL_COR) {
+        if constexpr (dim == 2) return T(2.0) * corMinN / area + T(8.0) / (T(3.0) * corAvgN);
+        else return T(2.0) * corMinN / area + T(8.0) * corMinD / (T(3.0) * corAvgN);
+    }
+    T ds = T(0);
+    if constexpr (dim == 3) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) { const T x = G.em[d] - E.cen[d]; ds += x * x; }
+    }
+    if (type == DL_FIVEPOINT) {
+        if constexpr (dim == 2) return T(2.0) * nn / area + T(8.0) / nn;
+        else return T(2.0) * nn / area + T(8.0) * ds / nn;
+    }
+    if constexpr (dim == 2) return T(1.0) / (T(0.5) * area / nn + T(3.0) * nn / T(8.0));
+    else return T(1.0) / (T(0.5) * area / nn + T(3.0) * ds / T(8.0));
+}
+
+template <int ROID, typename T>
+__device__ __forceinline__ void cor_data(const Elem<ROID, T>& E, T& minN, T& minD, T& avgN) {
+    using R = Ref<ROID>;
+    minN = T(3.0e38); minD = T(3.0e38); avgN = T(0);
+#pragma unroll 1
+    for (int ip = 0; ip < R::nip; ++ip) {
+        IpGeo<T> G;
+        ip_geom<ROID, T>(E, ip, G);
+        T nn = T(0);
+#pragma unroll
+        for (int d = 0; d < R::dim; ++d) nn += G.n[d] * G.n[d];
+        minN = nn < minN ? nn : minN;
+        avgN += nn;
+        if constexpr (R::dim == 3) {
+            T ds = T(0);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) { const T x = G.em[d] - E.cen[d]; ds += x * x; }
+            minD = ds < minD ? ds : minD;
+        }
+    }
+    avgN = avgN / T(R::nip);
+}
+
+// ---------------------------------------------------------------------------
+// Per-SCVF state shared by the defect and the Jacobian
+// ---------------------------------------------------------------------------
+template <int ROID, typename T>
+struct IpState {
+    static constexpr int nsh = Ref<ROID>::nsh;
+    T StdVel[3];
+    T upC[nsh];         // convection upwind shapes
+    T upS[nsh];         // stabilisation upwind shapes
+    T dnS[nsh];         // stabilisation downwind shapes (FLOW)
+    T nuL;              // nu / L_diff^2
+    T nsvcl, nsvdl;     // |v| / L_up ; |v| / (L_down + L_up)
+    T diag;
+    bool ok;
+};
+
+// Upwind / stabilisation coefficients of one SCVF.
+template <int ROID, typename T>
+__device__ __forceinline__ void ip_state(const DiscParams& P, const Elem<ROID, T>& E, const IpGeo<T>& G, const int ip,
+                                         const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh], const T corMinN, const T corMinD, const T corAvgN,
+                                         IpState<ROID, T>& S) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh;
+    S.ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) S.StdVel[d] = T(0);
+#pragma unroll
+    for (int sh = 0; sh < nsh; ++sh) {
+        const T N = ipN<ROID, T>(ip, sh);
+#pragma unroll
+        for (int d = 0; d < dim; ++d) S.StdVel[d] += u[d][sh] * N;
+    }
+    const bool stokes = P.stokes != 0;
+    T Lup = T(1), Ldown = T(1);
+#pragma unroll
+    for (int k = 0; k < nsh; ++k) { S.upS[k] = T(0); S.dnS[k] = T(0); S.upC[k] = T(0); }
+    if (!stokes) {
+        // the stabilisation's upwind (and downwind for FLOW) first, then the
+        // convection's own upwind when it is a different object
+        const int nUp = (P.stab == STAB_FLOW ? 2 : 1) + (P.sameUpwind ? 0 : 1);
+#pragma unroll 1
+        for (int w = 0; w < nUp; ++w) {
+            const bool isDown = (w == 1 && P.stab == STAB_FLOW);
+            const bool isConv = (w == nUp - 1 && !P.sameUpwind);
+            T vel[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) vel[d] = isDown ? S.StdVel[d] * T(-1) : S.StdVel[d];
+            T sh[nsh], L;
+            S.ok &= upwind_shapes<ROID, T>(isConv ? P.convUpwind : P.stabUpwind, E, G, ip, vel, sh, L);
+#pragma unroll
+            for (int k = 0; k < nsh; ++k) {
+                if (isConv) S.upC[k] = sh[k];
+                else if (isDown) S.dnS[k] = sh[k];
+                else S.upS[k] = sh[k];
+            }
+            if (!isConv) { if (isDown) Ldown = L; else Lup = L; }
+        }
+        if (P.sameUpwind) {
+#pragma unroll
+            for (int k = 0; k < nsh; ++k) S.upC[k] = S.upS[k];
+        }
+    }
+    S.nuL = T(0); S.nsvcl = T(0); S.nsvdl = T(0); S.diag = T(1);
+    if (P.stab == STAB_WITHOUT) return;
+    const T Linv = diff_len_sq_inv<ROID, T>(P.diffLen, E, G, corMinN, corMinD, corAvgN);
+    S.nuL = T(P.nu) * Linv;
+    if (!stokes) {
+        T vv = T(0);
+#pragma unroll
+        for (int d = 0; d < dim; ++d) vv += S.StdVel[d] * S.StdVel[d];
+        const T norm = Num<T>::sqrt_(vv);
+        S.nsvcl = norm / Lup;
+        if (P.stab == STAB_FLOW) S.nsvdl = norm / (Ldown + Lup);
+    }
+    S.diag = S.nuL;
+    if (P.transient) S.diag += T(1) / T(P.dt);
+    if (!stokes) S.diag += S.nsvcl;
+}
+
+// peclet_blend weight (navier_stokes_fv1.cpp:871-892); blends UpwindVel in place
+template <int ROID, typename T>
+__device__ __forceinline__ T peclet_blend(const IpGeo<T>& G, const T* StdVel, T nu, T* UpwindVel) {
+    constexpr int dim = Ref<ROID>::dim;
+    T vn = T(0), nn = T(0);
+#pragma unroll
+    for (int d = 0; d < dim; ++d) { vn += StdVel[d] * G.n[d]; nn += G.n[d] * G.n[d]; }
+    const T Pe = vn / nn * dist<T, dim>(G.xt, G.xf) / nu;
+    const T Pe2 = Pe * Pe;
+    const T w = Pe2 / (T(5.0) + Pe2);
+#pragma unroll
+    for (int d = 0; d < dim; ++d) UpwindVel[d] = w * UpwindVel[d] + (T(1) - w) * StdVel[d];
+    return w;
+}
+
+// ---------------------------------------------------------------------------
+// Local stiffness defect of one element into dA (fct-major [b][nsh]).
+// Returns false if an upwind ray found no side.
+// ---------------------------------------------------------------------------
+template <int ROID, typename T>
+__device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
+                                           const T (&uo)[Ref<ROID>::b][Ref<ROID>::nsh], T (&dA)[Ref<ROID>::b][Ref<ROID>::nsh]) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh, b = R::b, Pc = dim, nip = R::nip;
+    T corMinN = T(0), corMinD = T(0), corAvgN = T(1);
+    if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, T>(E, corMinN, corMinD, corAvgN);
+    const T rho = T(P.rho), nu = T(P.nu);
+    bool ok = true;
+    T fluxes[nip][b];   // per-SCVF fluxes, scattered to from/to after the loop
+#pragma unroll 1
+    for (int ip = 0; ip < nip; ++ip) {
+        IpGeo<T> G;
+        ip_geom<ROID, T>(E, ip, G);
+        IpState<ROID, T> S;
+        ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, S);
+        ok &= S.ok;
+        // velocity gradient, pressure gradient
+        T gradVel[3][3], gradP[3];
+#pragma unroll
+        for (int d1 = 0; d1 < 3; ++d1) {
+            gradP[d1] = T(0);
+#pragma unroll
+            for (int d2 = 0; d2 < 3; ++d2) gradVel[d1][d2] = T(0);
+        }
+#pragma unroll
+        for (int sh = 0; sh < nsh; ++sh) {
+            T g[3];
+            ip_grad<ROID, T>(G, ip, sh, g);
+#pragma unroll
+            for (int d1 = 0; d1 < dim; ++d1) {
+#pragma unroll
+                for (int d2 = 0; d2 < dim; ++d2) gradVel[d1][d2] += g[d2] * u[d1][sh];
+                gradP[d1] += g[d1] * u[Pc][sh];
+            }
+        }
+        // diffusion
+        T flux[3];
+#pragma unroll
+        for (int d1 = 0; d1 < dim; ++d1) {
+            T s = T(0);
+#pragma unroll
+            for (int d2 = 0; d2 < dim; ++d2) s += gradVel[d1][d2] * G.n[d2];
+            if (!P.laplace) {
+#pragma unroll
+                for (int d2 = 0; d2 < dim; ++d2) s += gradVel[d2][d1] * G.n[d2];
+            }
+            flux[d1] = s * (T(-1.0) * nu * rho);
+        }
+        // convection
+        if (!P.stokes) {
+            T UpwindVel[3];
+#pragma unroll
+            for (int d = 0; d < dim; ++d) {
+                T s = T(0);
+#pragma unroll
+                for (int sh = 0; sh < nsh; ++sh) s += S.upC[sh] * u[d][sh];
+                UpwindVel[d] = s;
+            }
+            if (P.peclet) peclet_blend<ROID, T>(G, S.StdVel, nu, UpwindVel);
+            T prod = T(0);
+#pragma unroll
+            for (int d = 0; d < dim; ++d) prod += S.StdVel[d] * G.n[d];
+            prod *= rho;
+#pragma unroll
+            for (int d1 = 0; d1 < dim; ++d1) flux[d1] += UpwindVel[d1] * prod;
+        }
+        // pressure
+        T pressure = T(0);
+#pragma unroll
+        for (int sh = 0; sh < nsh; ++sh) pressure += ipN<ROID, T>(ip, sh) * u[Pc][sh];
+#pragma unroll
+        for (int d1 = 0; d1 < dim; ++d1) flux[d1] += pressure * G.n[d1];
+        // continuity with the stabilised velocity
+        T stabVel[3];
+        if (P.stab == STAB_WITHOUT) {
+#pragma unroll
+            for (int d = 0; d < dim; ++d) stabVel[d] = S.StdVel[d];
+        } else {
+            T trace = T(0);
+#pragma unroll
+            for (int d = 0; d < dim; ++d) trace += gradVel[d][d];
+            const T idiag = T(1) / S.diag;
+#pragma unroll
+            for (int d = 0; d < dim; ++d) {
+                T rhs = T(0);
+                if (P.hasSource) rhs = T(P.src[d]);
+                if (P.transient) {
+                    T oldIPVel = T(0);
+#pragma unroll
+                    for (int sh = 0; sh < nsh; ++sh) oldIPVel += ipN<ROID, T>(ip, sh) * uo[d][sh];
+                    rhs += oldIPVel / T(P.dt);
+                }
+                rhs += S.nuL * S.StdVel[d];
+                if (!P.stokes) {
+                    T UpS = T(0), DnS = T(0);
+#pragma unroll
+                    for (int sh = 0; sh < nsh; ++sh) {
+                        UpS += S.upS[sh] * u[d][sh];
+                        if (P.stab == STAB_FLOW) DnS += S.dnS[sh] * u[d][sh];
+                    }
+                    rhs += S.nsvcl * UpS;
+                    if (P.stab == STAB_FLOW) rhs += S.nsvdl * (DnS - UpS);
+                }
+                if (P.stab == STAB_FLOW) {
+                    T cross = T(0);
+#pragma unroll
+                    for (int d2 = 0; d2 < dim; ++d2)
+                        if (d2 != d) cross += S.StdVel[d2] * gradVel[d][d2];
+                    rhs += S.StdVel[d] * (trace - gradVel[d][d]) - cross;
+                }
+                rhs -= gradP[d] / rho;
+                stabVel[d] = rhs * idiag;
+            }
+        }
+        T contFlux = T(0);
+#pragma unroll
+        for (int d = 0; d < dim; ++d) contFlux += stabVel[d] * G.n[d];
+#pragma unroll
+        for (int d1 = 0; d1 < dim; ++d1) fluxes[ip][d1] = flux[d1];
+        fluxes[ip][Pc] = contFlux * rho;
+    }
+    // scatter the SCVF fluxes: + at from, - at to (compile-time indices)
+#pragma unroll
+    for (int ip = 0; ip < nip; ++ip) {
+#pragma unroll
+        for (int f = 0; f < b; ++f) {
+            dA[f][R::edge(ip, 0)] += fluxes[ip][f];
+            dA[f][R::edge(ip, 1)] -= fluxes[ip][f];
+        }
+    }
+    return ok;
+}
+
+// ---------------------------------------------------------------------------
+// Local stiffness Jacobian: for every SCVF ip and column corner k the b x b
+// block B is added to row corner 'from' and subtracted from row corner 'to'
+// through the sink (sink.add(i, k, B, plus)); 'scale' multiplies B (dt for the
+// implicit-Euler Jacobian M + dt dA/du).
+// ---------------------------------------------------------------------------
+template <int ROID, typename T, class Sink>
+__device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
+                                           const T scale, Sink& sink) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh, b = R::b, Pc = dim;
+    T corMinN = T(0), corMinD = T(0), corAvgN = T(1);
+    if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, T>(E, corMinN, corMinD, corAvgN);
+    const T rho = T(P.rho), nu = T(P.nu);
+    const T mnr = T(-1.0) * nu * rho;
+    bool ok = true;
+#pragma unroll 1
+    for (int ip = 0; ip < R::nip; ++ip) {
+        IpGeo<T> G;
+        ip_geom<ROID, T>(E, ip, G);
+        IpState<ROID, T> S;
+        ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, S);
+        ok &= S.ok;
+        T UpwindVel[3] = {T(0), T(0), T(0)};
+        T w = T(1), prod = T(0), Vn = T(0);
+#pragma unroll
+        for (int d = 0; d < dim; ++d) Vn += S.StdVel[d] * G.n[d];
+        if (!P.stokes) {
+#pragma unroll
+            for (int d = 0; d < dim; ++d) {
+                T s = T(0);
+#pragma unroll
+                for (int sh = 0; sh < nsh; ++sh) s += S.upC[sh] * u[d][sh];
+                UpwindVel[d] = s;
+            }
+            if (P.peclet) w = peclet_blend<ROID, T>(G, S.StdVel, nu, UpwindVel);
+            prod = Vn * rho;
+        }
+        const T idiag = (P.stab == STAB_WITHOUT) ? T(0) : T(1) / S.diag;
+        const T ri = rho * idiag;
+#pragma unroll
+        for (int k = 0; k < nsh; ++k) {
+            T g[3];
+            ip_grad<ROID, T>(G, ip, k, g);
+            const T N = ipN<ROID, T>(ip, k);
+            T gn = T(0), Vg = T(0);
+#pragma unroll
+            for (int d = 0; d < dim; ++d) { gn += g[d] * G.n[d]; Vg += S.StdVel[d] * g[d]; }
+            T B[b][b];
+#pragma unroll
+            for (int r = 0; r < b; ++r)
+#pragma unroll
+                for (int c = 0; c < b; ++c) B[r][c] = T(0);
+            // diffusion
+            const T flux_sh = mnr * gn;
+#pragma unroll
+            for (int d1 = 0; d1 < dim; ++d1) {
+                B[d1][d1] += flux_sh;
+                if (!P.laplace) {
+#pragma unroll
+                    for (int d2 = 0; d2 < dim; ++d2) B[d1][d2] += mnr * g[d1] * G.n[d2];
+                }
+            }
+            // pressure
+#pragma unroll
+            for (int d1 = 0; d1 < dim; ++d1) B[d1][Pc] += N * G.n[d1];
+            // convection
+            if (!P.stokes) {
+                T diagConv = S.upC[k] * (prod * w);
+                if (P.peclet) diagConv += prod * (T(1) - w) * N;
+#pragma unroll
+                for (int d1 = 0; d1 < dim; ++d1) B[d1][d1] += diagConv;
+                if (P.fullNewton != 0.0) {
+#pragma unroll
+                    for (int d2 = 0; d2 < dim; ++d2) {
+                        T pv = w * S.upC[k] * G.n[d2] * rho;
+                        if (P.peclet) pv += (T(1) - w) * N * G.n[d2] * rho;
+#pragma unroll
+                        for (int d1 = 0; d1 < dim; ++d1) B[d1][d2] += pv * UpwindVel[d1];
+                    }
+                }
+            }
+            // continuity
+            if (P.stab == STAB_WITHOUT) {
+#pragma unroll
+                for (int d1 = 0; d1 < dim; ++d1) B[Pc][d1] = N * G.n[d1] * rho;
+            } else {
+                T Sk = S.nuL * N;
+                if (!P.stokes) {
+                    Sk += S.nsvcl * S.upS[k];
+                    if (P.stab == STAB_FLOW) Sk += S.nsvdl * (S.dnS[k] - S.upS[k]);
+                }
+                if (P.stab == STAB_FLOW) {
+#pragma unroll
+                    for (int d1 = 0; d1 < dim; ++d1) B[Pc][d1] = ri * ((Sk - Vg) * G.n[d1] + Vn * g[d1]);
+                } else {
+#pragma unroll
+                    for (int d1 = 0; d1 < dim; ++d1) B[Pc][d1] = ri * Sk * G.n[d1];
+                }
+                B[Pc][Pc] = -(gn / rho) * ri;
+            }
+            if (scale != T(1)) {
+#pragma unroll
+                for (int r = 0; r < b; ++r)
+#pragma unroll
+                    for (int c = 0; c < b; ++c) B[r][c] *= scale;
+            }
+            sink.add(G.from, k, B, true);
+            sink.add(G.to, k, B, false);
+        }
+    }
+    return ok;
+}
+
+}  // namespace nsfv1

@@ -1,0 +1,68 @@
+// The element-disc handle behind the opaque nsfv1_disc* of the C ABI.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+#include "nsfv1_params.h"
+
+namespace nsfv1 {
+
+std::string lower_trim(const char* s);
+int ref_dim(int roid);
+int ref_nsh(int roid);
+
+// Newton / Krylov device workspace (allocated on first solve, per precision)
+struct Workspace {
+    int prec = -1, gmresM = 0;
+    int64_t n = 0;
+    double *D = nullptr, *Dt = nullptr, *Ut = nullptr, *du = nullptr;   // FP64 Newton vectors
+    void* J = nullptr;        // Jacobian values (VT)
+    void* Dinv = nullptr;     // inverted diagonal blocks (VT)
+    void* vec = nullptr;      // Krylov vectors (VT), nvec * n
+    int nvec = 0;
+    double* red = nullptr;    // reduction partials
+    double* scal = nullptr;   // device scalars
+    double* hscal = nullptr;  // pinned host mirror of the scalars
+    int32_t* diagPos = nullptr;
+};
+
+struct Disc {
+    int dim = 2;
+    // parameters (defaults of the reference constructors)
+    double nu = 0.0, rho = 1.0, fullNewton = 0.0;
+    double src[3] = {0, 0, 0};
+    int hasSource = 0, stokes = 0, laplace = 0, peclet = 0;
+    bool viscoSet = false, stabSet = false, convUpwindSet = false, stabSharesConv = false;
+    int convUpwindType = -1, stabUpwindType = -1, stabType = -1, diffLen = DL_RAW;
+
+    // mesh
+    bool hasMesh = false;
+    int roid = 0, nsh = 0, nColors = 0;
+    int64_t nNodes = 0, nElems = 0;
+    std::vector<int32_t> rowPtr, colIdx, elemBlk, color, colorPtr, colorElems;
+    double* d_coords = nullptr;
+    int32_t *d_conn = nullptr, *d_elemBlk = nullptr, *d_colorElems = nullptr, *d_rowPtr = nullptr, *d_colIdx = nullptr;
+    int32_t* d_dirRow = nullptr;
+    double* d_dirVal = nullptr;
+    int64_t nDir = 0;
+    int* d_err = nullptr;
+
+    Workspace ws;
+
+    int status = 0;
+    std::string lastError;
+
+    ~Disc();
+    void free_mesh();
+    void free_workspace();
+    bool fail(int code, const std::string& msg);
+    bool cuda_ok(cudaError_t e, const char* where);
+    bool check_err_word(cudaStream_t s);
+    bool params(DiscParams& P, bool transient, double dt);
+    bool assemble_defect(const double* u, const double* u_old, double dt, double* d, cudaStream_t s);
+    bool assemble_jacobian(const double* u, const double* u_old, double dt, void* vals, int prec, cudaStream_t s, bool sync = true);
+    bool ensure_workspace(int prec, int gmresM);
+};
+
+}  // namespace nsfv1

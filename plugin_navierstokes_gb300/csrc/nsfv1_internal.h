@@ -1,0 +1,41 @@
+// Internal declarations shared by the host C-ABI layer and the CUDA sources.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+#include "nsfv1_params.h"
+
+namespace nsfv1 {
+
+// Device view of a mesh for one assembly launch (the elements of one colour).
+struct AsmArgs {
+    const double* coords;     // [nNodes][dim]
+    const int32_t* conn;      // [nElems][nsh]
+    const int32_t* elemBlk;   // [nElems][nsh][nsh] block index into the BSR values
+    const int32_t* elems;     // element ids of this launch
+    int32_t count;
+    int* err;                 // error word (bit 0: upwind side not found)
+    const double* U;          // [nNodes][b]
+    const double* Uold;       // [nNodes][b] or null
+    double* D;                // defect [nNodes][b]
+    void* vals;               // BSR values (double or float)
+};
+
+// Batched element-local callbacks (no global scatter).
+struct ElemBatchArgs {
+    int64_t n;
+    const double* corners;    // [n][nsh][dim]
+    const double* u;          // [n][b][nsh]
+    const double* uold;       // [n][b][nsh] or null
+    double* defA; double* jacA; double* defM; double* jacM; double* rhs;
+    int* err;
+};
+
+cudaError_t launch_defect(int roid, const DiscParams& P, const AsmArgs& a, cudaStream_t s);
+cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s);
+cudaError_t launch_elem_batch(int roid, const DiscParams& P, const ElemBatchArgs& a, cudaStream_t s);
+cudaError_t launch_dirichlet(int b, int64_t n, const int32_t* rows, const double* vals, const int32_t* rowPtr,
+                             const int32_t* colIdx, const double* U, double* D, void* J, int prec, cudaStream_t s);
+
+}  // namespace nsfv1

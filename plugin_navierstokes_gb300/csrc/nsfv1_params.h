@@ -1,0 +1,22 @@
+// Parameter block and option ids shared by the host layer and the kernels.
+#pragma once
+
+namespace nsfv1 {
+
+enum { ROID_TRIANGLE = 2, ROID_QUADRILATERAL = 3, ROID_TETRAHEDRON = 4, ROID_HEXAHEDRON = 8 };
+enum { UPW_NO = 0, UPW_FULL = 1, UPW_SKEWED = 2, UPW_LPS = 3 };
+enum { STAB_FIELDS = 0, STAB_FLOW = 1, STAB_WITHOUT = 2 };
+enum { DL_RAW = 0, DL_FIVEPOINT = 1, DL_COR = 2 };
+
+// Uniform (per launch) discretisation parameters.
+struct DiscParams {
+    double nu, rho, fullNewton, dt;
+    double src[3];
+    int convUpwind;   // upwind of the convective term (ignored when stokes)
+    int stabUpwind;   // upwind object of the stabilisation
+    int sameUpwind;   // 1: the stabilisation shares the convection upwind object
+    int stab, diffLen;
+    int stokes, laplace, peclet, hasSource, transient;
+};
+
+}  // namespace nsfv1

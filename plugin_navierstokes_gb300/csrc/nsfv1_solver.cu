@@ -1,0 +1,671 @@
+// Device linear algebra on the handle's block-CSR pattern and the Newton
+// driver: block SpMV, point-block Jacobi (inverted b x b diagonal blocks),
+// right-preconditioned BiCGStab and restarted GMRES, FP64 defect norms.
+// Krylov vectors and the Jacobian share one value type VT (double for the
+// plain method, float for the FP32-Jacobian mode); reductions accumulate in
+// FP64 with a fixed grid and a fixed summation tree, so results are bitwise
+// reproducible run to run.
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+#include "nsfv1_internal.h"
+#include "nsfv1_host.h"
+#include "../../include/nsfv1_gb300.h"
+
+namespace nsfv1 {
+
+static constexpr int kRedBlocks = 608;   // 4 x 152 SMs
+static constexpr int kRedThreads = 256;
+
+// ---------------------------------------------------------------------------
+// block SpMV: one group of G lanes per block row; lane l takes entries l, l+G,
+// ... of the row's contiguous b*b-blocks (coalesced over the values), then the
+// group reduces the b row sums with shuffles in a fixed order.
+// ---------------------------------------------------------------------------
+template <typename VT, typename XT, int b, int G>
+__global__ void __launch_bounds__(256) k_bsr_mv(int64_t nRows, const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx,
+                                                const VT* __restrict__ vals, const XT* __restrict__ x, XT* __restrict__ y) {
+    constexpr int bb = b * b;
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t row = gid / G;
+    const int lane = threadIdx.x % G;
+    if (row >= nRows) return;
+    const int64_t q0 = rowPtr[row], q1 = rowPtr[row + 1];
+    double acc[b];
+#pragma unroll
+    for (int i = 0; i < b; ++i) acc[i] = 0.0;
+    for (int64_t idx = q0 * bb + lane; idx < q1 * bb; idx += G) {
+        const int64_t q = idx / bb;
+        const int w = (int)(idx - q * bb);
+        const int i = w / b, j = w - (w / b) * b;
+        const double v = (double)__ldg(vals + idx) * (double)__ldg(x + (int64_t)__ldg(colIdx + q) * b + j);
+#pragma unroll
+        for (int r = 0; r < b; ++r)
+            if (r == i) acc[r] += v;
+    }
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1)
+#pragma unroll
+        for (int r = 0; r < b; ++r) acc[r] += __shfl_down_sync(0xffffffffu, acc[r], off, G);
+    if (lane == 0) {
+#pragma unroll
+        for (int r = 0; r < b; ++r) y[row * b + r] = (XT)acc[r];
+    }
+}
+
+// inverse of the diagonal blocks (Gauss-Jordan, partial pivoting); err bit 2 on a zero pivot
+template <typename VT, int b>
+__global__ void k_block_inv(int64_t nRows, const int32_t* __restrict__ diagPos, const VT* __restrict__ vals, VT* __restrict__ Dinv, int* err) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nRows) return;
+    double M[b][2 * b];
+    const VT* A = vals + (int64_t)diagPos[r] * b * b;
+#pragma unroll
+    for (int i = 0; i < b; ++i)
+#pragma unroll
+        for (int j = 0; j < b; ++j) { M[i][j] = (double)A[i * b + j]; M[i][b + j] = (i == j) ? 1.0 : 0.0; }
+    bool ok = true;
+#pragma unroll
+    for (int c = 0; c < b; ++c) {
+        int p = c;
+#pragma unroll
+        for (int q = c + 1; q < b; ++q) if (fabs(M[q][c]) > fabs(M[p][c])) p = q;
+        if (M[p][c] == 0.0) { ok = false; break; }
+        if (p != c) {
+#pragma unroll
+            for (int j = 0; j < 2 * b; ++j) { const double t = M[p][j]; M[p][j] = M[c][j]; M[c][j] = t; }
+        }
+        const double piv = 1.0 / M[c][c];
+#pragma unroll
+        for (int j = 0; j < 2 * b; ++j) M[c][j] *= piv;
+#pragma unroll
+        for (int q = 0; q < b; ++q) {
+            if (q == c) continue;
+            const double f = M[q][c];
+#pragma unroll
+            for (int j = 0; j < 2 * b; ++j) M[q][j] -= f * M[c][j];
+        }
+    }
+    if (!ok) { atomicOr(err, 2); return; }
+    VT* O = Dinv + r * b * b;
+#pragma unroll
+    for (int i = 0; i < b; ++i)
+#pragma unroll
+        for (int j = 0; j < b; ++j) O[i * b + j] = (VT)M[i][b + j];
+}
+
+template <typename VT, int b>
+__global__ void k_prec(int64_t nRows, const VT* __restrict__ Dinv, const VT* __restrict__ in, VT* __restrict__ out) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nRows) return;
+    VT x[b];
+#pragma unroll
+    for (int j = 0; j < b; ++j) x[j] = in[r * b + j];
+    const VT* M = Dinv + r * b * b;
+#pragma unroll
+    for (int i = 0; i < b; ++i) {
+        VT a = VT(0);
+#pragma unroll
+        for (int j = 0; j < b; ++j) a += M[i * b + j] * x[j];
+        out[r * b + i] = a;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// deterministic reductions: K dot products at once, partials per block, then
+// one block sums the partials in a fixed order.
+// pairs: dot_k = sum a_k[i] * c_k[i]
+// ---------------------------------------------------------------------------
+template <typename VT, int K>
+struct DotArgs { const VT* a[K]; const VT* c[K]; };
+
+template <typename VT, int K>
+__global__ void __launch_bounds__(kRedThreads) k_dot_partial(int64_t n, DotArgs<VT, K> A, double* __restrict__ partials) {
+    __shared__ double sh[K][kRedThreads];
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRedThreads) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[k] += (double)A.a[k][i] * (double)A.c[k][i];
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) partials[k * gridDim.x + blockIdx.x] = sh[k][0];
+    }
+}
+
+// sums K x nb partials into out[k] (one block, fixed order)
+template <int K>
+__device__ __forceinline__ void block_sum_partials(const double* __restrict__ partials, int nb, double* out) {
+    __shared__ double sh[K][kRedThreads];
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.0;
+    for (int i = threadIdx.x; i < nb; i += kRedThreads)
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[k] += partials[k * nb + i];
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[k] = sh[k][0];
+    }
+}
+
+// scalar slots of the BiCGStab state in ws.scal
+enum { S_RHO = 0, S_ALPHA, S_OMEGA, S_RHO1, S_BETA, S_R0V, S_TS, S_TT, S_NR2, S_NR02, S_FLAG, S_NSCAL = 16 };
+
+template <int K>
+__global__ void k_dot_final(const double* partials, int nb, double* out) { block_sum_partials<K>(partials, nb, out); }
+
+// rho1 = (r0, r); beta = (rho1 / rho) * (alpha / omega)
+__global__ void k_bicg_beta(const double* partials, int nb, double* S) {
+    double v[1];
+    block_sum_partials<1>(partials, nb, v);
+    if (threadIdx.x == 0) {
+        S[S_RHO1] = v[0];
+        S[S_BETA] = (v[0] / S[S_RHO]) * (S[S_ALPHA] / S[S_OMEGA]);
+        if (v[0] == 0.0) S[S_FLAG] = 1.0;
+    }
+}
+// alpha = rho1 / (r0, v)
+__global__ void k_bicg_alpha(const double* partials, int nb, double* S) {
+    double v[1];
+    block_sum_partials<1>(partials, nb, v);
+    if (threadIdx.x == 0) {
+        S[S_R0V] = v[0];
+        S[S_ALPHA] = (v[0] != 0.0) ? S[S_RHO1] / v[0] : 0.0;
+        if (v[0] == 0.0) S[S_FLAG] = 1.0;
+    }
+}
+// omega = (t, s) / (t, t)
+__global__ void k_bicg_omega(const double* partials, int nb, double* S) {
+    double v[2];
+    block_sum_partials<2>(partials, nb, v);
+    if (threadIdx.x == 0) {
+        S[S_TS] = v[0]; S[S_TT] = v[1];
+        S[S_OMEGA] = (v[1] != 0.0) ? v[0] / v[1] : 0.0;
+    }
+}
+// ||r||^2 and rho <- rho1
+__global__ void k_bicg_rnorm(const double* partials, int nb, double* S) {
+    double v[1];
+    block_sum_partials<1>(partials, nb, v);
+    if (threadIdx.x == 0) { S[S_NR2] = v[0]; S[S_RHO] = S[S_RHO1]; }
+}
+
+// p = r + beta (p - omega v)
+template <typename VT>
+__global__ void k_bicg_p(int64_t n, const double* S, const VT* __restrict__ r, const VT* __restrict__ v, VT* __restrict__ p) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const VT beta = (VT)S[S_BETA], omega = (VT)S[S_OMEGA];
+    p[i] = r[i] + beta * (p[i] - omega * v[i]);
+}
+// s = r - alpha v
+template <typename VT>
+__global__ void k_bicg_s(int64_t n, const double* S, const VT* __restrict__ r, const VT* __restrict__ v, VT* __restrict__ s) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    s[i] = r[i] - (VT)S[S_ALPHA] * v[i];
+}
+// x += alpha ph + omega sh ; r = s - omega t
+template <typename VT>
+__global__ void k_bicg_x(int64_t n, const double* S, const VT* __restrict__ ph, const VT* __restrict__ sh, const VT* __restrict__ s,
+                         const VT* __restrict__ t, VT* __restrict__ x, VT* __restrict__ r) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const VT alpha = (VT)S[S_ALPHA], omega = (VT)S[S_OMEGA];
+    x[i] += alpha * ph[i] + omega * sh[i];
+    r[i] = s[i] - omega * t[i];
+}
+
+template <typename A, typename B>
+__global__ void k_convert(int64_t n, const A* __restrict__ a, B* __restrict__ b) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (B)a[i];
+}
+template <typename VT>
+__global__ void k_fill(int64_t n, VT* a, VT v) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+// ut = u - lambda du
+template <typename VT>
+__global__ void k_newton_update(int64_t n, const double* __restrict__ u, const VT* __restrict__ du, double lambda, double* __restrict__ ut) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) ut[i] = u[i] - lambda * (double)du[i];
+}
+__global__ void k_set_dirichlet(int64_t n, const int32_t* __restrict__ rows, const double* __restrict__ vals, double* u) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) u[rows[i]] = vals[i];
+}
+
+// GMRES helpers ---------------------------------------------------------------
+// h[k] = (V_k, w) for k < m (one pass over w, partials per block)
+template <typename VT>
+__global__ void __launch_bounds__(kRedThreads) k_multidot_partial(int64_t n, int m, const VT* __restrict__ V, const VT* __restrict__ w,
+                                                                 double* __restrict__ partials) {
+    __shared__ double sh[kRedThreads];
+    for (int k = 0; k < m; ++k) {
+        double acc = 0.0;
+        const VT* vk = V + (int64_t)k * n;
+        for (int64_t i = (int64_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRedThreads)
+            acc += (double)vk[i] * (double)w[i];
+        sh[threadIdx.x] = acc;
+        __syncthreads();
+        for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+            if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) partials[k * gridDim.x + blockIdx.x] = sh[0];
+        __syncthreads();
+    }
+}
+__global__ void k_multidot_final(const double* __restrict__ partials, int nb, int m, double* out) {
+    __shared__ double sh[kRedThreads];
+    for (int k = 0; k < m; ++k) {
+        double acc = 0.0;
+        for (int i = threadIdx.x; i < nb; i += kRedThreads) acc += partials[k * nb + i];
+        sh[threadIdx.x] = acc;
+        __syncthreads();
+        for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+            if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[k] = sh[0];
+        __syncthreads();
+    }
+}
+// w -= sum_k h[k] V_k
+template <typename VT>
+__global__ void k_multi_axpy(int64_t n, int m, const double* __restrict__ h, const VT* __restrict__ V, VT* __restrict__ w) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double a = (double)w[i];
+    for (int k = 0; k < m; ++k) a -= h[k] * (double)V[(int64_t)k * n + i];
+    w[i] = (VT)a;
+}
+// v = w / beta
+template <typename VT>
+__global__ void k_scale(int64_t n, const VT* __restrict__ w, double inv, VT* __restrict__ v) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (VT)((double)w[i] * inv);
+}
+// x += sum_k y[k] Z_k   (Z = preconditioned basis)
+template <typename VT>
+__global__ void k_multi_axpy_add(int64_t n, int m, const double* __restrict__ y, const VT* __restrict__ Z, VT* __restrict__ x) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double a = (double)x[i];
+    for (int k = 0; k < m; ++k) a += y[k] * (double)Z[(int64_t)k * n + i];
+    x[i] = (VT)a;
+}
+
+static inline int grid_for(int64_t n, int t = 256) { return (int)((n + t - 1) / t); }
+
+template <typename VT>
+static cudaError_t spmv(const Disc& D, const VT* vals, const VT* x, VT* y, cudaStream_t s) {
+    const int64_t nR = D.nNodes;
+    const int b = D.dim + 1;
+    if (b == 4) {
+        constexpr int G = 16;
+        k_bsr_mv<VT, VT, 4, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y);
+    } else {
+        constexpr int G = 8;
+        k_bsr_mv<VT, VT, 3, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y);
+    }
+    return cudaGetLastError();
+}
+
+template <typename VT>
+static void prec_apply(const Disc& D, const VT* Dinv, const VT* in, VT* out, cudaStream_t s) {
+    if (D.dim == 3) k_prec<VT, 4><<<grid_for(D.nNodes), 256, 0, s>>>(D.nNodes, Dinv, in, out);
+    else k_prec<VT, 3><<<grid_for(D.nNodes), 256, 0, s>>>(D.nNodes, Dinv, in, out);
+}
+
+template <typename VT, int K>
+static void dots(int64_t n, const VT* const (&a)[K], const VT* const (&c)[K], double* partials, cudaStream_t s) {
+    DotArgs<VT, K> A;
+    for (int k = 0; k < K; ++k) { A.a[k] = a[k]; A.c[k] = c[k]; }
+    k_dot_partial<VT, K><<<kRedBlocks, kRedThreads, 0, s>>>(n, A, partials);
+}
+
+// ||x||_2^2 of an FP64 vector into out (device)
+static void norm2sq(int64_t n, const double* x, double* partials, double* out, cudaStream_t s) {
+    const double* a[1] = {x};
+    dots<double, 1>(n, a, a, partials, s);
+    k_dot_final<1><<<1, kRedThreads, 0, s>>>(partials, kRedBlocks, out);
+}
+
+}  // namespace nsfv1
+
+// ============================================================================
+using namespace nsfv1;
+
+namespace nsfv1 {
+
+void Disc::free_workspace() {
+    auto f = [](auto*& p) { if (p) cudaFree((void*)p); p = nullptr; };
+    f(ws.D); f(ws.Dt); f(ws.Ut); f(ws.du); f(ws.J); f(ws.Dinv); f(ws.vec); f(ws.red); f(ws.scal); f(ws.diagPos);
+    if (ws.hscal) cudaFreeHost(ws.hscal);
+    ws = Workspace();
+}
+
+bool Disc::ensure_workspace(int prec, int gmresM) {
+    const int b = dim + 1;
+    const int64_t n = nNodes * b;
+    const int nvec = 9 + 2 * (gmresM + 1);
+    if (ws.prec == prec && ws.n == n && ws.nvec >= nvec) return true;
+    free_workspace();
+    const size_t vt = prec == NSFV1_F64 ? sizeof(double) : sizeof(float);
+    auto al = [&](auto*& p, size_t bytes) { return cuda_ok(cudaMalloc((void**)&p, bytes), "workspace alloc"); };
+    if (!al(ws.D, n * 8) || !al(ws.Dt, n * 8) || !al(ws.Ut, n * 8) || !al(ws.du, n * 8) ||
+        !al(ws.J, colIdx.size() * b * b * vt) || !al(ws.Dinv, (size_t)nNodes * b * b * vt) ||
+        !al(ws.vec, (size_t)nvec * n * vt) || !al(ws.red, sizeof(double) * kRedBlocks * 80) ||
+        !al(ws.scal, sizeof(double) * 256) || !al(ws.diagPos, sizeof(int32_t) * nNodes))
+        return false;
+    if (!cuda_ok(cudaMallocHost((void**)&ws.hscal, sizeof(double) * 256), "pinned alloc")) return false;
+    std::vector<int32_t> dp(nNodes);
+    for (int64_t r = 0; r < nNodes; ++r) {
+        int32_t q = rowPtr[r];
+        while (colIdx[q] != r) ++q;
+        dp[r] = q;
+    }
+    if (!cuda_ok(cudaMemcpy(ws.diagPos, dp.data(), sizeof(int32_t) * nNodes, cudaMemcpyHostToDevice), "diagPos")) return false;
+    ws.prec = prec; ws.n = n; ws.nvec = nvec; ws.gmresM = gmresM;
+    return true;
+}
+
+}  // namespace nsfv1
+
+namespace {
+
+// reads k scalars from ws.scal (device) into ws.hscal (pinned) and waits
+static bool read_scal(Disc& D, int first, int k, cudaStream_t s) {
+    if (!D.cuda_ok(cudaMemcpyAsync(D.ws.hscal + first, D.ws.scal + first, sizeof(double) * k, cudaMemcpyDeviceToHost, s), "read scalars")) return false;
+    return D.cuda_ok(cudaStreamSynchronize(s), "sync");
+}
+
+// BiCGStab on J x = rhs (right point-block-Jacobi preconditioning), x = 0 start.
+// Returns iterations, or -1 on breakdown / failure (D.status set on CUDA errors).
+template <typename VT>
+static int bicgstab(Disc& D, const VT* J, const VT* Dinv, const VT* rhs, VT* x, double rtol, int maxit, double* relres, cudaStream_t s) {
+    Workspace& W = D.ws;
+    const int64_t n = W.n;
+    VT* V = (VT*)W.vec;
+    VT *r = V + 0 * n, *r0 = V + 1 * n, *p = V + 2 * n, *v = V + 3 * n, *sv = V + 4 * n, *t = V + 5 * n, *ph = V + 6 * n, *shv = V + 7 * n;
+    double* S = W.scal;
+    const int g = grid_for(n);
+    k_fill<VT><<<g, 256, 0, s>>>(n, x, VT(0));
+    cudaMemcpyAsync(r, rhs, n * sizeof(VT), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(r0, rhs, n * sizeof(VT), cudaMemcpyDeviceToDevice, s);
+    k_fill<VT><<<g, 256, 0, s>>>(n, p, VT(0));
+    k_fill<VT><<<g, 256, 0, s>>>(n, v, VT(0));
+    double init[S_NSCAL] = {0};
+    init[S_RHO] = 1.0; init[S_ALPHA] = 1.0; init[S_OMEGA] = 1.0;
+    std::memcpy(W.hscal, init, sizeof(init));
+    cudaMemcpyAsync(S, W.hscal, sizeof(init), cudaMemcpyHostToDevice, s);
+    {
+        const VT* a[1] = {r};
+        dots<VT, 1>(n, a, a, W.red, s);
+        k_dot_final<1><<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S + S_NR02);
+    }
+    if (!read_scal(D, S_NR02, 1, s)) return -1;
+    const double nr0 = std::sqrt(W.hscal[S_NR02]);
+    *relres = 1.0;
+    if (nr0 == 0.0) return 0;
+    for (int it = 1; it <= maxit; ++it) {
+        { const VT* a[1] = {r0}; const VT* c[1] = {r}; dots<VT, 1>(n, a, c, W.red, s); }
+        k_bicg_beta<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
+        k_bicg_p<VT><<<g, 256, 0, s>>>(n, S, r, v, p);
+        prec_apply<VT>(D, Dinv, p, ph, s);
+        spmv<VT>(D, J, ph, v, s);
+        { const VT* a[1] = {r0}; const VT* c[1] = {v}; dots<VT, 1>(n, a, c, W.red, s); }
+        k_bicg_alpha<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
+        k_bicg_s<VT><<<g, 256, 0, s>>>(n, S, r, v, sv);
+        prec_apply<VT>(D, Dinv, sv, shv, s);
+        spmv<VT>(D, J, shv, t, s);
+        { const VT* a[2] = {t, t}; const VT* c[2] = {sv, t}; dots<VT, 2>(n, a, c, W.red, s); }
+        k_bicg_omega<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
+        k_bicg_x<VT><<<g, 256, 0, s>>>(n, S, ph, shv, sv, t, x, r);
+        { const VT* a[1] = {r}; dots<VT, 1>(n, a, a, W.red, s); }
+        k_bicg_rnorm<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
+        if (!D.cuda_ok(cudaGetLastError(), "bicgstab launch")) return -1;
+        if (!read_scal(D, 0, S_NSCAL, s)) return -1;
+        const double nr = std::sqrt(W.hscal[S_NR2]);
+        *relres = nr / nr0;
+        if (!std::isfinite(nr)) return -1;
+        if (*relres < rtol) return it;
+        if (W.hscal[S_FLAG] != 0.0 || W.hscal[S_OMEGA] == 0.0) return -1;
+    }
+    return maxit;
+}
+
+// restarted GMRES(m), right preconditioned, classical Gram-Schmidt with one
+// re-orthogonalisation pass; Hessenberg least squares (Givens) on the host.
+template <typename VT>
+static int gmres(Disc& D, const VT* J, const VT* Dinv, const VT* rhs, VT* x, double rtol, int maxit, int m, double* relres, cudaStream_t s) {
+    Workspace& W = D.ws;
+    const int64_t n = W.n;
+    VT* base = (VT*)W.vec;
+    VT* w = base;                 // work vector
+    VT* Vb = base + 1 * n;        // basis V_0..V_m
+    VT* Zb = base + (1 + m + 1) * n;   // preconditioned basis Z_0..Z_{m-1}
+    double* hdev = W.scal + 32;   // up to 64 + 1 coefficients
+    const int g = grid_for(n);
+    k_fill<VT><<<g, 256, 0, s>>>(n, x, VT(0));
+    std::vector<double> H((m + 1) * m), cs(m), sn(m), gam(m + 1), y(m);
+    double beta0 = -1.0;
+    int it = 0;
+    *relres = 1.0;
+    while (it < maxit) {
+        // V_0 = rhs - J x
+        spmv<VT>(D, J, x, w, s);
+        cudaMemcpyAsync(Vb, rhs, n * sizeof(VT), cudaMemcpyDeviceToDevice, s);
+        W.hscal[40] = 1.0;
+        cudaMemcpyAsync(hdev, W.hscal + 40, sizeof(double), cudaMemcpyHostToDevice, s);
+        k_multi_axpy<VT><<<g, 256, 0, s>>>(n, 1, hdev, w, Vb);
+        {
+            const VT* a[1] = {Vb};
+            dots<VT, 1>(n, a, a, W.red, s);
+            k_dot_final<1><<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, W.scal + S_NR2);
+        }
+        if (!read_scal(D, S_NR2, 1, s)) return -1;
+        const double beta = std::sqrt(W.hscal[S_NR2]);
+        if (beta0 < 0) beta0 = beta;
+        if (beta0 == 0.0) return 0;
+        *relres = beta / beta0;
+        if (*relres < rtol) return it;
+        k_scale<VT><<<g, 256, 0, s>>>(n, Vb, 1.0 / beta, Vb);
+        std::fill(gam.begin(), gam.end(), 0.0);
+        gam[0] = beta;
+        int j = 0;
+        for (; j < m && it < maxit; ++j) {
+            ++it;
+            VT* Zj = Zb + (int64_t)j * n;
+            prec_apply<VT>(D, Dinv, Vb + (int64_t)j * n, Zj, s);
+            spmv<VT>(D, J, Zj, w, s);
+            double hcol[66] = {0};
+            for (int pass = 0; pass < 2; ++pass) {
+                k_multidot_partial<VT><<<kRedBlocks, kRedThreads, 0, s>>>(n, j + 1, Vb, w, W.red);
+                k_multidot_final<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, j + 1, hdev);
+                k_multi_axpy<VT><<<g, 256, 0, s>>>(n, j + 1, hdev, Vb, w);
+                if (!D.cuda_ok(cudaMemcpyAsync(W.hscal + 64, hdev, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s), "h")) return -1;
+                if (!D.cuda_ok(cudaStreamSynchronize(s), "sync")) return -1;
+                for (int k = 0; k <= j; ++k) hcol[k] += W.hscal[64 + k];
+            }
+            {
+                const VT* a[1] = {w};
+                dots<VT, 1>(n, a, a, W.red, s);
+                k_dot_final<1><<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, W.scal + S_NR2);
+            }
+            if (!read_scal(D, S_NR2, 1, s)) return -1;
+            const double hn = std::sqrt(W.hscal[S_NR2]);
+            hcol[j + 1] = hn;
+            if (hn > 0.0) k_scale<VT><<<g, 256, 0, s>>>(n, w, 1.0 / hn, Vb + (int64_t)(j + 1) * n);
+            // apply previous Givens rotations, then a new one
+            for (int k = 0; k < j; ++k) {
+                const double a = hcol[k], b2 = hcol[k + 1];
+                hcol[k] = cs[k] * a + sn[k] * b2;
+                hcol[k + 1] = -sn[k] * a + cs[k] * b2;
+            }
+            const double a = hcol[j], b2 = hcol[j + 1];
+            const double rr = std::sqrt(a * a + b2 * b2);
+            cs[j] = rr > 0 ? a / rr : 1.0; sn[j] = rr > 0 ? b2 / rr : 0.0;
+            hcol[j] = rr; hcol[j + 1] = 0.0;
+            gam[j + 1] = -sn[j] * gam[j];
+            gam[j] = cs[j] * gam[j];
+            for (int k = 0; k <= j; ++k) H[k * m + j] = hcol[k];
+            *relres = std::fabs(gam[j + 1]) / beta0;
+            if (!std::isfinite(*relres)) return -1;
+            if (*relres < rtol || hn == 0.0) { ++j; break; }
+        }
+        // y = H^-1 gam ; x += Z y
+        for (int k = j - 1; k >= 0; --k) {
+            double acc = gam[k];
+            for (int q = k + 1; q < j; ++q) acc -= H[k * m + q] * y[q];
+            if (H[k * m + k] == 0.0) return -1;
+            y[k] = acc / H[k * m + k];
+        }
+        std::memcpy(W.hscal + 64, y.data(), sizeof(double) * j);
+        cudaMemcpyAsync(hdev, W.hscal + 64, sizeof(double) * j, cudaMemcpyHostToDevice, s);
+        k_multi_axpy_add<VT><<<g, 256, 0, s>>>(n, j, hdev, Zb, x);
+        if (!D.cuda_ok(cudaGetLastError(), "gmres launch")) return -1;
+        if (*relres < rtol) return it;
+    }
+    return it;
+}
+
+template <typename VT>
+static int newton_impl(Disc& D, double* u, const double* u_old, double dt, const nsfv1_newton_params& p, nsfv1_newton_result& res,
+                       cudaStream_t s) {
+    const int prec = std::is_same<VT, double>::value ? NSFV1_F64 : NSFV1_F32;
+    const int m = std::min(std::max(p.gmres_restart, 1), 64);
+    if (!D.ensure_workspace(prec, p.linear_solver == NSFV1_GMRES ? m : 0)) return D.status;
+    Workspace& W = D.ws;
+    const int64_t n = W.n;
+    const int g = grid_for(n);
+    const int b = D.dim + 1;
+    VT* J = (VT*)W.J;
+    VT* Dinv = (VT*)W.Dinv;
+    VT* Vv = (VT*)W.vec;
+    VT* rhsV = Vv + (int64_t)(W.nvec - 2) * n;   // rhs of the linear solve (VT)
+    VT* xsol = Vv + (int64_t)(W.nvec - 1) * n;   // its solution du (VT)
+
+    if (D.nDir > 0) k_set_dirichlet<<<grid_for(D.nDir), 256, 0, s>>>(D.nDir, D.d_dirRow, D.d_dirVal, u);
+    if (!D.assemble_defect(u, u_old, dt, W.D, s)) return D.status;
+    norm2sq(n, W.D, W.red, W.scal + 100, s);
+    if (!read_scal(D, 100, 1, s)) return D.status;
+    double nd = std::sqrt(W.hscal[100]);
+    const double nd0 = nd;
+    res.initial_defect = nd0; res.final_defect = nd; res.iterations = 0; res.linear_iterations = 0;
+    if (!std::isfinite(nd0)) { res.status = NSFV1_ERR_NONFINITE; return res.status; }
+    int status = NSFV1_ERR_NOT_CONVERGED;
+    if (nd0 == 0.0) status = NSFV1_OK;
+    int it = 0;
+    while (status == NSFV1_ERR_NOT_CONVERGED && it < p.max_iter) {
+        if (nd <= p.rtol * nd0 || nd <= p.atol) { status = NSFV1_OK; break; }
+        ++it;
+        if (!D.assemble_jacobian(u, u_old, dt, J, prec, s, false)) return D.status;
+        cudaMemsetAsync(D.d_err, 0, sizeof(int), s);
+        if (b == 4) k_block_inv<VT, 4><<<grid_for(D.nNodes), 128, 0, s>>>(D.nNodes, W.diagPos, J, Dinv, D.d_err);
+        else k_block_inv<VT, 3><<<grid_for(D.nNodes), 128, 0, s>>>(D.nNodes, W.diagPos, J, Dinv, D.d_err);
+        int herr = 0;
+        cudaMemcpyAsync(&herr, D.d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (!D.cuda_ok(cudaStreamSynchronize(s), "jacobian")) return D.status;
+        if (herr & 1) { D.fail(NSFV1_ERR_GEOMETRY, "upwind: cannot find cut side"); cudaMemsetAsync(D.d_err, 0, sizeof(int), s); return D.status; }
+        if (herr & 2) { status = NSFV1_ERR_BREAKDOWN; D.fail(NSFV1_ERR_BREAKDOWN, "singular diagonal block"); cudaMemsetAsync(D.d_err, 0, sizeof(int), s); break; }
+        k_convert<double, VT><<<g, 256, 0, s>>>(n, W.D, rhsV);
+        double rr = 0;
+        int li;
+        if (p.linear_solver == NSFV1_GMRES) li = gmres<VT>(D, J, Dinv, rhsV, xsol, p.lin_rtol, p.lin_max_iter, m, &rr, s);
+        else li = bicgstab<VT>(D, J, Dinv, rhsV, xsol, p.lin_rtol, p.lin_max_iter, &rr, s);
+        if (D.status == NSFV1_ERR_CUDA) return D.status;
+        if (li < 0) { status = NSFV1_ERR_BREAKDOWN; D.fail(NSFV1_ERR_BREAKDOWN, "linear solver breakdown"); break; }
+        res.linear_iterations += li;
+        double lambda = 1.0, ndt = 0.0;
+        for (int k = 0; k <= p.line_search_steps; ++k) {
+            k_newton_update<VT><<<g, 256, 0, s>>>(n, u, xsol, lambda, W.Ut);
+            if (!D.assemble_defect(W.Ut, u_old, dt, W.Dt, s)) return D.status;
+            norm2sq(n, W.Dt, W.red, W.scal + 100, s);
+            if (!read_scal(D, 100, 1, s)) return D.status;
+            ndt = std::sqrt(W.hscal[100]);
+            if (ndt <= (1.0 - 1e-4 * lambda) * nd || k == p.line_search_steps) break;
+            lambda *= 0.5;
+        }
+        cudaMemcpyAsync(u, W.Ut, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        std::swap(W.D, W.Dt);
+        nd = ndt;
+        if (!std::isfinite(nd)) { status = NSFV1_ERR_NONFINITE; break; }
+    }
+    if (status == NSFV1_ERR_NOT_CONVERGED && (nd <= p.rtol * nd0 || nd <= p.atol)) status = NSFV1_OK;
+    if (!D.cuda_ok(cudaStreamSynchronize(s), "newton")) return D.status;
+    res.iterations = it; res.final_defect = nd; res.status = status;
+    if (status != NSFV1_OK && status != NSFV1_ERR_BREAKDOWN) D.fail(status, status == NSFV1_ERR_NONFINITE ? "non-finite defect" : "Newton did not converge");
+    return status;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nsfv1_bsr_mv(nsfv1_disc* h, const void* vals, int prec, const double* x, double* y, void* stream) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "bsr_mv: no mesh"); return D->status; }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t nR = D->nNodes;
+    if (prec == NSFV1_F64) {
+        if (D->dim == 3) k_bsr_mv<double, double, 4, 16><<<grid_for(nR * 16), 256, 0, s>>>(nR, D->d_rowPtr, D->d_colIdx, (const double*)vals, x, y);
+        else k_bsr_mv<double, double, 3, 8><<<grid_for(nR * 8), 256, 0, s>>>(nR, D->d_rowPtr, D->d_colIdx, (const double*)vals, x, y);
+    } else if (prec == NSFV1_F32) {
+        if (D->dim == 3) k_bsr_mv<float, double, 4, 16><<<grid_for(nR * 16), 256, 0, s>>>(nR, D->d_rowPtr, D->d_colIdx, (const float*)vals, x, y);
+        else k_bsr_mv<float, double, 3, 8><<<grid_for(nR * 8), 256, 0, s>>>(nR, D->d_rowPtr, D->d_colIdx, (const float*)vals, x, y);
+    } else {
+        D->fail(NSFV1_ERR_ARGUMENT, "bsr_mv: bad precision");
+        return D->status;
+    }
+    return D->cuda_ok(cudaGetLastError(), "bsr_mv") ? NSFV1_OK : D->status;
+}
+
+int nsfv1_newton_solve(nsfv1_disc* h, double* u, const double* u_old, double dt, const nsfv1_newton_params* p,
+                       nsfv1_newton_result* r, void* stream) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "newton_solve: no mesh"); return D->status; }
+    if (!u || !p || !r) { D->fail(NSFV1_ERR_ARGUMENT, "newton_solve: null argument"); return D->status; }
+    nsfv1_newton_result res;
+    std::memset(&res, 0, sizeof(res));
+    int st;
+    if (p->jacobian_prec == NSFV1_F64) st = newton_impl<double>(*D, u, u_old, dt, *p, res, (cudaStream_t)stream);
+    else if (p->jacobian_prec == NSFV1_F32) st = newton_impl<float>(*D, u, u_old, dt, *p, res, (cudaStream_t)stream);
+    else { D->fail(NSFV1_ERR_ARGUMENT, "newton_solve: bad precision"); return D->status; }
+    if (res.status == 0 && st != 0) res.status = st;
+    *r = res;
+    return st;
+}
+
+}  // extern "C"

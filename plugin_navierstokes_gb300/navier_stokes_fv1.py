@@ -1,0 +1,196 @@
+"""Host-side mirror of the reference's ``NavierStokesFV1`` element disc.
+
+Same method names, string ids, defaults and error behaviour as the reference
+(incompressible/fv1/navier_stokes_fv1.h:160-225, navier_stokes_base.h:163-196,
+incompressible_navier_stokes_base.h:183-225, registered for Lua in
+incompressible/fv1/register_fv1.cpp:167-184); every call goes through the
+C ABI of ``libnsfv1_gb300.so``. Device vectors are torch CUDA tensors (torch is
+only the device-memory / stream plumbing here).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from ._capi import NSFV1Error, check
+
+
+def _ptr(t) -> int | None:
+    if t is None:
+        return None
+    return t.data_ptr()
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        import torch
+
+        return torch.cuda.current_stream().cuda_stream
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+class NavierStokesFV1:
+    """``NavierStokesFV1(fcts, subsets)`` (navier_stokes_fv1.cpp:45-87) for dim 2 or 3.
+
+    ``functions``/``subsets`` are accepted for API parity; the disc always
+    carries dim+1 P1 functions (u, v, [w], p) like the reference's init check.
+    """
+
+    def __init__(self, functions: str | list[str] = "", subsets: str | list[str] = "", dim: int | None = None):
+        fcts = [f.strip() for f in functions.split(",")] if isinstance(functions, str) else list(functions)
+        fcts = [f for f in fcts if f]
+        if dim is None:
+            dim = len(fcts) - 1 if fcts else 2
+        if fcts and len(fcts) != dim + 1:
+            raise NSFV1Error(_capi.ERR_ARGUMENT, f"Wrong number of functions: The ElemDisc 'NavierStokes' needs exactly {dim + 1} symbolic function.")
+        self.dim = dim
+        self.functions = fcts
+        self.subsets = subsets
+        self._lib = _capi.load()
+        h = ctypes.c_void_p()
+        st = self._lib.nsfv1_create(dim, ctypes.byref(h))
+        if st != _capi.OK:
+            raise NSFV1Error(st, "nsfv1_create failed")
+        self._h = h
+        self.elem_type = None
+        self.n_nodes = 0
+        self.n_elems = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.nsfv1_destroy(h)
+            self._h = None
+
+    def _c(self, st: int) -> None:
+        check(self._h, st)
+
+    # ---- reference setters -------------------------------------------------
+    def disc_type(self) -> str:
+        return self._lib.nsfv1_disc_type(self._h).decode()
+
+    def set_kinematic_viscosity(self, nu: float) -> None:
+        self._c(self._lib.nsfv1_set_kinematic_viscosity(self._h, float(nu)))
+
+    def set_density(self, rho: float) -> None:
+        self._c(self._lib.nsfv1_set_density(self._h, float(rho)))
+
+    def set_source(self, f) -> None:
+        a = np.ascontiguousarray(np.asarray(f, dtype=np.float64))
+        self._c(self._lib.nsfv1_set_source(self._h, a.ctypes.data, a.size))
+
+    def set_exact_jacobian(self, v) -> None:
+        factor = (1.0 if v else 0.0) if isinstance(v, bool) else float(v)
+        self._c(self._lib.nsfv1_set_exact_jacobian(self._h, factor))
+
+    def set_stokes(self, on: bool) -> None:
+        self._c(self._lib.nsfv1_set_stokes(self._h, int(bool(on))))
+
+    def set_laplace(self, on: bool) -> None:
+        self._c(self._lib.nsfv1_set_laplace(self._h, int(bool(on))))
+
+    def set_peclet_blend(self, on: bool) -> None:
+        self._c(self._lib.nsfv1_set_peclet_blend(self._h, int(bool(on))))
+
+    def set_upwind(self, name: str) -> None:
+        self._c(self._lib.nsfv1_set_upwind(self._h, name.encode()))
+
+    def set_stabilization(self, name: str, diff_length: str | None = None) -> None:
+        self._c(self._lib.nsfv1_set_stabilization(self._h, name.encode(), diff_length.encode() if diff_length else None))
+
+    def set_stabilization_upwind(self, name: str) -> None:
+        self._c(self._lib.nsfv1_set_stabilization_upwind(self._h, name.encode()))
+
+    # ---- mesh ----------------------------------------------------------------
+    def set_mesh(self, elem_type: int, coords: np.ndarray, conn: np.ndarray) -> None:
+        coords = np.ascontiguousarray(coords, dtype=np.float64)
+        conn = np.ascontiguousarray(conn, dtype=np.int32)
+        n_nodes = coords.shape[0]
+        n_elems = conn.shape[0]
+        self._c(self._lib.nsfv1_set_mesh(self._h, int(elem_type), n_nodes, coords.ctypes.data, n_elems, conn.ctypes.data))
+        self.elem_type = elem_type
+        self.n_nodes = n_nodes
+        self.n_elems = n_elems
+
+    def pattern_info(self) -> dict:
+        nr, nnz = ctypes.c_int64(), ctypes.c_int64()
+        bs, nc = ctypes.c_int(), ctypes.c_int()
+        self._c(self._lib.nsfv1_pattern_info(self._h, ctypes.byref(nr), ctypes.byref(nnz), ctypes.byref(bs), ctypes.byref(nc)))
+        return {"n_rows": nr.value, "nnz_blocks": nnz.value, "block_size": bs.value, "n_colors": nc.value}
+
+    def pattern(self) -> tuple[np.ndarray, np.ndarray]:
+        info = self.pattern_info()
+        rp = np.empty(info["n_rows"] + 1, np.int32)
+        ci = np.empty(info["nnz_blocks"], np.int32)
+        self._c(self._lib.nsfv1_get_pattern(self._h, rp.ctypes.data, ci.ctypes.data))
+        return rp, ci
+
+    def coloring(self) -> np.ndarray:
+        c = np.empty(self.n_elems, np.int32)
+        self._c(self._lib.nsfv1_get_coloring(self._h, c.ctypes.data))
+        return c
+
+    def set_dirichlet(self, dofs: np.ndarray, values: np.ndarray) -> None:
+        dofs = np.ascontiguousarray(dofs, dtype=np.int32)
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        self._c(self._lib.nsfv1_set_dirichlet(self._h, dofs.size, dofs.ctypes.data, values.ctypes.data))
+
+    # ---- assembly (torch CUDA tensors) ----------------------------------------
+    def assemble_defect(self, u, d, u_old=None, dt: float = 0.0, stream=None) -> None:
+        self._c(self._lib.nsfv1_assemble_defect(self._h, _ptr(u), _ptr(u_old), float(dt), _ptr(d), _stream_ptr(stream)))
+
+    def assemble_jacobian(self, u, vals, u_old=None, dt: float = 0.0, stream=None) -> None:
+        import torch
+
+        prec = _capi.F64 if vals.dtype == torch.float64 else _capi.F32
+        self._c(self._lib.nsfv1_assemble_jacobian(self._h, _ptr(u), _ptr(u_old), float(dt), _ptr(vals), prec, _stream_ptr(stream)))
+
+    def elem_batch(self, elem_type: int, corners, u, u_old=None, dt: float = 0.0, defA=None, jacA=None, defM=None,
+                   jacM=None, rhs=None, stream=None) -> None:
+        n = corners.shape[0]
+        self._c(self._lib.nsfv1_elem_batch(self._h, int(elem_type), n, _ptr(corners), _ptr(u), _ptr(u_old), float(dt),
+                                           _ptr(defA), _ptr(jacA), _ptr(defM), _ptr(jacM), _ptr(rhs), _stream_ptr(stream)))
+
+    def bsr_mv(self, vals, x, y, stream=None) -> None:
+        import torch
+
+        prec = _capi.F64 if vals.dtype == torch.float64 else _capi.F32
+        self._c(self._lib.nsfv1_bsr_mv(self._h, _ptr(vals), prec, _ptr(x), _ptr(y), _stream_ptr(stream)))
+
+    def newton_solve(self, u, u_old=None, dt: float = 0.0, rtol: float = 1e-8, atol: float = 0.0, max_iter: int = 100,
+                     lin_rtol: float = 1e-4, lin_max_iter: int = 2000, line_search_steps: int = 6, jacobian_prec: str = "f64",
+                     linear_solver: str = "bicgstab", gmres_restart: int = 30, stream=None, raise_on_error: bool = True) -> dict:
+        p = _capi.NewtonParams(rtol, atol, max_iter, lin_rtol, lin_max_iter, line_search_steps,
+                               _capi.F64 if jacobian_prec == "f64" else _capi.F32,
+                               _capi.GMRES if linear_solver == "gmres" else _capi.BICGSTAB, gmres_restart)
+        r = _capi.NewtonResult()
+        st = self._lib.nsfv1_newton_solve(self._h, _ptr(u), _ptr(u_old), float(dt), ctypes.byref(p), ctypes.byref(r),
+                                          _stream_ptr(stream))
+        res = {"status": r.status, "iterations": r.iterations, "linear_iterations": r.linear_iterations,
+               "initial_defect": r.initial_defect, "final_defect": r.final_defect}
+        if st != _capi.OK and raise_on_error:
+            raise NSFV1Error(st, self._lib.nsfv1_last_error(self._h).decode() + f" {res}")
+        return res
+
+    def last_error(self) -> str:
+        return self._lib.nsfv1_last_error(self._h).decode()
+
+
+def mesh_pattern(elem_type: int, n_nodes: int, conn: np.ndarray):
+    """Host-only block-CSR pattern + greedy colouring (nsfv1_mesh_pattern)."""
+    lib = _capi.load()
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    nnz, nc = ctypes.c_int64(), ctypes.c_int()
+    st = lib.nsfv1_mesh_pattern(int(elem_type), n_nodes, conn.shape[0], conn.ctypes.data, ctypes.byref(nnz), ctypes.byref(nc), None, None, None)
+    if st != _capi.OK:
+        raise NSFV1Error(st, "nsfv1_mesh_pattern failed")
+    rp = np.empty(n_nodes + 1, np.int32)
+    ci = np.empty(nnz.value, np.int32)
+    col = np.empty(conn.shape[0], np.int32)
+    st = lib.nsfv1_mesh_pattern(int(elem_type), n_nodes, conn.shape[0], conn.ctypes.data, ctypes.byref(nnz), ctypes.byref(nc),
+                                rp.ctypes.data, ci.ctypes.data, col.ctypes.data)
+    if st != _capi.OK:
+        raise NSFV1Error(st, "nsfv1_mesh_pattern failed")
+    return rp, ci, col, nc.value

@@ -1,0 +1,93 @@
+"""The C-ABI library on the host (no GPU compute): symbols, setters, pattern."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from plugin_navierstokes_gb300 import NavierStokesFV1, NSFV1Error, _capi, mesh, mesh_pattern
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _capi.load()
+    syms = _capi.header_symbols()
+    assert len(syms) >= 25
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_setters_string_ids_and_errors():
+    d = NavierStokesFV1("u,v,p", "Inner")
+    assert d.dim == 2 and d.disc_type() == "fv1"
+    for name in ["no", "FULL", " lps ", "LinearProfileSkewed", "skewed"]:
+        d.set_upwind(name)
+    with pytest.raises(NSFV1Error) as ex:
+        d.set_upwind("weighted")
+    assert ex.value.status == _capi.ERR_ARGUMENT and "not found" in str(ex.value)
+    for name in ["fields", "Flow", "without"]:
+        d.set_stabilization(name)
+    d.set_stabilization("fields", "FivePoint")
+    with pytest.raises(NSFV1Error):
+        d.set_stabilization("supg")
+    with pytest.raises(NSFV1Error):
+        d.set_stabilization("fields", "bogus")
+    with pytest.raises(NSFV1Error):
+        d.set_source([1.0, 2.0, 3.0])
+    d.set_source([1.0, 2.0])
+    with pytest.raises(NSFV1Error):
+        NavierStokesFV1("u,v,w,p,q")
+
+
+def test_assembly_without_setup_is_a_state_error():
+    d = NavierStokesFV1("u,v,p")
+    lib = _capi.load()
+    st = lib.nsfv1_assemble_defect(d._h, None, None, 0.0, None, None)
+    assert st == _capi.ERR_STATE
+
+
+@pytest.mark.parametrize("gen", ["quads", "hexes", "tris"])
+def test_pattern_and_coloring_bit_exact_with_oracle(gen):
+    roid, X, C = {"quads": lambda: mesh.structured_quads(7), "hexes": lambda: mesh.structured_hexes(4),
+                  "tris": lambda: mesh.jittered_triangles(6)}[gen]()
+    rp, ci, col, nc = mesh_pattern(roid, X.shape[0], C)
+    o = oracle.Oracle(X.shape[1])
+    o.set_mesh(roid, X, C)
+    orp, oci = o.pattern()
+    ocol, onc = o.coloring()
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    assert np.array_equal(col, ocol) and nc == onc
+
+
+def test_pattern_rejects_bad_connectivity():
+    roid, X, C = mesh.structured_quads(2)
+    C = C.copy(); C[0, 0] = 99
+    with pytest.raises(NSFV1Error):
+        mesh_pattern(roid, X.shape[0], C)
+
+
+@pytest.mark.parametrize("roid", [2, 3, 4, 8])
+def test_reference_tables_match_oracle(roid):
+    lib = _capi.load()
+    nco, ne, ns = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    edges = np.zeros(24, np.int32); snc = np.zeros(6, np.int32); sides = np.zeros(24, np.int32); ef = np.zeros(24, np.int32)
+    assert lib.nsfv1_ref_tables(roid, ctypes.byref(nco), ctypes.byref(ne), edges.ctypes.data, ctypes.byref(ns),
+                                snc.ctypes.data, sides.ctypes.data, ef.ctypes.data) == 0
+    t = oracle.ref_tables(roid)
+    assert nco.value == t["nco"]
+    assert np.array_equal(edges[:2 * ne.value].reshape(-1, 2), t["edges"])
+    assert np.array_equal(snc[:ns.value], t["side_nco"])
+    for s in range(ns.value):
+        assert np.array_equal(sides[4 * s:4 * s + snc[s]], t["sides"][s][:snc[s]])
+    if roid in (4, 8):
+        assert np.array_equal(ef[:2 * ne.value].reshape(-1, 2), t["edge_face"])
+
+
+def test_cavity_dirichlet_rows():
+    roid, X, C = mesh.structured_quads(4)
+    dofs, vals = mesh.cavity_dirichlet(X, 2.0)
+    b = 3
+    nodes = dofs // b
+    assert np.all(np.diff(dofs) > 0)
+    assert (0 * b + 2) in dofs.tolist()
+    lid = [(n, v) for d, n, v in zip(dofs, nodes, vals) if d % b == 0 and v != 0]
+    assert all(abs(X[n, 1] - 1) < 1e-12 and 0 < X[n, 0] < 1 for n, _ in lid) and len(lid) == 3

@@ -1,0 +1,171 @@
+"""GPU parity of the FV1 assembly against the oracle and the golden fixtures.
+
+Tolerance (FP64 path): max |gpu - ref| / max |ref| <= 1e-12 per output array.
+FP32-Jacobian mode: <= 2e-5 against the FP64 oracle Jacobian.
+Integer data (pattern, colouring): bit-exact.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from _cases import CONFIGS, DIM, NSH, ROIDS, cfg_name, configure, random_elements, random_local_u, rel_err
+from plugin_navierstokes_gb300 import NavierStokesFV1, NSFV1Error, mesh
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL64 = 1e-12
+TOL32 = 2e-5
+
+
+def _gpu_elem(cuda, roid, cfg, corners, u, uo, dt=0.01):
+    import torch
+    dim = DIM[roid]
+    d = NavierStokesFV1(dim=dim)
+    configure(d, dim, cfg)
+    n = corners.shape[0]
+    nloc = (dim + 1) * NSH[roid]
+    t = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=cuda)
+    out = {k: torch.zeros((n, nloc), dtype=torch.float64, device=cuda) for k in ("defA", "defM", "rhs")}
+    out.update({k: torch.zeros((n, nloc * nloc), dtype=torch.float64, device=cuda) for k in ("jacA", "jacM")})
+    d.elem_batch(roid, t(corners), t(u), None if uo is None else t(uo), dt, **out)
+    torch.cuda.synchronize()
+    return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+@pytest.mark.parametrize("tname", list(ROIDS))
+@pytest.mark.parametrize("ci", range(len(CONFIGS)))
+def test_element_callbacks_match_golden(cuda, tname, ci):
+    g = np.load(os.path.join(GOLDEN, "elements.npz"))
+    roid = ROIDS[tname]
+    key = f"{tname}_{ci}"
+    uo = g[key + "_uold"] if (key + "_uold") in g else None
+    r = _gpu_elem(cuda, roid, CONFIGS[ci], g[key + "_corners"], g[key + "_u"], uo)
+    for k in ("defA", "jacA", "defM", "jacM", "rhs"):
+        assert rel_err(r[k], g[key + "_" + k]) <= TOL64, (key, cfg_name(CONFIGS[ci]), k, rel_err(r[k], g[key + "_" + k]))
+
+
+@pytest.mark.parametrize("tname", list(ROIDS))
+@pytest.mark.parametrize("ci", range(len(CONFIGS)))
+def test_element_callbacks_match_oracle_random(cuda, tname, ci):
+    roid = ROIDS[tname]
+    dim = DIM[roid]
+    cfg = CONFIGS[ci]
+    n = 257
+    corners = random_elements(roid, n, 9000 + 17 * ci + roid)
+    u = random_local_u(roid, n, 9100 + ci, zero_frac=0.1)
+    uo = random_local_u(roid, n, 9200 + ci) if cfg[3] else None
+    o = oracle.Oracle(dim)
+    configure(o, dim, cfg)
+    ref = o.elem_batch(roid, corners, u, uo, 0.01)
+    r = _gpu_elem(cuda, roid, cfg, corners, u, uo)
+    for k in ref:
+        assert rel_err(r[k], ref[k]) <= TOL64, (tname, cfg_name(cfg), k, rel_err(r[k], ref[k]))
+
+
+def _setup_mesh_pair(name, g):
+    if name == "quad":
+        roid, dim, cfg, U, Uo, dt = 3, 2, CONFIGS[0], g["quad_U"], None, 0.0
+    elif name == "hex":
+        roid, dim, cfg, U, Uo, dt = 8, 3, CONFIGS[1], g["hex_U"], None, 0.0
+    else:
+        roid, dim, cfg, U, Uo, dt = 2, 2, CONFIGS[0], g["tri_U"], g["tri_Uold"], 0.01
+    return roid, dim, cfg, U, Uo, dt
+
+
+@pytest.mark.parametrize("name", ["quad", "hex", "tri"])
+def test_global_assembly_matches_golden(cuda, name):
+    import torch
+    g = np.load(os.path.join(GOLDEN, "meshes.npz"))
+    roid, dim, cfg, U, Uo, dt = _setup_mesh_pair(name, g)
+    d = NavierStokesFV1(dim=dim)
+    configure(d, dim, cfg)
+    d.set_mesh(roid, g[name + "_coords"], g[name + "_conn"])
+    if name + "_dofs" in g:
+        d.set_dirichlet(g[name + "_dofs"], g[name + "_dvals"])
+    rp, ci = d.pattern()
+    assert np.array_equal(rp, g[name + "_rowptr"]) and np.array_equal(ci, g[name + "_colidx"])
+    assert np.array_equal(d.coloring(), g[name + "_color"])
+    tu = torch.tensor(U.ravel(), dtype=torch.float64, device=cuda)
+    tuo = None if Uo is None else torch.tensor(Uo.ravel(), dtype=torch.float64, device=cuda)
+    D = torch.empty_like(tu)
+    b = dim + 1
+    J = torch.empty(ci.size * b * b, dtype=torch.float64, device=cuda)
+    d.assemble_defect(tu, D, tuo, dt)
+    d.assemble_jacobian(tu, J, tuo, dt)
+    torch.cuda.synchronize()
+    assert rel_err(D.cpu().numpy(), g[name + "_D"]) <= TOL64
+    assert rel_err(J.cpu().numpy(), g[name + "_J"]) <= TOL64
+    # FP32-Jacobian mode against the FP64 oracle Jacobian
+    J32 = torch.empty(ci.size * b * b, dtype=torch.float32, device=cuda)
+    d.assemble_jacobian(tu, J32, tuo, dt)
+    torch.cuda.synchronize()
+    assert rel_err(J32.double().cpu().numpy(), g[name + "_J"]) <= TOL32
+    # determinism: a second run is bitwise identical
+    D2 = torch.empty_like(tu)
+    J2 = torch.empty_like(J)
+    d.assemble_defect(tu, D2, tuo, dt)
+    d.assemble_jacobian(tu, J2, tuo, dt)
+    torch.cuda.synchronize()
+    assert torch.equal(D, D2) and torch.equal(J, J2)
+
+
+@pytest.mark.parametrize("gen,cfgi", [("quads", 0), ("quads", 3), ("hexes", 1), ("hexes", 2), ("tris", 4)])
+def test_global_assembly_matches_oracle(cuda, gen, cfgi):
+    import torch
+    roid, X, C = {"quads": lambda: mesh.structured_quads(24), "hexes": lambda: mesh.structured_hexes(6),
+                  "tris": lambda: mesh.jittered_triangles(16, seed=4)}[gen]()
+    dim = DIM[roid]
+    cfg = CONFIGS[cfgi]
+    b = dim + 1
+    U = mesh.solenoidal_state(X, seed=7) if dim == 3 else (mesh.uniform(8, X.shape[0] * 3) * 2 - 1).reshape(-1, 3)
+    Uo = (U * 0.9) if cfg[3] else None
+    dt = 0.01 if cfg[3] else 0.0
+    o = oracle.Oracle(dim); configure(o, dim, cfg); o.set_mesh(roid, X, C)
+    d = NavierStokesFV1(dim=dim); configure(d, dim, cfg); d.set_mesh(roid, X, C)
+    if dim == 2:
+        dofs, vals = mesh.cavity_dirichlet(X, 1.0)
+        o.set_dirichlet(dofs, vals); d.set_dirichlet(dofs, vals)
+    Dref, Jref = o.assemble(U, Uo, dt)
+    tu = torch.tensor(U.ravel(), dtype=torch.float64, device=cuda)
+    tuo = None if Uo is None else torch.tensor(Uo.ravel(), dtype=torch.float64, device=cuda)
+    D = torch.empty_like(tu)
+    J = torch.empty(o.nnzb * b * b, dtype=torch.float64, device=cuda)
+    d.assemble_defect(tu, D, tuo, dt)
+    d.assemble_jacobian(tu, J, tuo, dt)
+    torch.cuda.synchronize()
+    assert rel_err(D.cpu().numpy(), Dref) <= TOL64
+    assert rel_err(J.cpu().numpy(), Jref) <= TOL64
+
+
+def test_bsr_spmv_matches_oracle(cuda):
+    import torch
+    g = np.load(os.path.join(GOLDEN, "meshes.npz"))
+    o = oracle.Oracle(3); configure(o, 3, CONFIGS[1]); o.set_mesh(8, g["hex_coords"], g["hex_conn"])
+    d = NavierStokesFV1(dim=3); configure(d, 3, CONFIGS[1]); d.set_mesh(8, g["hex_coords"], g["hex_conn"])
+    x = mesh.uniform(5, g["hex_U"].size) - 0.5
+    y_ref = o.bsr_mv(g["hex_J"], x)
+    for dt_ in (torch.float64, torch.float32):
+        V = torch.tensor(g["hex_J"], dtype=dt_, device=cuda)
+        tx = torch.tensor(x, dtype=torch.float64, device=cuda)
+        ty = torch.empty_like(tx)
+        d.bsr_mv(V, tx, ty)
+        torch.cuda.synchronize()
+        assert rel_err(ty.cpu().numpy(), y_ref) <= (TOL64 if dt_ == torch.float64 else TOL32)
+
+
+def test_lps_no_cut_side_is_reported(cuda):
+    """A degenerate element (zero volume) makes the LPS ray miss every side: the
+    call returns NSFV1_ERR_GEOMETRY like the reference's UG_THROW, and the
+    handle stays usable."""
+    import torch
+    d = NavierStokesFV1(dim=2)
+    d.set_kinematic_viscosity(0.01); d.set_upwind("lps"); d.set_stabilization("fields")
+    corners = torch.tensor([[[0, 0], [1, 0], [2, 0], [3, 0.0]]], dtype=torch.float64, device=cuda)
+    u = torch.ones((1, 12), dtype=torch.float64, device=cuda)
+    dA = torch.zeros((1, 12), dtype=torch.float64, device=cuda)
+    with pytest.raises(NSFV1Error):
+        d.elem_batch(3, corners, u, defA=dA)
+    ok = torch.tensor(random_elements(3, 1, 1), dtype=torch.float64, device=cuda)
+    d.elem_batch(3, ok, u, defA=dA)
