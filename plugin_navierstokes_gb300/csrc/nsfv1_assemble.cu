@@ -60,13 +60,16 @@ struct GlobalJacSink {
     const int32_t* __restrict__ blk;   // this element's [nsh][nsh] block indices
     template <int b, typename T>
     __device__ __forceinline__ void add(const int i, const int k, const T (&B)[b][b], const bool plus) {
+        // fire-and-forget reductions (executed in L2, no load latency); within a
+        // colour no other thread touches this block and one thread's updates to an
+        // address apply in program order, so the sums stay deterministic
         VT* p = vals + (int64_t)__ldg(blk + i * nsh + k) * (b * b);
 #pragma unroll
         for (int r = 0; r < b; ++r)
 #pragma unroll
             for (int c = 0; c < b; ++c) {
                 const VT v = (VT)B[r][c];
-                p[r * b + c] = plus ? p[r * b + c] + v : p[r * b + c] - v;
+                atomicAdd(p + r * b + c, plus ? v : -v);
             }
     }
 };
@@ -88,44 +91,82 @@ struct LocalJacSink {
 
 // ---- global assembly kernels -------------------------------------------------
 
-template <int ROID>
+// defect sink of the global assembly: reductions into D[node * b + fct]
+template <int nsh, int b>
+struct GlobalDefSink {
+    double* __restrict__ D;
+    int32_t nodes[nsh];
+    __device__ __forceinline__ void add(const int i, const int f, const double v) {
+        int32_t n = nodes[0];
+#pragma unroll
+        for (int k = 1; k < nsh; ++k) n = (k == i) ? nodes[k] : n;
+        atomicAdd(D + (int64_t)n * b + f, v);
+    }
+};
+
+// defect sink of the element-local callbacks: dA[f][corner]
+template <int nsh, int b>
+struct LocalDefSink {
+    double (&dA)[b][nsh];
+    __device__ __forceinline__ void add(const int i, const int f, const double v) {
+#pragma unroll
+        for (int k = 0; k < nsh; ++k)
+            if (k == i) dA[f][k] += v;
+    }
+};
+
+template <int ROID, bool TRANSIENT>
 __global__ void __launch_bounds__(kThreads) k_defect(const DiscParams P, const AsmArgs A) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, b = R::b;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= A.count) return;
     const int32_t e = __ldg(A.elems + t);
-    int32_t nodes[nsh];
+    GlobalDefSink<nsh, b> sink;
+    sink.D = A.D;
 #pragma unroll
-    for (int k = 0; k < nsh; ++k) nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
+    for (int k = 0; k < nsh; ++k) sink.nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
     Elem<ROID, double> E;
-    load_corners<ROID, double>(A.coords, nodes, E);
+    load_corners<ROID, double>(A.coords, sink.nodes, E);
     elem_setup<ROID, double>(E);
-    double u[b][nsh], uo[b][nsh], dA[b][nsh];
-    load_u<ROID, double>(A.U, nodes, u);
-    if (P.transient) load_u<ROID, double>(A.Uold, nodes, uo);
+    double u[b][nsh];
+    load_u<ROID, double>(A.U, sink.nodes, u);
+    double uo[TRANSIENT ? dim : 1][nsh];
+    if constexpr (TRANSIENT) {
+        double t4[b][nsh];
+        load_u<ROID, double>(A.Uold, sink.nodes, t4);
 #pragma unroll
-    for (int f = 0; f < b; ++f)
+        for (int d = 0; d < dim; ++d)
 #pragma unroll
-        for (int k = 0; k < nsh; ++k) dA[f][k] = 0.0;
-    if (!elem_def_A<ROID, double>(P, E, u, uo, dA)) atomicOr(A.err, 1);
+            for (int k = 0; k < nsh; ++k) uo[d][k] = t4[d][k];
+    }
+    DiscParams Q = P;
+    Q.transient = TRANSIENT ? 1 : 0;
+    // the stiffness defect is scaled by dt in the implicit-Euler form: scale the
+    // fluxes through a scaled sink there
+    bool ok;
+    if constexpr (TRANSIENT) {
+        struct Scaled {
+            GlobalDefSink<nsh, b>& s; double dt;
+            __device__ __forceinline__ void add(int i, int f, double v) { s.add(i, f, v * dt); }
+        } ss{sink, P.dt};
+        ok = elem_def_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(uo), ss);
+    } else {
+        ok = elem_def_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(u), sink);
+    }
+    if (!ok) atomicOr(A.err, 1);
+    // mass (implicit Euler) and source parts, per SCV
     const double rho = P.rho;
 #pragma unroll
     for (int k = 0; k < nsh; ++k) {
-        double loc[b];
 #pragma unroll
-        for (int f = 0; f < b; ++f) {
-            double v = dA[f][k];
-            if (f < dim && P.hasSource) v -= P.src[f] * E.vol[k] * rho;
-            if (P.transient) {
-                v = v * P.dt;
-                if (f < dim) v = (u[f][k] * E.vol[k] * rho - uo[f][k] * E.vol[k] * rho) + v;
-            }
-            loc[f] = v;
+        for (int f = 0; f < dim; ++f) {
+            double v = 0.0;
+            bool any = false;
+            if (P.hasSource) { v -= P.src[f] * E.vol[k] * rho; any = true; }
+            if constexpr (TRANSIENT) { v = (u[f][k] * E.vol[k] * rho - uo[f][k] * E.vol[k] * rho) + v * P.dt; any = true; }
+            if (any) atomicAdd(A.D + (int64_t)sink.nodes[k] * b + f, v);
         }
-        double* dp = A.D + (int64_t)nodes[k] * b;
-#pragma unroll
-        for (int f = 0; f < b; ++f) dp[f] += loc[f];
     }
 }
 
@@ -153,7 +194,7 @@ __global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const
         for (int k = 0; k < nsh; ++k) {
             VT* p = sink.vals + (int64_t)__ldg(sink.blk + k * nsh + k) * (b * b);
 #pragma unroll
-            for (int d = 0; d < dim; ++d) p[d * b + d] += (VT)(E.vol[k] * T(P.rho));
+            for (int d = 0; d < dim; ++d) atomicAdd(p + d * b + d, (VT)(E.vol[k] * T(P.rho)));
         }
     }
 }
@@ -188,7 +229,8 @@ __global__ void __launch_bounds__(kThreads) k_elem_batch(const DiscParams P, con
         for (int f = 0; f < b; ++f)
 #pragma unroll
             for (int k = 0; k < nsh; ++k) dA[f][k] = 0.0;
-        if (!elem_def_A<ROID, double>(Q, E, u, uo, dA)) atomicOr(A.err, 1);
+        LocalDefSink<nsh, b> ls{dA};
+        if (!elem_def_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(uo), ls)) atomicOr(A.err, 1);
 #pragma unroll
         for (int f = 0; f < b; ++f)
 #pragma unroll
@@ -263,7 +305,10 @@ static cudaError_t dispatch_roid(int roid, F&& f) {
 cudaError_t launch_defect(int roid, const DiscParams& P, const AsmArgs& a, cudaStream_t s) {
     if (a.count <= 0) return cudaSuccess;
     const int grid = (a.count + kThreads - 1) / kThreads;
-    return dispatch_roid(roid, [&](auto r) { k_defect<decltype(r)::value><<<grid, kThreads, 0, s>>>(P, a); });
+    return dispatch_roid(roid, [&](auto r) {
+        if (P.transient) k_defect<decltype(r)::value, true><<<grid, kThreads, 0, s>>>(P, a);
+        else k_defect<decltype(r)::value, false><<<grid, kThreads, 0, s>>>(P, a);
+    });
 }
 
 cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s) {

@@ -35,6 +35,7 @@ namespace nsfv1 {
 // per-element-type tables (generated at compile time from nsfv1_refelem.cuh)
 // ---------------------------------------------------------------------------
 struct ElemTab {
+    double ipLoc[12][3];   // local (reference) coordinates of the SCVF integration points
     double ipShape[12][8];
     double ipLGrad[12][8][3];
     double refCo[8][3];
@@ -53,6 +54,7 @@ template <int ROID> constexpr ElemTab make_tab() {
             t.ipShape[ip][k] = ip_shape<ROID>(ip, k);
             for (int d = 0; d < R::dim; ++d) t.ipLGrad[ip][k][d] = ip_lgrad<ROID>(ip, k, d);
         }
+        for (int d = 0; d < 3; ++d) t.ipLoc[ip][d] = d < R::dim ? loc_ip<R>(ip, d) : 0.0;
         t.edge[ip][0] = R::edge(ip, 0); t.edge[ip][1] = R::edge(ip, 1);
         t.edgeFace[ip][0] = R::edge_face(ip, 0); t.edgeFace[ip][1] = R::edge_face(ip, 1);
     }
@@ -104,7 +106,72 @@ struct Elem {
     T cen[dim];
     T face[nside][dim];
     T vol[nsh];
+    bool affine;        // the reference mapping is affine (simplex, parallelogram, parallelepiped)
+    T JtInv[3][3];      // constant J^-T of an affine element
 };
+
+// Affine test: simplices always; a quadrilateral / hexahedron when every corner
+// equals x0 + the sum of its edge vectors to within rtol of the element size.
+// On such elements the mapping Jacobian is one constant matrix and the FV1
+// quantities below are evaluated from it (algebraically identical to the
+// per-ip evaluation, equal to rounding).
+// running maximum that propagates NaN (fmax would drop it)
+template <typename T> __device__ __forceinline__ T nanmax(const T a, const T b) { return (b <= a) ? a : b; }
+
+template <int ROID, typename T>
+__device__ __forceinline__ bool elem_is_affine(const Elem<ROID, T>& E) {
+    if constexpr (ROID == ROID_TRIANGLE || ROID == ROID_TETRAHEDRON) return true;
+    const T rtol = sizeof(T) == 8 ? T(1e-14) : T(1e-6);
+    T sz = T(0), dev = T(0);
+    if constexpr (ROID == ROID_QUADRILATERAL) {
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+            sz = nanmax(sz, nanmax(Num<T>::abs_(E.x[1][d] - E.x[0][d]), Num<T>::abs_(E.x[3][d] - E.x[0][d])));
+            dev = nanmax(dev, Num<T>::abs_((E.x[2][d] - E.x[1][d]) - (E.x[3][d] - E.x[0][d])));
+        }
+    } else {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const T a = E.x[1][d] - E.x[0][d], b = E.x[3][d] - E.x[0][d], c = E.x[4][d] - E.x[0][d];
+            sz = nanmax(sz, nanmax(Num<T>::abs_(a), nanmax(Num<T>::abs_(b), Num<T>::abs_(c))));
+            dev = nanmax(dev, Num<T>::abs_((E.x[2][d] - E.x[0][d]) - (a + b)));
+            dev = nanmax(dev, Num<T>::abs_((E.x[5][d] - E.x[0][d]) - (a + c)));
+            dev = nanmax(dev, Num<T>::abs_((E.x[7][d] - E.x[0][d]) - (b + c)));
+            dev = nanmax(dev, Num<T>::abs_((E.x[6][d] - E.x[0][d]) - (a + b + c)));
+        }
+    }
+    return dev <= rtol * sz;   // false when anything is NaN
+}
+
+// J^-T and |det J| from a 2x2 / 3x3 Jacobian
+template <int dim, typename T>
+__device__ __forceinline__ T jt_inverse(const T (&J)[3][3], T (&JtInv)[3][3]) {
+    if constexpr (dim == 2) {
+        const T det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        const T id = T(1) / det;
+        JtInv[0][0] = J[1][1] * id;  JtInv[0][1] = -J[1][0] * id;
+        JtInv[1][0] = -J[0][1] * id; JtInv[1][1] = J[0][0] * id;
+        return det;
+    } else {
+        T C[3][3];
+        C[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        C[0][1] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        C[0][2] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        C[1][0] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+        C[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+        C[1][2] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+        C[2][0] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+        C[2][1] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+        C[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        const T det = J[0][0] * C[0][0] + J[0][1] * C[0][1] + J[0][2] * C[0][2];
+        const T id = T(1) / det;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) JtInv[i][j] = C[i][j] * id;
+        return det;
+    }
+}
 
 // corner 'i' (runtime index) of a register array, by selects (no local memory)
 template <int N, int D, typename T>
@@ -149,6 +216,27 @@ __device__ __forceinline__ void elem_setup(Elem<ROID, T>& E) {
                 for (int j = 0; j < R::side_nco(f); ++j) s += E.x[R::side(f, j)][d];
                 E.face[f][d] = s * T(1.0 / R::side_nco(f));
             }
+    }
+    E.affine = elem_is_affine<ROID, T>(E);
+    if (E.affine) {
+        // constant Jacobian: columns are the edge vectors of the reference axes
+        T J[3][3] = {{T(0), T(0), T(0)}, {T(0), T(0), T(0)}, {T(0), T(0), T(0)}};
+        constexpr int ax1 = (ROID == ROID_QUADRILATERAL || ROID == ROID_HEXAHEDRON) ? 3 : 2;
+        constexpr int ax2 = (ROID == ROID_HEXAHEDRON) ? 4 : 3;
+#pragma unroll
+        for (int r = 0; r < dim; ++r) {
+            J[r][0] = E.x[1][r] - E.x[0][r];
+            J[r][1] = E.x[ax1][r] - E.x[0][r];
+            if constexpr (dim == 3) J[r][2] = E.x[ax2][r] - E.x[0][r];
+        }
+        const T det = jt_inverse<dim, T>(J, E.JtInv);
+        // SCV measure: |det J| x reference measure / number of corners
+        constexpr double frac = ROID == ROID_TRIANGLE ? 1.0 / 6.0 : ROID == ROID_QUADRILATERAL ? 0.25
+                              : ROID == ROID_TETRAHEDRON ? 1.0 / 24.0 : 0.125;
+        const T v = Num<T>::abs_(det) * T(frac);
+#pragma unroll
+        for (int a = 0; a < nsh; ++a) E.vol[a] = v;
+        return;
     }
     // SCV volumes
 #pragma unroll
@@ -222,8 +310,15 @@ __device__ __forceinline__ void ip_geom(const Elem<ROID, T>& E, const int ip, Ip
 #pragma unroll
         for (int d = 0; d < 3; ++d) G.gip[d] = (G.em[d] + f1[d] + E.cen[d] + f2[d]) * T(0.25);
     }
+    if (E.affine) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) G.JtInv[i][j] = E.JtInv[i][j];
+        return;
+    }
     // Jacobian of the reference mapping at the local ip
-    T J[3][3];
+    T J[3][3] = {{T(0), T(0), T(0)}, {T(0), T(0), T(0)}, {T(0), T(0), T(0)}};
 #pragma unroll
     for (int r = 0; r < dim; ++r)
 #pragma unroll
@@ -233,29 +328,7 @@ __device__ __forceinline__ void ip_geom(const Elem<ROID, T>& E, const int ip, Ip
             for (int k = 0; k < nsh; ++k) s += E.x[k][r] * T(tb.ipLGrad[ip][k][c]);
             J[r][c] = s;
         }
-    if constexpr (dim == 2) {
-        const T det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-        const T id = T(1) / det;
-        G.JtInv[0][0] = J[1][1] * id;  G.JtInv[0][1] = -J[1][0] * id;
-        G.JtInv[1][0] = -J[0][1] * id; G.JtInv[1][1] = J[0][0] * id;
-    } else {
-        T C[3][3];
-        C[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-        C[0][1] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-        C[0][2] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-        C[1][0] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
-        C[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
-        C[1][2] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
-        C[2][0] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
-        C[2][1] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
-        C[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-        const T det = J[0][0] * C[0][0] + J[0][1] * C[0][1] + J[0][2] * C[0][2];
-        const T id = T(1) / det;
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) G.JtInv[i][j] = C[i][j] * id;
-    }
+    jt_inverse<dim, T>(J, G.JtInv);
 }
 
 // global gradient of shape k at the SCVF ip
@@ -410,11 +483,92 @@ __device__ __forceinline__ bool ray_upwind(const Elem<ROID, T>& E, const T* from
     return true;
 }
 
+// LPS on an affine element: the upwind ray gip - s vel (s >= 0) in reference
+// coordinates xi(s) = xi_ip - s w, w = J^-1 vel, leaves the reference element
+// through the side with the smallest positive crossing parameter; the shapes are
+// the P1 shapes at the exit point (the exit coordinate is set exactly on its
+// side, so corners off that side get exactly zero) and the convection length is
+// s* |vel|. Same point as the side-by-side ray test, evaluated in closed form.
+template <int ROID, typename T>
+__device__ __forceinline__ bool lps_affine(const Elem<ROID, T>& E, const int ip, const T* vel, const T vnorm,
+                                           T (&up)[Ref<ROID>::nsh], T& convLen) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh;
+    const ElemTab& tb = tab<ROID>();
+    T w[3], xi[3];
+#pragma unroll
+    for (int a = 0; a < dim; ++a) {
+        T s = T(0);
+#pragma unroll
+        for (int r = 0; r < dim; ++r) s += E.JtInv[r][a] * vel[r];
+        w[a] = s;
+        xi[a] = T(tb.ipLoc[ip][a]);
+    }
+    const T inf = T(3.0e38);
+    T best = inf;
+    int side = -1;   // 0..dim-1: axis side at the lower bound (xi_a = 0); dim..2dim-1: upper (xi_a = 1) / simplex diagonal
+#pragma unroll
+    for (int a = 0; a < dim; ++a) {
+        if (w[a] > T(0)) {
+            const T sa = xi[a] / w[a];
+            if (sa < best) { best = sa; side = a; }
+        } else if (w[a] < T(0)) {
+            if constexpr (ROID == ROID_QUADRILATERAL || ROID == ROID_HEXAHEDRON) {
+                const T sa = (T(1) - xi[a]) / (-w[a]);
+                if (sa < best) { best = sa; side = dim + a; }
+            }
+        }
+    }
+    if constexpr (ROID == ROID_TRIANGLE || ROID == ROID_TETRAHEDRON) {
+        T sw = T(0), sx = T(0);
+#pragma unroll
+        for (int a = 0; a < dim; ++a) { sw += w[a]; sx += xi[a]; }
+        if (sw < T(0)) {
+            const T sd = (T(1) - sx) / (-sw);
+            if (sd < best) { best = sd; side = dim; }
+        }
+    }
+    if (side < 0) return false;
+    T li[3];
+#pragma unroll
+    for (int a = 0; a < dim; ++a) li[a] = xi[a] - best * w[a];
+#pragma unroll
+    for (int a = 0; a < dim; ++a) {
+        if (side == a) li[a] = T(0);
+        if (ROID == ROID_QUADRILATERAL || ROID == ROID_HEXAHEDRON) { if (side == dim + a) li[a] = T(1); }
+    }
+#pragma unroll
+    for (int k = 0; k < nsh; ++k) {
+        T v;
+        if constexpr (ROID == ROID_TRIANGLE) v = (k == 0) ? T(1) - li[0] - li[1] : (k == 1 ? li[0] : li[1]);
+        else if constexpr (ROID == ROID_TETRAHEDRON) v = (k == 0) ? T(1) - li[0] - li[1] - li[2] : li[k - 1];
+        else if constexpr (ROID == ROID_QUADRILATERAL) {
+            const T xa = (k == 1 || k == 2) ? li[0] : T(1) - li[0];
+            const T xb = (k == 2 || k == 3) ? li[1] : T(1) - li[1];
+            v = xa * xb;
+        } else {
+            const T xa = (k == 1 || k == 2 || k == 5 || k == 6) ? li[0] : T(1) - li[0];
+            const T xb = (k == 2 || k == 3 || k == 6 || k == 7) ? li[1] : T(1) - li[1];
+            const T xc = (k >= 4) ? li[2] : T(1) - li[2];
+            v = xa * xb * xc;
+        }
+        up[k] = v;
+    }
+    if constexpr (ROID == ROID_TRIANGLE) {
+        // the diagonal side: corner 0 exactly off it
+        if (side == dim) up[0] = T(0);
+    } else if constexpr (ROID == ROID_TETRAHEDRON) {
+        if (side == dim) up[0] = T(0);
+    }
+    convLen = best * vnorm;
+    return true;
+}
+
 // Upwind shapes and convection length of SCVF 'ip' for IP velocity 'vel'.
 // Returns false if a skewed / LPS ray finds no side.
 template <int ROID, typename T>
 __device__ __forceinline__ bool upwind_shapes(const int type, const Elem<ROID, T>& E, const IpGeo<T>& G, const int ip,
-                                              const T* vel, T (&up)[Ref<ROID>::nsh], T& convLen) {
+                                              const T* vel, const T vnorm, T (&up)[Ref<ROID>::nsh], T& convLen) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh;
     if (type == UPW_NO) {
@@ -435,15 +589,13 @@ __device__ __forceinline__ bool upwind_shapes(const int type, const Elem<ROID, T
         return true;
     }
     // skewed / LPS
-    T vv = T(0);
-#pragma unroll
-    for (int d = 0; d < dim; ++d) vv += vel[d] * vel[d];
-    if (Num<T>::sqrt_(vv) < T(1e-14)) {
+    if (vnorm < T(1e-14)) {
 #pragma unroll
         for (int k = 0; k < nsh; ++k) up[k] = T(0);
         convLen = T(1);
         return true;
     }
+    if (type == UPW_LPS && E.affine) return lps_affine<ROID, T>(E, ip, vel, vnorm, up, convLen);
     return ray_upwind<ROID, T>(E, G.gip, vel, type == UPW_LPS, up, convLen);
 }
 
@@ -537,6 +689,10 @@ __device__ __forceinline__ void ip_state(const DiscParams& P, const Elem<ROID, T
         for (int d = 0; d < dim; ++d) S.StdVel[d] += u[d][sh] * N;
     }
     const bool stokes = P.stokes != 0;
+    T vv = T(0);
+#pragma unroll
+    for (int d = 0; d < dim; ++d) vv += S.StdVel[d] * S.StdVel[d];
+    const T norm = Num<T>::sqrt_(vv);   // |StdVel|, also the norm of the negated (downwind) velocity
     T Lup = T(1), Ldown = T(1);
 #pragma unroll
     for (int k = 0; k < nsh; ++k) { S.upS[k] = T(0); S.dnS[k] = T(0); S.upC[k] = T(0); }
@@ -552,7 +708,7 @@ __device__ __forceinline__ void ip_state(const DiscParams& P, const Elem<ROID, T
 #pragma unroll
             for (int d = 0; d < 3; ++d) vel[d] = isDown ? S.StdVel[d] * T(-1) : S.StdVel[d];
             T sh[nsh], L;
-            S.ok &= upwind_shapes<ROID, T>(isConv ? P.convUpwind : P.stabUpwind, E, G, ip, vel, sh, L);
+            S.ok &= upwind_shapes<ROID, T>(isConv ? P.convUpwind : P.stabUpwind, E, G, ip, vel, norm, sh, L);
 #pragma unroll
             for (int k = 0; k < nsh; ++k) {
                 if (isConv) S.upC[k] = sh[k];
@@ -571,10 +727,6 @@ __device__ __forceinline__ void ip_state(const DiscParams& P, const Elem<ROID, T
     const T Linv = diff_len_sq_inv<ROID, T>(P.diffLen, E, G, corMinN, corMinD, corAvgN);
     S.nuL = T(P.nu) * Linv;
     if (!stokes) {
-        T vv = T(0);
-#pragma unroll
-        for (int d = 0; d < dim; ++d) vv += S.StdVel[d] * S.StdVel[d];
-        const T norm = Num<T>::sqrt_(vv);
         S.nsvcl = norm / Lup;
         if (P.stab == STAB_FLOW) S.nsvdl = norm / (Ldown + Lup);
     }
@@ -599,19 +751,20 @@ __device__ __forceinline__ T peclet_blend(const IpGeo<T>& G, const T* StdVel, T 
 }
 
 // ---------------------------------------------------------------------------
-// Local stiffness defect of one element into dA (fct-major [b][nsh]).
+// Local stiffness defect of one element: every SCVF flux is handed to the sink
+// with sink.add(corner, fct, value) (+ at from, - at to).
+// uo is read only when P.transient (pass any array otherwise).
 // Returns false if an upwind ray found no side.
 // ---------------------------------------------------------------------------
-template <int ROID, typename T>
+template <int ROID, typename T, class DSink>
 __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
-                                           const T (&uo)[Ref<ROID>::b][Ref<ROID>::nsh], T (&dA)[Ref<ROID>::b][Ref<ROID>::nsh]) {
+                                           const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], DSink& sink) {
     using R = Ref<ROID>;
-    constexpr int dim = R::dim, nsh = R::nsh, b = R::b, Pc = dim, nip = R::nip;
+    constexpr int dim = R::dim, nsh = R::nsh, Pc = dim, nip = R::nip;
     T corMinN = T(0), corMinD = T(0), corAvgN = T(1);
     if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, T>(E, corMinN, corMinD, corAvgN);
     const T rho = T(P.rho), nu = T(P.nu);
     bool ok = true;
-    T fluxes[nip][b];   // per-SCVF fluxes, scattered to from/to after the loop
 #pragma unroll 1
     for (int ip = 0; ip < nip; ++ip) {
         IpGeo<T> G;
@@ -720,18 +873,11 @@ __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID,
         T contFlux = T(0);
 #pragma unroll
         for (int d = 0; d < dim; ++d) contFlux += stabVel[d] * G.n[d];
+        contFlux *= rho;
 #pragma unroll
-        for (int d1 = 0; d1 < dim; ++d1) fluxes[ip][d1] = flux[d1];
-        fluxes[ip][Pc] = contFlux * rho;
-    }
-    // scatter the SCVF fluxes: + at from, - at to (compile-time indices)
-#pragma unroll
-    for (int ip = 0; ip < nip; ++ip) {
-#pragma unroll
-        for (int f = 0; f < b; ++f) {
-            dA[f][R::edge(ip, 0)] += fluxes[ip][f];
-            dA[f][R::edge(ip, 1)] -= fluxes[ip][f];
-        }
+        for (int d1 = 0; d1 < dim; ++d1) { sink.add(G.from, d1, flux[d1]); sink.add(G.to, d1, -flux[d1]); }
+        sink.add(G.from, Pc, contFlux);
+        sink.add(G.to, Pc, -contFlux);
     }
     return ok;
 }

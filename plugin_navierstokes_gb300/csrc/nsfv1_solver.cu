@@ -30,8 +30,9 @@ __global__ void __launch_bounds__(256) k_bsr_mv(int64_t nRows, const int32_t* __
     const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t row = gid / G;
     const int lane = threadIdx.x % G;
-    if (row >= nRows) return;
-    const int64_t q0 = rowPtr[row], q1 = rowPtr[row + 1];
+    // rows past the end run the (empty) loop so every lane reaches the shuffles
+    const bool valid = row < nRows;
+    const int64_t q0 = valid ? rowPtr[row] : 0, q1 = valid ? rowPtr[row + 1] : 0;
     double acc[b];
 #pragma unroll
     for (int i = 0; i < b; ++i) acc[i] = 0.0;
@@ -48,7 +49,7 @@ __global__ void __launch_bounds__(256) k_bsr_mv(int64_t nRows, const int32_t* __
     for (int off = G / 2; off > 0; off >>= 1)
 #pragma unroll
         for (int r = 0; r < b; ++r) acc[r] += __shfl_down_sync(0xffffffffu, acc[r], off, G);
-    if (lane == 0) {
+    if (valid && lane == 0) {
 #pragma unroll
         for (int r = 0; r < b; ++r) y[row * b + r] = (XT)acc[r];
     }
@@ -455,9 +456,11 @@ static int bicgstab(Disc& D, const VT* J, const VT* Dinv, const VT* rhs, VT* x, 
         if (!read_scal(D, 0, S_NSCAL, s)) return -1;
         const double nr = std::sqrt(W.hscal[S_NR2]);
         *relres = nr / nr0;
-        if (!std::isfinite(nr)) return -1;
+        if (!std::isfinite(nr)) return -1;   // hard failure: x is not usable
         if (*relres < rtol) return it;
-        if (W.hscal[S_FLAG] != 0.0 || W.hscal[S_OMEGA] == 0.0) return -1;
+        // breakdown (rho = 0, (r0, v) = 0 or omega = 0): stop with the last
+        // finite iterate and let the Newton line search judge it
+        if (W.hscal[S_FLAG] != 0.0 || W.hscal[S_OMEGA] == 0.0) return it;
     }
     return maxit;
 }
@@ -545,8 +548,7 @@ static int gmres(Disc& D, const VT* J, const VT* Dinv, const VT* rhs, VT* x, dou
         for (int k = j - 1; k >= 0; --k) {
             double acc = gam[k];
             for (int q = k + 1; q < j; ++q) acc -= H[k * m + q] * y[q];
-            if (H[k * m + k] == 0.0) return -1;
-            y[k] = acc / H[k * m + k];
+            y[k] = (H[k * m + k] != 0.0) ? acc / H[k * m + k] : 0.0;
         }
         std::memcpy(W.hscal + 64, y.data(), sizeof(double) * j);
         cudaMemcpyAsync(hdev, W.hscal + 64, sizeof(double) * j, cudaMemcpyHostToDevice, s);
@@ -589,8 +591,8 @@ static int newton_impl(Disc& D, double* u, const double* u_old, double dt, const
         ++it;
         if (!D.assemble_jacobian(u, u_old, dt, J, prec, s, false)) return D.status;
         cudaMemsetAsync(D.d_err, 0, sizeof(int), s);
-        if (b == 4) k_block_inv<VT, 4><<<grid_for(D.nNodes), 128, 0, s>>>(D.nNodes, W.diagPos, J, Dinv, D.d_err);
-        else k_block_inv<VT, 3><<<grid_for(D.nNodes), 128, 0, s>>>(D.nNodes, W.diagPos, J, Dinv, D.d_err);
+        if (b == 4) k_block_inv<VT, 4><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, W.diagPos, J, Dinv, D.d_err);
+        else k_block_inv<VT, 3><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, W.diagPos, J, Dinv, D.d_err);
         int herr = 0;
         cudaMemcpyAsync(&herr, D.d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (!D.cuda_ok(cudaStreamSynchronize(s), "jacobian")) return D.status;

@@ -156,13 +156,13 @@ def test_bsr_spmv_matches_oracle(cuda):
 
 
 def test_lps_no_cut_side_is_reported(cuda):
-    """A degenerate element (zero volume) makes the LPS ray miss every side: the
-    call returns NSFV1_ERR_GEOMETRY like the reference's UG_THROW, and the
-    handle stays usable."""
+    """An element whose corner coordinate is NaN makes every LPS ray test fail:
+    the call returns NSFV1_ERR_GEOMETRY (the reference's UG_THROW "Cannot find
+    cut side"), and the handle stays usable."""
     import torch
     d = NavierStokesFV1(dim=2)
     d.set_kinematic_viscosity(0.01); d.set_upwind("lps"); d.set_stabilization("fields")
-    corners = torch.tensor([[[0, 0], [1, 0], [2, 0], [3, 0.0]]], dtype=torch.float64, device=cuda)
+    corners = torch.tensor([[[0, 0], [1, 0], [1, float("nan")], [0, 1.0]]], dtype=torch.float64, device=cuda)
     u = torch.ones((1, 12), dtype=torch.float64, device=cuda)
     dA = torch.zeros((1, 12), dtype=torch.float64, device=cuda)
     with pytest.raises(NSFV1Error):
