@@ -143,6 +143,15 @@ int nsfv1_elem_batch(nsfv1_disc* h, int elem_type, int64_t n, const double* corn
 /* y = J x with J in the handle's block CSR (prec as above; x, y FP64) */
 int nsfv1_bsr_mv(nsfv1_disc* h, const void* vals, int prec, const double* x, double* y, void* stream);
 
+/* Point-block Jacobi preconditioner of a Jacobian on the handle's pattern
+ * (the preconditioner of the Newton loop's linear solves): inverts every
+ * b x b diagonal block of vals (prec NSFV1_F64 / NSFV1_F32) in FP64 into
+ * scratch owned by the handle (allocated on first use, nNodes*b*b doubles)
+ * and returns z = D^-1 r (device vectors). NSFV1_ERR_BREAKDOWN on a singular
+ * block. Replaces the core's block-Jacobi preconditioner step of the
+ * reference's linear solver. */
+int nsfv1_block_jacobi(nsfv1_disc* h, const void* vals, int prec, const double* r, double* z, void* stream);
+
 /* ---- Newton solve (the plain method and the FP32-Jacobian mode) ---------- */
 
 typedef struct {

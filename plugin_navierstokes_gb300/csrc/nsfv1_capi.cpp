@@ -76,7 +76,7 @@ template <class T> static cudaError_t dupload(T*& dst, const T* src, size_t n) {
 
 void Disc::free_mesh() {
     dfree(d_coords); dfree(d_conn); dfree(d_elemBlk); dfree(d_colorElems); dfree(d_rowPtr); dfree(d_colIdx);
-    dfree(d_dirRow); dfree(d_dirVal);
+    dfree(d_dirRow); dfree(d_dirVal); dfree(d_diagPos); dfree(d_bjDinv);
 }
 
 Disc::~Disc() {
@@ -316,6 +316,15 @@ int nsfv1_set_mesh(nsfv1_disc* h, int elem_type, int64_t n_nodes, const double* 
             !D->cuda_ok(dupload(D->d_rowPtr, D->rowPtr.data(), D->rowPtr.size()), "upload rowPtr") ||
             !D->cuda_ok(dupload(D->d_colIdx, D->colIdx.data(), D->colIdx.size()), "upload colIdx"))
             return D->status;
+        {
+            std::vector<int32_t> dp(n_nodes);
+            for (int64_t r = 0; r < n_nodes; ++r) {
+                int32_t q = D->rowPtr[r];
+                while (D->colIdx[q] != r) ++q;
+                dp[r] = q;
+            }
+            if (!D->cuda_ok(dupload(D->d_diagPos, dp.data(), dp.size()), "upload diagPos")) return D->status;
+        }
         if (!D->d_err) {
             if (!D->cuda_ok(cudaMalloc((void**)&D->d_err, sizeof(int)), "alloc err")) return D->status;
         }

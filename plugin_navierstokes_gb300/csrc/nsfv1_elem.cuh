@@ -485,57 +485,51 @@ __device__ __forceinline__ bool ray_upwind(const Elem<ROID, T>& E, const T* from
 
 // LPS on an affine element: the upwind ray gip - s vel (s >= 0) in reference
 // coordinates xi(s) = xi_ip - s w, w = J^-1 vel, leaves the reference element
-// through the side with the smallest positive crossing parameter; the shapes are
-// the P1 shapes at the exit point (the exit coordinate is set exactly on its
-// side, so corners off that side get exactly zero) and the convection length is
-// s* |vel|. Same point as the side-by-side ray test, evaluated in closed form.
+// through the side with the smallest crossing parameter s = num/den (ratios are
+// compared by cross-multiplication, one division for the winner); the shapes
+// are the P1 shapes at the exit point (its exit coordinate is set exactly on the
+// side, so corners off the side get exactly zero) and the convection length is
+// s |vel|. The downwind exit (velocity negated, FLOW) uses the same w with the
+// opposite sign. Same point as the side-by-side ray test, in closed form.
 template <int ROID, typename T>
-__device__ __forceinline__ bool lps_affine(const Elem<ROID, T>& E, const int ip, const T* vel, const T vnorm,
+__device__ __forceinline__ bool lps_affine(const ElemTab& tb, const T (&w)[3], const int ip, const bool down, const T vnorm,
                                            T (&up)[Ref<ROID>::nsh], T& convLen) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh;
-    const ElemTab& tb = tab<ROID>();
-    T w[3], xi[3];
+    constexpr bool tensor = (ROID == ROID_QUADRILATERAL || ROID == ROID_HEXAHEDRON);
+    T xi[3];
+#pragma unroll
+    for (int a = 0; a < dim; ++a) xi[a] = T(tb.ipLoc[ip][a]);
+    T bn = T(1), bd = T(0);   // best ratio bn / bd (bd = 0: none yet)
+    int side = -1;            // a: lower side xi_a = 0 ; dim + a: upper side xi_a = 1 (tensor) ; dim: diagonal (simplex)
 #pragma unroll
     for (int a = 0; a < dim; ++a) {
-        T s = T(0);
-#pragma unroll
-        for (int r = 0; r < dim; ++r) s += E.JtInv[r][a] * vel[r];
-        w[a] = s;
-        xi[a] = T(tb.ipLoc[ip][a]);
+        const T wa = down ? -w[a] : w[a];   // the ray moves along -wa
+        T num, den;
+        int sd;
+        if (wa > T(0)) { num = xi[a]; den = wa; sd = a; }
+        else if (tensor && wa < T(0)) { num = T(1) - xi[a]; den = -wa; sd = dim + a; }
+        else continue;
+        if (side < 0 || num * bd < bn * den) { bn = num; bd = den; side = sd; }
     }
-    const T inf = T(3.0e38);
-    T best = inf;
-    int side = -1;   // 0..dim-1: axis side at the lower bound (xi_a = 0); dim..2dim-1: upper (xi_a = 1) / simplex diagonal
-#pragma unroll
-    for (int a = 0; a < dim; ++a) {
-        if (w[a] > T(0)) {
-            const T sa = xi[a] / w[a];
-            if (sa < best) { best = sa; side = a; }
-        } else if (w[a] < T(0)) {
-            if constexpr (ROID == ROID_QUADRILATERAL || ROID == ROID_HEXAHEDRON) {
-                const T sa = (T(1) - xi[a]) / (-w[a]);
-                if (sa < best) { best = sa; side = dim + a; }
-            }
-        }
-    }
-    if constexpr (ROID == ROID_TRIANGLE || ROID == ROID_TETRAHEDRON) {
+    if constexpr (!tensor) {
         T sw = T(0), sx = T(0);
 #pragma unroll
-        for (int a = 0; a < dim; ++a) { sw += w[a]; sx += xi[a]; }
+        for (int a = 0; a < dim; ++a) { sw += down ? -w[a] : w[a]; sx += xi[a]; }
         if (sw < T(0)) {
-            const T sd = (T(1) - sx) / (-sw);
-            if (sd < best) { best = sd; side = dim; }
+            const T num = T(1) - sx, den = -sw;
+            if (side < 0 || num * bd < bn * den) { bn = num; bd = den; side = dim; }
         }
     }
     if (side < 0) return false;
+    const T best = bn / bd;
     T li[3];
 #pragma unroll
-    for (int a = 0; a < dim; ++a) li[a] = xi[a] - best * w[a];
-#pragma unroll
     for (int a = 0; a < dim; ++a) {
+        const T wa = down ? -w[a] : w[a];
+        li[a] = xi[a] - best * wa;
         if (side == a) li[a] = T(0);
-        if (ROID == ROID_QUADRILATERAL || ROID == ROID_HEXAHEDRON) { if (side == dim + a) li[a] = T(1); }
+        if (tensor && side == dim + a) li[a] = T(1);
     }
 #pragma unroll
     for (int k = 0; k < nsh; ++k) {
@@ -554,11 +548,8 @@ __device__ __forceinline__ bool lps_affine(const Elem<ROID, T>& E, const int ip,
         }
         up[k] = v;
     }
-    if constexpr (ROID == ROID_TRIANGLE) {
-        // the diagonal side: corner 0 exactly off it
-        if (side == dim) up[0] = T(0);
-    } else if constexpr (ROID == ROID_TETRAHEDRON) {
-        if (side == dim) up[0] = T(0);
+    if constexpr (!tensor) {
+        if (side == dim) up[0] = T(0);   // the diagonal side does not contain corner 0
     }
     convLen = best * vnorm;
     return true;
@@ -568,7 +559,8 @@ __device__ __forceinline__ bool lps_affine(const Elem<ROID, T>& E, const int ip,
 // Returns false if a skewed / LPS ray finds no side.
 template <int ROID, typename T>
 __device__ __forceinline__ bool upwind_shapes(const int type, const Elem<ROID, T>& E, const IpGeo<T>& G, const int ip,
-                                              const T* vel, const T vnorm, T (&up)[Ref<ROID>::nsh], T& convLen) {
+                                              const T* vel, const T vnorm, const bool down, const T (&wref)[3],
+                                              T (&up)[Ref<ROID>::nsh], T& convLen) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh;
     if (type == UPW_NO) {
@@ -595,7 +587,7 @@ __device__ __forceinline__ bool upwind_shapes(const int type, const Elem<ROID, T
         convLen = T(1);
         return true;
     }
-    if (type == UPW_LPS && E.affine) return lps_affine<ROID, T>(E, ip, vel, vnorm, up, convLen);
+    if (type == UPW_LPS && E.affine) return lps_affine<ROID, T>(tab<ROID>(), wref, ip, down, vnorm, up, convLen);
     return ray_upwind<ROID, T>(E, G.gip, vel, type == UPW_LPS, up, convLen);
 }
 
@@ -625,12 +617,14 @@ __device__ __forceinline__ T diff_len_sq_inv(const int type, const Elem<ROID, T>
 #pragma unroll
         for (int d = 0; d < 3; ++d) { const T x = G.em[d] - E.cen[d]; ds += x * x; }
     }
+    // one division each: 2 nn/A + 8 ds/nn = (2 nn^2 + 8 ds A) / (A nn)   (2D: ds -> 1) and
+    // 1 / (0.5 A/nn + 3 ds/8) = nn / (0.5 A + 0.375 ds nn)               (2D: ds -> nn)
     if (type == DL_FIVEPOINT) {
-        if constexpr (dim == 2) return T(2.0) * nn / area + T(8.0) / nn;
-        else return T(2.0) * nn / area + T(8.0) * ds / nn;
+        if constexpr (dim == 2) return (T(2.0) * nn * nn + T(8.0) * area) / (area * nn);
+        else return (T(2.0) * nn * nn + T(8.0) * ds * area) / (area * nn);
     }
-    if constexpr (dim == 2) return T(1.0) / (T(0.5) * area / nn + T(3.0) * nn / T(8.0));
-    else return T(1.0) / (T(0.5) * area / nn + T(3.0) * ds / T(8.0));
+    if constexpr (dim == 2) ds = nn;
+    return nn / (T(0.5) * area + T(0.375) * ds * nn);
 }
 
 template <int ROID, typename T>
@@ -696,6 +690,17 @@ __device__ __forceinline__ void ip_state(const DiscParams& P, const Elem<ROID, T
     T Lup = T(1), Ldown = T(1);
 #pragma unroll
     for (int k = 0; k < nsh; ++k) { S.upS[k] = T(0); S.dnS[k] = T(0); S.upC[k] = T(0); }
+    // J^-1 StdVel (reference-coordinate velocity) for the affine LPS exits
+    T wref[3] = {T(0), T(0), T(0)};
+    if (!stokes && E.affine && (P.stabUpwind == UPW_LPS || P.convUpwind == UPW_LPS)) {
+#pragma unroll
+        for (int a = 0; a < dim; ++a) {
+            T s = T(0);
+#pragma unroll
+            for (int r = 0; r < dim; ++r) s += E.JtInv[r][a] * S.StdVel[r];
+            wref[a] = s;
+        }
+    }
     if (!stokes) {
         // the stabilisation's upwind (and downwind for FLOW) first, then the
         // convection's own upwind when it is a different object
@@ -708,7 +713,7 @@ __device__ __forceinline__ void ip_state(const DiscParams& P, const Elem<ROID, T
 #pragma unroll
             for (int d = 0; d < 3; ++d) vel[d] = isDown ? S.StdVel[d] * T(-1) : S.StdVel[d];
             T sh[nsh], L;
-            S.ok &= upwind_shapes<ROID, T>(isConv ? P.convUpwind : P.stabUpwind, E, G, ip, vel, norm, sh, L);
+            S.ok &= upwind_shapes<ROID, T>(isConv ? P.convUpwind : P.stabUpwind, E, G, ip, vel, norm, isDown, wref, sh, L);
 #pragma unroll
             for (int k = 0; k < nsh; ++k) {
                 if (isConv) S.upC[k] = sh[k];
@@ -772,24 +777,31 @@ __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID,
         IpState<ROID, T> S;
         ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, S);
         ok &= S.ok;
-        // velocity gradient, pressure gradient
+        // velocity and pressure gradients: local gradients first, then one J^-T
+        // (grad_k = J^-T lgrad_k, so sum_k u_k grad_k = J^-T sum_k u_k lgrad_k)
         T gradVel[3][3], gradP[3];
+        {
+            const ElemTab& tb = tab<ROID>();
+            T gl[4][3];
 #pragma unroll
-        for (int d1 = 0; d1 < 3; ++d1) {
-            gradP[d1] = T(0);
+            for (int f = 0; f <= dim; ++f)
 #pragma unroll
-            for (int d2 = 0; d2 < 3; ++d2) gradVel[d1][d2] = T(0);
-        }
+                for (int c = 0; c < dim; ++c) {
+                    T acc = T(0);
 #pragma unroll
-        for (int sh = 0; sh < nsh; ++sh) {
-            T g[3];
-            ip_grad<ROID, T>(G, ip, sh, g);
+                    for (int sh = 0; sh < nsh; ++sh) acc += u[f][sh] * T(tb.ipLGrad[ip][sh][c]);
+                    gl[f][c] = acc;
+                }
 #pragma unroll
-            for (int d1 = 0; d1 < dim; ++d1) {
+            for (int f = 0; f <= dim; ++f)
 #pragma unroll
-                for (int d2 = 0; d2 < dim; ++d2) gradVel[d1][d2] += g[d2] * u[d1][sh];
-                gradP[d1] += g[d1] * u[Pc][sh];
-            }
+                for (int d2 = 0; d2 < dim; ++d2) {
+                    T acc = T(0);
+#pragma unroll
+                    for (int c = 0; c < dim; ++c) acc += G.JtInv[d2][c] * gl[f][c];
+                    if (f < dim) gradVel[f][d2] = acc;
+                    else gradP[d2] = acc;
+                }
         }
         // diffusion
         T flux[3];
@@ -805,6 +817,7 @@ __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID,
             flux[d1] = s * (T(-1.0) * nu * rho);
         }
         // convection
+        T UpVelShared[3] = {T(0), T(0), T(0)};   // upwind velocity before blending (= the stabilisation's when shared)
         if (!P.stokes) {
             T UpwindVel[3];
 #pragma unroll
@@ -813,6 +826,7 @@ __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID,
 #pragma unroll
                 for (int sh = 0; sh < nsh; ++sh) s += S.upC[sh] * u[d][sh];
                 UpwindVel[d] = s;
+                UpVelShared[d] = s;
             }
             if (P.peclet) peclet_blend<ROID, T>(G, S.StdVel, nu, UpwindVel);
             T prod = T(0);
@@ -851,9 +865,10 @@ __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID,
                 rhs += S.nuL * S.StdVel[d];
                 if (!P.stokes) {
                     T UpS = T(0), DnS = T(0);
+                    if (P.sameUpwind) UpS = UpVelShared[d];
 #pragma unroll
                     for (int sh = 0; sh < nsh; ++sh) {
-                        UpS += S.upS[sh] * u[d][sh];
+                        if (!P.sameUpwind) UpS += S.upS[sh] * u[d][sh];
                         if (P.stab == STAB_FLOW) DnS += S.dnS[sh] * u[d][sh];
                     }
                     rhs += S.nsvcl * UpS;
@@ -922,6 +937,11 @@ __device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID,
         }
         const T idiag = (P.stab == STAB_WITHOUT) ? T(0) : T(1) / S.diag;
         const T ri = rho * idiag;
+        // per-SCVF factors of the column loop
+        T mn[3], rin[3], nrho[3];
+#pragma unroll
+        for (int d = 0; d < dim; ++d) { mn[d] = mnr * G.n[d]; rin[d] = ri * G.n[d]; nrho[d] = G.n[d] * rho; }
+        const T riVn = ri * Vn, pw = prod * w, ppe = prod * (T(1) - w), ppr = -ri / rho;
 #pragma unroll
         for (int k = 0; k < nsh; ++k) {
             T g[3];
@@ -931,43 +951,38 @@ __device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID,
 #pragma unroll
             for (int d = 0; d < dim; ++d) { gn += g[d] * G.n[d]; Vg += S.StdVel[d] * g[d]; }
             T B[b][b];
+            // diffusion: -nu rho ((g.n) I + g (x) n)
+            T dd = mnr * gn;
+            // convection (fixpoint part) on the diagonal
+            if (!P.stokes) {
+                dd += S.upC[k] * pw;
+                if (P.peclet) dd += ppe * N;
+            }
 #pragma unroll
-            for (int r = 0; r < b; ++r)
+            for (int d1 = 0; d1 < dim; ++d1)
 #pragma unroll
-                for (int c = 0; c < b; ++c) B[r][c] = T(0);
-            // diffusion
-            const T flux_sh = mnr * gn;
+                for (int d2 = 0; d2 < dim; ++d2) {
+                    T v = P.laplace ? T(0) : g[d1] * mn[d2];
+                    if (d1 == d2) v += dd;
+                    B[d1][d2] = v;
+                }
+            if (!P.stokes && P.fullNewton != 0.0) {
 #pragma unroll
-            for (int d1 = 0; d1 < dim; ++d1) {
-                B[d1][d1] += flux_sh;
-                if (!P.laplace) {
+                for (int d2 = 0; d2 < dim; ++d2) {
+                    T pv = w * S.upC[k] * nrho[d2];
+                    if (P.peclet) pv += (T(1) - w) * N * nrho[d2];
 #pragma unroll
-                    for (int d2 = 0; d2 < dim; ++d2) B[d1][d2] += mnr * g[d1] * G.n[d2];
+                    for (int d1 = 0; d1 < dim; ++d1) B[d1][d2] += pv * UpwindVel[d1];
                 }
             }
             // pressure
 #pragma unroll
-            for (int d1 = 0; d1 < dim; ++d1) B[d1][Pc] += N * G.n[d1];
-            // convection
-            if (!P.stokes) {
-                T diagConv = S.upC[k] * (prod * w);
-                if (P.peclet) diagConv += prod * (T(1) - w) * N;
-#pragma unroll
-                for (int d1 = 0; d1 < dim; ++d1) B[d1][d1] += diagConv;
-                if (P.fullNewton != 0.0) {
-#pragma unroll
-                    for (int d2 = 0; d2 < dim; ++d2) {
-                        T pv = w * S.upC[k] * G.n[d2] * rho;
-                        if (P.peclet) pv += (T(1) - w) * N * G.n[d2] * rho;
-#pragma unroll
-                        for (int d1 = 0; d1 < dim; ++d1) B[d1][d2] += pv * UpwindVel[d1];
-                    }
-                }
-            }
+            for (int d1 = 0; d1 < dim; ++d1) B[d1][Pc] = N * G.n[d1];
             // continuity
             if (P.stab == STAB_WITHOUT) {
 #pragma unroll
-                for (int d1 = 0; d1 < dim; ++d1) B[Pc][d1] = N * G.n[d1] * rho;
+                for (int d1 = 0; d1 < dim; ++d1) B[Pc][d1] = N * nrho[d1];
+                B[Pc][Pc] = T(0);
             } else {
                 T Sk = S.nuL * N;
                 if (!P.stokes) {
@@ -975,13 +990,14 @@ __device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID,
                     if (P.stab == STAB_FLOW) Sk += S.nsvdl * (S.dnS[k] - S.upS[k]);
                 }
                 if (P.stab == STAB_FLOW) {
+                    const T sv = Sk - Vg;
 #pragma unroll
-                    for (int d1 = 0; d1 < dim; ++d1) B[Pc][d1] = ri * ((Sk - Vg) * G.n[d1] + Vn * g[d1]);
+                    for (int d1 = 0; d1 < dim; ++d1) B[Pc][d1] = sv * rin[d1] + riVn * g[d1];
                 } else {
 #pragma unroll
-                    for (int d1 = 0; d1 < dim; ++d1) B[Pc][d1] = ri * Sk * G.n[d1];
+                    for (int d1 = 0; d1 < dim; ++d1) B[Pc][d1] = Sk * rin[d1];
                 }
-                B[Pc][Pc] = -(gn / rho) * ri;
+                B[Pc][Pc] = gn * ppr;
             }
             if (scale != T(1)) {
 #pragma unroll

@@ -24,7 +24,6 @@ struct Workspace {
     double* red = nullptr;    // reduction partials
     double* scal = nullptr;   // device scalars
     double* hscal = nullptr;  // pinned host mirror of the scalars
-    int32_t* diagPos = nullptr;
 };
 
 struct Disc {
@@ -43,6 +42,8 @@ struct Disc {
     std::vector<int32_t> rowPtr, colIdx, elemBlk, color, colorPtr, colorElems;
     double* d_coords = nullptr;
     int32_t *d_conn = nullptr, *d_elemBlk = nullptr, *d_colorElems = nullptr, *d_rowPtr = nullptr, *d_colIdx = nullptr;
+    int32_t* d_diagPos = nullptr;   // block index of each row's diagonal block
+    double* d_bjDinv = nullptr;     // nsfv1_block_jacobi scratch: inverted diagonal blocks
     int32_t* d_dirRow = nullptr;
     double* d_dirVal = nullptr;
     int64_t nDir = 0;
@@ -64,5 +65,9 @@ struct Disc {
     bool assemble_jacobian(const double* u, const double* u_old, double dt, void* vals, int prec, cudaStream_t s, bool sync = true);
     bool ensure_workspace(int prec, int gmresM);
 };
+
+// point-block Jacobi on a caller's Jacobian with Dinv as scratch (nNodes*b*b
+// doubles): shared by nsfv1_block_jacobi and its variant without allocation
+bool block_jacobi_run(Disc& D, const void* vals, int prec, const double* r, double* z, double* Dinv, cudaStream_t s);
 
 }  // namespace nsfv1

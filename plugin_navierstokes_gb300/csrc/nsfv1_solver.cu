@@ -56,8 +56,8 @@ __global__ void __launch_bounds__(256) k_bsr_mv(int64_t nRows, const int32_t* __
 }
 
 // inverse of the diagonal blocks (Gauss-Jordan, partial pivoting); err bit 2 on a zero pivot
-template <typename VT, int b>
-__global__ void k_block_inv(int64_t nRows, const int32_t* __restrict__ diagPos, const VT* __restrict__ vals, VT* __restrict__ Dinv, int* err) {
+template <typename VT, typename OT, int b>
+__global__ void k_block_inv(int64_t nRows, const int32_t* __restrict__ diagPos, const VT* __restrict__ vals, OT* __restrict__ Dinv, int* err) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nRows) return;
     double M[b][2 * b];
@@ -89,11 +89,11 @@ __global__ void k_block_inv(int64_t nRows, const int32_t* __restrict__ diagPos, 
         }
     }
     if (!ok) { atomicOr(err, 2); return; }
-    VT* O = Dinv + r * b * b;
+    OT* O = Dinv + r * b * b;
 #pragma unroll
     for (int i = 0; i < b; ++i)
 #pragma unroll
-        for (int j = 0; j < b; ++j) O[i * b + j] = (VT)M[i][b + j];
+        for (int j = 0; j < b; ++j) O[i * b + j] = (OT)M[i][b + j];
 }
 
 template <typename VT, int b>
@@ -368,7 +368,7 @@ namespace nsfv1 {
 
 void Disc::free_workspace() {
     auto f = [](auto*& p) { if (p) cudaFree((void*)p); p = nullptr; };
-    f(ws.D); f(ws.Dt); f(ws.Ut); f(ws.du); f(ws.J); f(ws.Dinv); f(ws.vec); f(ws.red); f(ws.scal); f(ws.diagPos);
+    f(ws.D); f(ws.Dt); f(ws.Ut); f(ws.du); f(ws.J); f(ws.Dinv); f(ws.vec); f(ws.red); f(ws.scal);
     if (ws.hscal) cudaFreeHost(ws.hscal);
     ws = Workspace();
 }
@@ -384,16 +384,9 @@ bool Disc::ensure_workspace(int prec, int gmresM) {
     if (!al(ws.D, n * 8) || !al(ws.Dt, n * 8) || !al(ws.Ut, n * 8) || !al(ws.du, n * 8) ||
         !al(ws.J, colIdx.size() * b * b * vt) || !al(ws.Dinv, (size_t)nNodes * b * b * vt) ||
         !al(ws.vec, (size_t)nvec * n * vt) || !al(ws.red, sizeof(double) * kRedBlocks * 80) ||
-        !al(ws.scal, sizeof(double) * 256) || !al(ws.diagPos, sizeof(int32_t) * nNodes))
+        !al(ws.scal, sizeof(double) * 256))
         return false;
     if (!cuda_ok(cudaMallocHost((void**)&ws.hscal, sizeof(double) * 256), "pinned alloc")) return false;
-    std::vector<int32_t> dp(nNodes);
-    for (int64_t r = 0; r < nNodes; ++r) {
-        int32_t q = rowPtr[r];
-        while (colIdx[q] != r) ++q;
-        dp[r] = q;
-    }
-    if (!cuda_ok(cudaMemcpy(ws.diagPos, dp.data(), sizeof(int32_t) * nNodes, cudaMemcpyHostToDevice), "diagPos")) return false;
     ws.prec = prec; ws.n = n; ws.nvec = nvec; ws.gmresM = gmresM;
     return true;
 }
@@ -591,8 +584,8 @@ static int newton_impl(Disc& D, double* u, const double* u_old, double dt, const
         ++it;
         if (!D.assemble_jacobian(u, u_old, dt, J, prec, s, false)) return D.status;
         cudaMemsetAsync(D.d_err, 0, sizeof(int), s);
-        if (b == 4) k_block_inv<VT, 4><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, W.diagPos, J, Dinv, D.d_err);
-        else k_block_inv<VT, 3><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, W.diagPos, J, Dinv, D.d_err);
+        if (b == 4) k_block_inv<VT, VT, 4><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, J, Dinv, D.d_err);
+        else k_block_inv<VT, VT, 3><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, J, Dinv, D.d_err);
         int herr = 0;
         cudaMemcpyAsync(&herr, D.d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (!D.cuda_ok(cudaStreamSynchronize(s), "jacobian")) return D.status;
@@ -630,6 +623,32 @@ static int newton_impl(Disc& D, double* u, const double* u_old, double dt, const
 
 }  // namespace
 
+namespace nsfv1 {
+// point-block Jacobi on a caller's Jacobian: Dinv (FP64 scratch) = inverse
+// diagonal blocks, z = Dinv r.
+bool block_jacobi_run(Disc& D, const void* vals, int prec, const double* r, double* z, double* Dinv, cudaStream_t s) {
+    const int b = D.dim + 1;
+    const int64_t nR = D.nNodes;
+    if (!D.cuda_ok(cudaMemsetAsync(D.d_err, 0, sizeof(int), s), "block_jacobi")) return false;
+    const int g = grid_for(nR, 128);
+    if (prec == NSFV1_F64) {
+        if (b == 4) k_block_inv<double, double, 4><<<g, 128, 0, s>>>(nR, D.d_diagPos, (const double*)vals, Dinv, D.d_err);
+        else k_block_inv<double, double, 3><<<g, 128, 0, s>>>(nR, D.d_diagPos, (const double*)vals, Dinv, D.d_err);
+    } else {
+        if (b == 4) k_block_inv<float, double, 4><<<g, 128, 0, s>>>(nR, D.d_diagPos, (const float*)vals, Dinv, D.d_err);
+        else k_block_inv<float, double, 3><<<g, 128, 0, s>>>(nR, D.d_diagPos, (const float*)vals, Dinv, D.d_err);
+    }
+    if (b == 4) k_prec<double, 4><<<grid_for(nR), 256, 0, s>>>(nR, Dinv, r, z);
+    else k_prec<double, 3><<<grid_for(nR), 256, 0, s>>>(nR, Dinv, r, z);
+    if (!D.cuda_ok(cudaGetLastError(), "block_jacobi launch")) return false;
+    int err = 0;
+    if (!D.cuda_ok(cudaMemcpyAsync(&err, D.d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "block_jacobi")) return false;
+    if (!D.cuda_ok(cudaStreamSynchronize(s), "block_jacobi sync")) return false;
+    if (err & 2) return D.fail(NSFV1_ERR_BREAKDOWN, "block_jacobi: singular diagonal block");
+    return true;
+}
+}  // namespace nsfv1
+
 extern "C" {
 
 int nsfv1_bsr_mv(nsfv1_disc* h, const void* vals, int prec, const double* x, double* y, void* stream) {
@@ -650,6 +669,18 @@ int nsfv1_bsr_mv(nsfv1_disc* h, const void* vals, int prec, const double* x, dou
         return D->status;
     }
     return D->cuda_ok(cudaGetLastError(), "bsr_mv") ? NSFV1_OK : D->status;
+}
+
+int nsfv1_block_jacobi(nsfv1_disc* h, const void* vals, int prec, const double* r, double* z, void* stream) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "block_jacobi: no mesh"); return D->status; }
+    if (!vals || !r || !z || (prec != NSFV1_F64 && prec != NSFV1_F32)) { D->fail(NSFV1_ERR_ARGUMENT, "block_jacobi: bad arguments"); return D->status; }
+    const int b = D->dim + 1;
+    if (!D->d_bjDinv && !D->cuda_ok(cudaMalloc((void**)&D->d_bjDinv, sizeof(double) * D->nNodes * b * b), "block_jacobi scratch"))
+        return D->status;
+    return block_jacobi_run(*D, vals, prec, r, z, D->d_bjDinv, (cudaStream_t)stream) ? NSFV1_OK : D->status;
 }
 
 int nsfv1_newton_solve(nsfv1_disc* h, double* u, const double* u_old, double dt, const nsfv1_newton_params* p,

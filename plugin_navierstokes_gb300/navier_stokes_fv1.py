@@ -159,6 +159,13 @@ class NavierStokesFV1:
         prec = _capi.F64 if vals.dtype == torch.float64 else _capi.F32
         self._c(self._lib.nsfv1_bsr_mv(self._h, _ptr(vals), prec, _ptr(x), _ptr(y), _stream_ptr(stream)))
 
+    def block_jacobi(self, vals, r, z, stream=None) -> None:
+        """z = D^-1 r with D the block diagonal of the Jacobian vals."""
+        import torch
+
+        prec = _capi.F64 if vals.dtype == torch.float64 else _capi.F32
+        self._c(self._lib.nsfv1_block_jacobi(self._h, _ptr(vals), prec, _ptr(r), _ptr(z), _stream_ptr(stream)))
+
     def newton_solve(self, u, u_old=None, dt: float = 0.0, rtol: float = 1e-8, atol: float = 0.0, max_iter: int = 100,
                      lin_rtol: float = 1e-4, lin_max_iter: int = 2000, line_search_steps: int = 6, jacobian_prec: str = "f64",
                      linear_solver: str = "bicgstab", gmres_restart: int = 30, stream=None, raise_on_error: bool = True) -> dict:

@@ -169,3 +169,25 @@ def test_lps_no_cut_side_is_reported(cuda):
         d.elem_batch(3, corners, u, defA=dA)
     ok = torch.tensor(random_elements(3, 1, 1), dtype=torch.float64, device=cuda)
     d.elem_batch(3, ok, u, defA=dA)
+
+
+@pytest.mark.parametrize("gen", ["quads", "hexes"])
+def test_block_jacobi_matches_numpy(cuda, gen):
+    import torch
+    roid, X, C = {"quads": lambda: mesh.structured_quads(12), "hexes": lambda: mesh.structured_hexes(4)}[gen]()
+    dim = DIM[roid]
+    b = dim + 1
+    d = NavierStokesFV1(dim=dim); configure(d, dim, CONFIGS[0] if dim == 2 else CONFIGS[1]); d.set_mesh(roid, X, C)
+    U = mesh.solenoidal_state(X, seed=3) if dim == 3 else (mesh.uniform(8, X.shape[0] * 3) * 2 - 1).reshape(-1, 3)
+    rp, ci = d.pattern()
+    tu = torch.tensor(U.ravel(), dtype=torch.float64, device=cuda)
+    J = torch.empty(ci.size * b * b, dtype=torch.float64, device=cuda)
+    d.assemble_jacobian(tu, J)
+    r = torch.tensor(mesh.uniform(4, tu.numel()) - 0.5, dtype=torch.float64, device=cuda)
+    z = torch.empty_like(r)
+    d.block_jacobi(J, r, z)
+    torch.cuda.synchronize()
+    Jh = J.cpu().numpy().reshape(-1, b, b)
+    diag = np.array([Jh[rp[i] + np.searchsorted(ci[rp[i]:rp[i + 1]], i)] for i in range(X.shape[0])])
+    zref = np.einsum("nij,nj->ni", np.linalg.inv(diag), r.cpu().numpy().reshape(-1, b)).ravel()
+    assert rel_err(z.cpu().numpy(), zref) <= TOL64
