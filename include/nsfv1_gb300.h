@@ -152,6 +152,20 @@ int nsfv1_bsr_mv(nsfv1_disc* h, const void* vals, int prec, const double* x, dou
  * reference's linear solver. */
 int nsfv1_block_jacobi(nsfv1_disc* h, const void* vals, int prec, const double* r, double* z, void* stream);
 
+/* Largest mesh (nodes) that nsfv1_block_jacobi_noalloc accepts. */
+#define NSFV1_NOALLOC_MAX_NODES 32768
+
+/* The same preconditioner as nsfv1_block_jacobi, allocating nothing: for
+ * callers whose device memory belongs to their own pool allocator, or whose
+ * solver loop cannot absorb cudaMalloc's implicit synchronisation. No
+ * counterpart in the reference (its CPU preconditioner allocates freely).
+ * The scratch is a fixed 4 MiB device array inside the library, shared by all
+ * calls; meshes above NSFV1_NOALLOC_MAX_NODES nodes are rejected with
+ * NSFV1_ERR_ARGUMENT. The first call on a device looks the array up with
+ * cudaGetSymbolAddress and should come before any stream capture. Calls that
+ * overlap on the GPU race on the shared array and must be serialised. */
+int nsfv1_block_jacobi_noalloc(nsfv1_disc* h, const void* vals, int prec, const double* r, double* z, void* stream);
+
 /* ---- Newton solve (the plain method and the FP32-Jacobian mode) ---------- */
 
 typedef struct {
