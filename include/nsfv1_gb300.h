@@ -197,6 +197,31 @@ typedef struct {
 int nsfv1_newton_solve(nsfv1_disc* h, double* u, const double* u_old, double dt, const nsfv1_newton_params* p,
                        nsfv1_newton_result* r, void* stream);
 
+/* ---- many independent instances (batched cavities) ------------------------ */
+
+/* Per-element kinematic viscosity (host array [n_elems]), replacing the
+ * constant of nsfv1_set_kinematic_viscosity; NULL returns to the constant.
+ * (The reference takes any CplUserData viscosity, navier_stokes_fv1.cpp:109-114.) */
+int nsfv1_set_elem_viscosity(nsfv1_disc* h, const double* nu);
+/* Declares the mesh as n_inst independent instances: node ranges
+ * [node_offsets[i], node_offsets[i+1]) (host array [n_inst+1], from 0 to
+ * n_nodes); no element may span two instances. */
+int nsfv1_set_instances(nsfv1_disc* h, int n_inst, const int32_t* node_offsets);
+
+typedef struct {
+    int cluster_size;   /* CTAs per thread-block cluster working on one instance (1..16; 0 = 4) */
+    int max_clusters;   /* upper bound on concurrently resident clusters (0 = as many as fit)  */
+} nsfv1_batch_options;
+
+/* Newton on every instance at once (each to its own ||d_i|| <= rtol ||d_i,0||):
+ * one assembly pass over all unconverged instances per step, then ONE
+ * persistent launch of a cluster-per-instance restarted GMRES (right
+ * point-block Jacobi, restart p->gmres_restart <= 32) over the unconverged
+ * instances, then a per-instance backtracking line search. results[n_inst]
+ * receives each instance's iterations, linear iterations, defects and status. */
+int nsfv1_newton_solve_batched(nsfv1_disc* h, double* u, const double* u_old, double dt, const nsfv1_newton_params* p,
+                               const nsfv1_batch_options* opt, nsfv1_newton_result* results, void* stream);
+
 /* reference-element tables used by the kernels (for the table-consistency test):
  * edges[2*nedge], sides[4*nside] (unused slots -1), side_nco[nside], edge_face[2*nedge] */
 int nsfv1_ref_tables(int elem_type, int* nco, int* nedge, int* edges, int* nside, int* side_nco, int* sides, int* edge_face);

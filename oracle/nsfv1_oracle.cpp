@@ -1197,15 +1197,17 @@ static int bicgstab(const Mesh& m, int b, const number* V, const number* Dinv, c
     r0 = r;
     number rho = 1, alpha = 1, omega = 1;
     std::fill(p.begin(), p.end(), 0.0); std::fill(v.begin(), v.end(), 0.0);
+    // breakdowns (rho = 0, (r0, v) = 0, (t, t) = 0, omega = 0) stop the iteration
+    // with the last finite iterate; only a non-finite residual is a failure
     for (int it = 1; it <= maxit; ++it) {
         const number rho1 = dot(n, r0.data(), r.data());
-        if (rho1 == 0.0) return -1;
+        if (rho1 == 0.0) return it - 1;
         const number beta = (rho1 / rho) * (alpha / omega);
         for (int64_t k = 0; k < n; ++k) p[k] = r[k] + beta * (p[k] - omega * v[k]);
         prec(p.data(), ph.data());
         bsr_mv(m, b, V, ph.data(), v.data());
         const number r0v = dot(n, r0.data(), v.data());
-        if (r0v == 0.0) return -1;
+        if (r0v == 0.0) return it - 1;
         alpha = rho1 / r0v;
         for (int64_t k = 0; k < n; ++k) s[k] = r[k] - alpha * v[k];
         const number ns = std::sqrt(dot(n, s.data(), s.data()));
@@ -1217,14 +1219,15 @@ static int bicgstab(const Mesh& m, int b, const number* V, const number* Dinv, c
         prec(s.data(), sh.data());
         bsr_mv(m, b, V, sh.data(), t.data());
         const number tt = dot(n, t.data(), t.data());
-        if (tt == 0.0) return -1;
+        if (tt == 0.0) { for (int64_t k = 0; k < n; ++k) x[k] += alpha * ph[k]; return it; }
         omega = dot(n, t.data(), s.data()) / tt;
         for (int64_t k = 0; k < n; ++k) { x[k] += alpha * ph[k] + omega * sh[k]; r[k] = s[k] - omega * t[k]; }
         rho = rho1;
         const number nr = std::sqrt(dot(n, r.data(), r.data()));
         *relres = nr / nr0;
+        if (!std::isfinite(nr)) return -1;
         if (*relres < rtol) return it;
-        if (omega == 0.0) return -1;
+        if (omega == 0.0) return it;
     }
     return maxit;
 }

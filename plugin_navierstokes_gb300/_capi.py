@@ -56,6 +56,10 @@ class NewtonResult(ctypes.Structure):
     ]
 
 
+class BatchOptions(ctypes.Structure):
+    _fields_ = [("cluster_size", c_int), ("max_clusters", c_int)]
+
+
 class NSFV1Error(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"[{STATUS_NAMES.get(status, status)}] {message}")
@@ -94,6 +98,10 @@ _SIGS = {
     "nsfv1_block_jacobi": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "nsfv1_block_jacobi_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "nsfv1_newton_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(NewtonResult), c_void_p]),
+    "nsfv1_set_elem_viscosity": (c_int, [c_void_p, c_void_p]),
+    "nsfv1_set_instances": (c_int, [c_void_p, c_int, c_void_p]),
+    "nsfv1_newton_solve_batched": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(BatchOptions),
+                                           c_void_p, c_void_p]),
     "nsfv1_ref_tables": (c_int, [c_int, POINTER(c_int), POINTER(c_int), c_void_p, POINTER(c_int), c_void_p, c_void_p, c_void_p]),
 }
 

@@ -122,6 +122,8 @@ __global__ void __launch_bounds__(kThreads) k_defect(const DiscParams P, const A
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= A.count) return;
     const int32_t e = __ldg(A.elems + t);
+    if (A.elemInst && !__ldg(A.instActive + __ldg(A.elemInst + e))) return;
+    const double nuEl = A.nuElem ? __ldg(A.nuElem + e) : P.nu;
     GlobalDefSink<nsh, b> sink;
     sink.D = A.D;
 #pragma unroll
@@ -150,9 +152,9 @@ __global__ void __launch_bounds__(kThreads) k_defect(const DiscParams P, const A
             GlobalDefSink<nsh, b>& s; double dt;
             __device__ __forceinline__ void add(int i, int f, double v) { s.add(i, f, v * dt); }
         } ss{sink, P.dt};
-        ok = elem_def_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(uo), ss);
+        ok = elem_def_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(uo), ss, nuEl);
     } else {
-        ok = elem_def_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(u), sink);
+        ok = elem_def_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(u), sink, nuEl);
     }
     if (!ok) atomicOr(A.err, 1);
     // mass (implicit Euler) and source parts, per SCV
@@ -177,6 +179,8 @@ __global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= A.count) return;
     const int32_t e = __ldg(A.elems + t);
+    if (A.elemInst && !__ldg(A.instActive + __ldg(A.elemInst + e))) return;
+    const T nuEl = (T)(A.nuElem ? __ldg(A.nuElem + e) : P.nu);
     int32_t nodes[nsh];
 #pragma unroll
     for (int k = 0; k < nsh; ++k) nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
@@ -187,7 +191,7 @@ __global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const
     load_u<ROID, T>(A.U, nodes, u);
     GlobalJacSink<VT, nsh> sink{reinterpret_cast<VT*>(A.vals), A.elemBlk + (int64_t)e * nsh * nsh};
     const T scale = P.transient ? (T)P.dt : T(1);
-    if (!elem_jac_A<ROID, T>(P, E, u, scale, sink)) atomicOr(A.err, 1);
+    if (!elem_jac_A<ROID, T>(P, E, u, scale, sink, nuEl)) atomicOr(A.err, 1);
     if (P.transient) {
         // mass part: J(d, sh, d, sh) += |SCV| rho
 #pragma unroll
@@ -230,7 +234,7 @@ __global__ void __launch_bounds__(kThreads) k_elem_batch(const DiscParams P, con
 #pragma unroll
             for (int k = 0; k < nsh; ++k) dA[f][k] = 0.0;
         LocalDefSink<nsh, b> ls{dA};
-        if (!elem_def_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(uo), ls)) atomicOr(A.err, 1);
+        if (!elem_def_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(uo), ls, P.nu)) atomicOr(A.err, 1);
 #pragma unroll
         for (int f = 0; f < b; ++f)
 #pragma unroll
@@ -240,7 +244,7 @@ __global__ void __launch_bounds__(kThreads) k_elem_batch(const DiscParams P, con
         double* J = A.jacA + e * n * n;
         for (int q = 0; q < n * n; ++q) J[q] = 0.0;
         LocalJacSink<nsh> sink{J};
-        if (!elem_jac_A<ROID, double>(Q, E, u, 1.0, sink)) atomicOr(A.err, 1);
+        if (!elem_jac_A<ROID, double>(Q, E, u, 1.0, sink, P.nu)) atomicOr(A.err, 1);
     }
     if (A.defM) {
         for (int q = 0; q < n; ++q) A.defM[e * n + q] = 0.0;

@@ -1,0 +1,636 @@
+// Many independent instances (e.g. lid-driven cavities of uneven size) solved
+// together: the instances are disjoint node ranges of one mesh, assembled by
+// the colour kernels in one pass (per-element viscosity, converged instances
+// skipped), and every Newton step runs ONE persistent launch of a
+// cluster-per-instance restarted GMRES (right point-block-Jacobi
+// preconditioning): each thread-block cluster takes instances from a queue
+// (largest first), keeps the Hessenberg state in the shared memory of every
+// CTA of the cluster (computed redundantly, so no broadcast is needed), and
+// reduces dot products over the cluster through distributed shared memory in a
+// fixed order. Cluster barriers are hardware barriers; the kernel has no
+// spin-wait. Results do not depend on which cluster runs an instance.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+#include <cooperative_groups.h>
+#include "nsfv1_internal.h"
+#include "nsfv1_host.h"
+#include "nsfv1_linalg.cuh"
+#include "../../include/nsfv1_gb300.h"
+
+namespace cg = cooperative_groups;
+
+namespace nsfv1 {
+
+static constexpr int kGT = 256;      // threads per CTA of the GMRES kernel
+static constexpr int kMaxM = 32;     // largest restart length
+static constexpr int kWarps = kGT / 32;
+
+template <typename VT>
+struct GmresBatchArgs {
+    const int32_t* queue;      // instance ids, largest first
+    int nQueue;
+    int* head;                 // queue position (zeroed before the launch)
+    const int32_t* instNode0;  // [nInst + 1] node ranges
+    const int32_t* rowPtr;
+    const int32_t* colIdx;
+    const VT* vals;
+    const VT* Dinv;            // inverted diagonal blocks
+    const double* rhs;         // FP64 right-hand side (the defect)
+    VT* x;                     // solution
+    VT* V;                     // basis [m + 1][nTot]
+    VT* t;                     // preconditioned vector [nTot]
+    int64_t nTot;
+    int m;
+    double rtol;
+    int maxit;
+    int* itersOut;
+    double* relresOut;
+};
+
+// warp-level part of a reduction: the warp sum of v goes to wred[warp][k]
+struct ClusterRed {
+    __device__ __forceinline__ static void block_part(double v, int k, double (*wred)[kMaxM + 2]) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if ((threadIdx.x & 31) == 0) wred[threadIdx.x >> 5][k] = v;
+    }
+};
+
+template <typename VT, int b, int G>
+__global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int crank = (int)cl.block_rank();
+    const int csize = (int)cl.num_blocks();
+    __shared__ double wred[kWarps][kMaxM + 2];
+    __shared__ double red[kMaxM + 2];
+    __shared__ double sum[kMaxM + 2];
+    __shared__ double H[(kMaxM + 1) * kMaxM];
+    __shared__ double hcol[kMaxM + 2];
+    __shared__ double cs[kMaxM], sn[kMaxM], gvec[kMaxM + 1], yv[kMaxM];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    const int ctid = crank * kGT + tid;
+    const int cth = csize * kGT;
+    const int m = A.m;
+
+    // sum over the cluster of K values that each thread deposited in wred[warp][k]
+    auto cluster_sum = [&](int K) {
+        __syncthreads();
+        if (tid < K) {
+            double s = 0.0;
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) s += wred[w][tid];
+            red[tid] = s;
+        }
+        cl.sync();
+        if (tid < K) {
+            double s = 0.0;
+            for (int r = 0; r < csize; ++r) s += cl.map_shared_rank(red, r)[tid];
+            sum[tid] = s;
+        }
+        cl.sync();   // red may be reused afterwards; sum is visible to this CTA
+    };
+
+    for (;;) {
+        if (crank == 0 && tid == 0) s_item = atomicAdd(A.head, 1);
+        cl.sync();
+        const int item = *cl.map_shared_rank(&s_item, 0);
+        cl.sync();
+        if (item >= A.nQueue) break;
+        const int inst = A.queue[item];
+        const int64_t node0 = A.instNode0[inst], nNode = A.instNode0[inst + 1] - node0;
+        const int64_t o = node0 * b, n = nNode * b;
+        VT* __restrict__ x = A.x + o;
+        const double* __restrict__ rhs = A.rhs + o;
+        auto Vk = [&](int k) { return A.V + (int64_t)k * A.nTot + o; };
+        VT* __restrict__ t = A.t + o;
+        const VT* __restrict__ Dinv = A.Dinv + node0 * b * b;
+        const int64_t nGroups = cth / G;
+        const int64_t spmvTrips = (nNode + nGroups - 1) / nGroups;
+
+        // y = M t  (rows of this instance; G lanes per block row, uniform trip count)
+        auto spmv = [&](const VT* __restrict__ xin, VT* __restrict__ yout) {
+            const int lane = ctid % G;
+            for (int64_t it = 0; it < spmvTrips; ++it) {
+                const int64_t lr = ctid / G + it * nGroups;
+                const bool valid = lr < nNode;
+                const int64_t row = node0 + lr;
+                const int64_t q0 = valid ? A.rowPtr[row] : 0, q1 = valid ? A.rowPtr[row + 1] : 0;
+                VT acc[b];
+#pragma unroll
+                for (int i = 0; i < b; ++i) acc[i] = VT(0);
+                for (int64_t idx = q0 * b * b + lane; idx < q1 * b * b; idx += G) {
+                    const int64_t q = idx / (b * b);
+                    const int w = (int)(idx - q * (b * b));
+                    const int i = w / b, j = w - (w / b) * b;
+                    const VT v = A.vals[idx] * xin[(int64_t)A.colIdx[q] * b + j - o];
+#pragma unroll
+                    for (int r = 0; r < b; ++r)
+                        if (r == i) acc[r] += v;
+                }
+#pragma unroll
+                for (int off = G / 2; off > 0; off >>= 1)
+#pragma unroll
+                    for (int r = 0; r < b; ++r) acc[r] += __shfl_down_sync(0xffffffffu, acc[r], off, G);
+                if (valid && lane == 0) {
+#pragma unroll
+                    for (int r = 0; r < b; ++r) yout[lr * b + r] = acc[r];
+                }
+            }
+        };
+        // out = Dinv in (per node)
+        auto precond = [&](const VT* __restrict__ in, VT* __restrict__ out) {
+            for (int64_t nd = ctid; nd < nNode; nd += cth) {
+                VT xi[b];
+#pragma unroll
+                for (int j = 0; j < b; ++j) xi[j] = in[nd * b + j];
+#pragma unroll
+                for (int i = 0; i < b; ++i) {
+                    VT a = VT(0);
+#pragma unroll
+                    for (int j = 0; j < b; ++j) a += Dinv[nd * b * b + i * b + j] * xi[j];
+                    out[nd * b + i] = a;
+                }
+            }
+        };
+        // ||v||^2 over the cluster
+        auto norm2 = [&](const VT* __restrict__ v) {
+            VT acc = VT(0);
+            for (int64_t e = ctid; e < n; e += cth) acc += v[e] * v[e];
+            ClusterRed::block_part((double)acc, 0, wred);
+            cluster_sum(1);
+            return sum[0];
+        };
+
+        // r0 = rhs (x0 = 0)
+        VT* v0 = Vk(0);
+        for (int64_t e = ctid; e < n; e += cth) { v0[e] = (VT)rhs[e]; x[e] = VT(0); }
+        cl.sync();
+        double beta = sqrt(norm2(v0));
+        const double beta0 = beta;
+        double relres = 0.0;
+        int total = 0;
+        if (beta0 > 0.0 && isfinite(beta0)) {
+            relres = 1.0;
+            for (;;) {
+                const VT ib = (VT)(1.0 / beta);
+                for (int64_t e = ctid; e < n; e += cth) v0[e] *= ib;
+                if (tid == 0) { gvec[0] = beta; for (int k = 1; k <= m; ++k) gvec[k] = 0.0; }
+                cl.sync();
+                int j = 0;
+                bool done = false;
+                for (; j < m && total < A.maxit; ++j) {
+                    ++total;
+                    precond(Vk(j), t);
+                    cl.sync();
+                    VT* w = Vk(j + 1);
+                    spmv(t, w);
+                    cl.sync();
+                    if (tid <= j) hcol[tid] = 0.0;
+                    // classical Gram-Schmidt, two passes
+                    for (int pass = 0; pass < 2; ++pass) {
+                        for (int k = 0; k <= j; ++k) {
+                            const VT* vk = Vk(k);
+                            VT acc = VT(0);
+                            for (int64_t e = ctid; e < n; e += cth) acc += vk[e] * w[e];
+                            ClusterRed::block_part((double)acc, k, wred);
+                        }
+                        cluster_sum(j + 1);
+                        if (tid <= j) hcol[tid] += sum[tid];
+                        for (int64_t e = ctid; e < n; e += cth) {
+                            VT a = w[e];
+                            for (int k = 0; k <= j; ++k) a -= (VT)sum[k] * Vk(k)[e];
+                            w[e] = a;
+                        }
+                        cl.sync();
+                    }
+                    const double hn = sqrt(norm2(w));
+                    if (hn > 0.0) {
+                        const VT ih = (VT)(1.0 / hn);
+                        for (int64_t e = ctid; e < n; e += cth) w[e] *= ih;
+                    }
+                    // Givens rotations (redundantly in every CTA; thread 0)
+                    if (tid == 0) {
+                        hcol[j + 1] = hn;
+                        for (int k = 0; k < j; ++k) {
+                            const double a = hcol[k], c = hcol[k + 1];
+                            hcol[k] = cs[k] * a + sn[k] * c;
+                            hcol[k + 1] = -sn[k] * a + cs[k] * c;
+                        }
+                        const double a = hcol[j], c = hcol[j + 1];
+                        const double rr = sqrt(a * a + c * c);
+                        cs[j] = rr > 0.0 ? a / rr : 1.0;
+                        sn[j] = rr > 0.0 ? c / rr : 0.0;
+                        hcol[j] = rr;
+                        gvec[j + 1] = -sn[j] * gvec[j];
+                        gvec[j] = cs[j] * gvec[j];
+                        for (int k = 0; k <= j; ++k) H[k * kMaxM + j] = hcol[k];
+                        red[kMaxM + 1] = fabs(gvec[j + 1]) / beta0;   // scratch slot for the estimate
+                    }
+                    cl.sync();
+                    relres = red[kMaxM + 1];
+                    if (!(relres >= A.rtol) || hn == 0.0) { ++j; done = true; break; }   // converged (or NaN: stop)
+                }
+                // y = H^-1 g ; x += Dinv (V y)
+                if (tid == 0) {
+                    for (int k = j - 1; k >= 0; --k) {
+                        double acc = gvec[k];
+                        for (int q = k + 1; q < j; ++q) acc -= H[k * kMaxM + q] * yv[q];
+                        yv[k] = (H[k * kMaxM + k] != 0.0) ? acc / H[k * kMaxM + k] : 0.0;
+                    }
+                }
+                __syncthreads();
+                for (int64_t e = ctid; e < n; e += cth) {
+                    VT a = VT(0);
+                    for (int k = 0; k < j; ++k) a += (VT)yv[k] * Vk(k)[e];
+                    t[e] = a;
+                }
+                cl.sync();
+                for (int64_t nd = ctid; nd < nNode; nd += cth) {
+#pragma unroll
+                    for (int i = 0; i < b; ++i) {
+                        VT a = x[nd * b + i];
+#pragma unroll
+                        for (int jj = 0; jj < b; ++jj) a += Dinv[nd * b * b + i * b + jj] * t[nd * b + jj];
+                        x[nd * b + i] = a;
+                    }
+                }
+                cl.sync();
+                if (done || total >= A.maxit || !isfinite(relres)) break;
+                // restart: V_0 = rhs - M x
+                spmv(x, v0);
+                cl.sync();
+                for (int64_t e = ctid; e < n; e += cth) v0[e] = (VT)(rhs[e] - (double)v0[e]);
+                cl.sync();
+                beta = sqrt(norm2(v0));
+                relres = beta / beta0;
+                if (!(relres >= A.rtol) || beta == 0.0) break;
+            }
+        }
+        if (crank == 0 && tid == 0) { A.itersOut[inst] = total; A.relresOut[inst] = relres; }
+        cl.sync();
+    }
+}
+
+// ---- small batch kernels ----------------------------------------------------------
+
+// per-instance ||v||^2 over its node range (one CTA per instance, fixed order)
+__global__ void __launch_bounds__(256) k_inst_norm2(const int32_t* __restrict__ instNode0, int b, const double* __restrict__ v,
+                                                    double* __restrict__ out) {
+    __shared__ double sh[256];
+    const int inst = blockIdx.x;
+    const int64_t e0 = (int64_t)instNode0[inst] * b, e1 = (int64_t)instNode0[inst + 1] * b;
+    double acc = 0.0;
+    for (int64_t e = e0 + threadIdx.x; e < e1; e += 256) acc += v[e] * v[e];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[inst] = sh[0];
+}
+
+// point-block Jacobi setup for the nodes of active instances
+template <typename VT, int b>
+__global__ void k_block_inv_active(int64_t nRows, const int32_t* __restrict__ diagPos, const int32_t* __restrict__ nodeInst,
+                                   const int32_t* __restrict__ active, const VT* __restrict__ vals, VT* __restrict__ Dinv, int* err) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nRows || !active[nodeInst[r]]) return;
+    if (!block_inverse<b>(vals + (int64_t)diagPos[r] * b * b, Dinv + r * b * b)) atomicOr(err, 2);
+}
+
+// trial iterate: ut = u - lambda[inst] du on the nodes of pending instances
+template <typename VT>
+__global__ void k_batch_trial(int64_t n, int b, const int32_t* __restrict__ nodeInst, const int32_t* __restrict__ pending,
+                              const double* __restrict__ lambda, const double* __restrict__ u, const VT* __restrict__ du,
+                              double* __restrict__ ut) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const int inst = nodeInst[e / b];
+    if (pending[inst]) ut[e] = u[e] - lambda[inst] * (double)du[e];
+}
+
+// copy the rows of flagged instances: dst[e] = src[e]
+__global__ void k_batch_copy(int64_t n, int b, const int32_t* __restrict__ nodeInst, const int32_t* __restrict__ flag,
+                             const double* __restrict__ src, double* __restrict__ dst) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n && flag[nodeInst[e / b]]) dst[e] = src[e];
+}
+
+template <typename VT, int b>
+static cudaError_t launch_gmres_batch(const GmresBatchArgs<VT>& a, int clusterSize, int nClusters, cudaStream_t s) {
+    constexpr int G = (b == 4) ? 16 : 8;
+    auto kern = k_gmres_batch<VT, b, G>;
+    if (clusterSize > 8) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(clusterSize * nClusters, 1, 1);
+    cfg.blockDim = dim3(kGT, 1, 1);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = clusterSize;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, a);
+}
+
+// most clusters of this size that can be resident at once
+template <typename VT, int b>
+static int max_clusters(int clusterSize) {
+    constexpr int G = (b == 4) ? 16 : 8;
+    auto kern = k_gmres_batch<VT, b, G>;
+    if (clusterSize > 8) cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(clusterSize, 1, 1);
+    cfg.blockDim = dim3(kGT, 1, 1);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = clusterSize;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+// ---- the batched Newton driver -----------------------------------------------------
+
+struct BatchWs {
+    int prec = -1, m = 0;
+    int64_t n = 0;
+    double *D = nullptr, *Dt = nullptr, *Ut = nullptr, *nrm = nullptr, *lambda = nullptr, *relres = nullptr;
+    void *J = nullptr, *Dinv = nullptr, *V = nullptr, *t = nullptr, *x = nullptr;
+    int32_t *queue = nullptr, *head = nullptr, *pending = nullptr, *accepted = nullptr, *iters = nullptr;
+    ~BatchWs() { release(); }
+    void release() {
+        auto f = [](auto*& p) { if (p) cudaFree((void*)p); p = nullptr; };
+        f(D); f(Dt); f(Ut); f(nrm); f(lambda); f(relres); f(J); f(Dinv); f(V); f(t); f(x);
+        f(queue); f(head); f(pending); f(accepted); f(iters);
+        prec = -1;
+    }
+};
+
+}  // namespace nsfv1
+
+using namespace nsfv1;
+
+namespace {
+struct BatchState;
+}
+
+namespace nsfv1 {
+void batch_free(void* p);
+}
+
+namespace {
+
+struct BatchState {
+    BatchWs ws;
+};
+
+BatchState* batch_state(Disc& D) {
+    if (!D.batch) D.batch = new BatchState();
+    return static_cast<BatchState*>(D.batch);
+}
+
+template <typename VT>
+int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsfv1_newton_params& p, const nsfv1_batch_options& opt,
+                   nsfv1_newton_result* res, cudaStream_t s) {
+    const int b = D.dim + 1;
+    const int nInst = D.nInst;
+    const int64_t n = D.nNodes * b;
+    const int prec = std::is_same<VT, double>::value ? NSFV1_F64 : NSFV1_F32;
+    const int m = std::min(std::max(p.gmres_restart, 2), kMaxM);
+    BatchWs& W = batch_state(D)->ws;
+    if (W.prec != prec || W.n != n || W.m != m) {
+        W.release();
+        const size_t vt = sizeof(VT);
+        auto al = [&](auto*& ptr, size_t bytes) { return D.cuda_ok(cudaMalloc((void**)&ptr, bytes), "batch workspace"); };
+        if (!al(W.D, n * 8) || !al(W.Dt, n * 8) || !al(W.Ut, n * 8) || !al(W.nrm, nInst * 8) || !al(W.lambda, nInst * 8) ||
+            !al(W.relres, nInst * 8) || !al(W.J, D.colIdx.size() * b * b * vt) || !al(W.Dinv, (size_t)D.nNodes * b * b * vt) ||
+            !al(W.V, (size_t)(m + 1) * n * vt) || !al(W.t, n * vt) || !al(W.x, n * vt) || !al(W.queue, nInst * 4) ||
+            !al(W.head, 4) || !al(W.pending, nInst * 4) || !al(W.accepted, nInst * 4) || !al(W.iters, nInst * 4))
+            return D.status;
+        W.prec = prec; W.n = n; W.m = m;
+    }
+    const int clusterSize = opt.cluster_size > 0 ? opt.cluster_size : 4;
+    int nClusters = (b == 4) ? max_clusters<VT, 4>(clusterSize) : max_clusters<VT, 3>(clusterSize);
+    if (nClusters <= 0) { D.fail(NSFV1_ERR_ARGUMENT, "batched solve: cluster size not launchable"); return D.status; }
+    if (opt.max_clusters > 0) nClusters = std::min(nClusters, opt.max_clusters);
+
+    std::vector<int32_t> active(nInst, 1), pend(nInst, 0), acc(nInst, 0), iters(nInst, 0);
+    std::vector<double> nd0(nInst, 0.0), nd(nInst, 0.0), ndt(nInst, 0.0), lam(nInst, 1.0), rr(nInst, 0.0);
+    std::vector<int64_t> size(nInst);
+    for (int i = 0; i < nInst; ++i) size[i] = D.instNode0[i + 1] - D.instNode0[i];
+    for (int i = 0; i < nInst; ++i) { res[i] = nsfv1_newton_result{}; res[i].status = NSFV1_ERR_NOT_CONVERGED; }
+
+    auto upload_flags = [&](const std::vector<int32_t>& f, int32_t* dst) {
+        return D.cuda_ok(cudaMemcpyAsync(dst, f.data(), nInst * 4, cudaMemcpyHostToDevice, s), "flags");
+    };
+    auto norms = [&](const double* v, std::vector<double>& out) {
+        k_inst_norm2<<<nInst, 256, 0, s>>>(D.d_instNode0, b, v, W.nrm);
+        if (!D.cuda_ok(cudaMemcpyAsync(out.data(), W.nrm, nInst * 8, cudaMemcpyDeviceToHost, s), "norms")) return false;
+        if (!D.cuda_ok(cudaStreamSynchronize(s), "norms")) return false;
+        for (auto& x : out) x = std::sqrt(x);
+        return true;
+    };
+
+    const int g = (int)((n + 255) / 256);
+    D.instSkip = false;
+    if (!upload_flags(active, D.d_instActive)) return D.status;
+    if (!D.set_dirichlet_values(u, s)) return D.status;
+    if (!D.assemble_defect(u, u_old, dt, W.D, s)) return D.status;
+    if (!norms(W.D, nd0)) return D.status;
+    nd = nd0;
+    for (int i = 0; i < nInst; ++i) {
+        res[i].initial_defect = nd0[i];
+        res[i].final_defect = nd0[i];
+        if (!std::isfinite(nd0[i])) { active[i] = 0; res[i].status = NSFV1_ERR_NONFINITE; }
+        else if (nd0[i] == 0.0) { active[i] = 0; res[i].status = NSFV1_OK; }
+    }
+    for (int it = 0; it < p.max_iter; ++it) {
+        int nAct = 0;
+        for (int i = 0; i < nInst; ++i) {
+            if (!active[i]) continue;
+            if (nd[i] <= p.rtol * nd0[i] || nd[i] <= p.atol) { active[i] = 0; res[i].status = NSFV1_OK; continue; }
+            ++nAct;
+        }
+        if (nAct == 0) break;
+        D.instSkip = true;
+        if (!upload_flags(active, D.d_instActive)) return D.status;
+        if (!D.assemble_jacobian(u, u_old, dt, W.J, prec, s, false)) return D.status;
+        cudaMemsetAsync(D.d_err, 0, sizeof(int), s);
+        if (b == 4) k_block_inv_active<VT, 4><<<(int)((D.nNodes + 127) / 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, D.d_nodeInst, D.d_instActive, (VT*)W.J, (VT*)W.Dinv, D.d_err);
+        else k_block_inv_active<VT, 3><<<(int)((D.nNodes + 127) / 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, D.d_nodeInst, D.d_instActive, (VT*)W.J, (VT*)W.Dinv, D.d_err);
+        // queue: active instances, largest first
+        std::vector<int32_t> q;
+        for (int i = 0; i < nInst; ++i) if (active[i]) q.push_back(i);
+        std::stable_sort(q.begin(), q.end(), [&](int a, int c) { return size[a] > size[c]; });
+        if (!D.cuda_ok(cudaMemcpyAsync(W.queue, q.data(), q.size() * 4, cudaMemcpyHostToDevice, s), "queue")) return D.status;
+        cudaMemsetAsync(W.head, 0, 4, s);
+        GmresBatchArgs<VT> a{W.queue, (int)q.size(), W.head, D.d_instNode0, D.d_rowPtr, D.d_colIdx, (const VT*)W.J, (const VT*)W.Dinv,
+                             W.D, (VT*)W.x, (VT*)W.V, (VT*)W.t, n, m, p.lin_rtol, p.lin_max_iter, W.iters, W.relres};
+        cudaError_t le = (b == 4) ? launch_gmres_batch<VT, 4>(a, clusterSize, std::min(nClusters, (int)q.size()), s)
+                                  : launch_gmres_batch<VT, 3>(a, clusterSize, std::min(nClusters, (int)q.size()), s);
+        if (!D.cuda_ok(le, "batched GMRES launch")) return D.status;
+        int herr = 0;
+        cudaMemcpyAsync(&herr, D.d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(iters.data(), W.iters, nInst * 4, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(rr.data(), W.relres, nInst * 8, cudaMemcpyDeviceToHost, s);
+        if (!D.cuda_ok(cudaStreamSynchronize(s), "batched GMRES")) return D.status;
+        if (herr & 1) { D.fail(NSFV1_ERR_GEOMETRY, "upwind: cannot find cut side"); cudaMemsetAsync(D.d_err, 0, sizeof(int), s); return D.status; }
+        for (int i : q) {
+            res[i].iterations = it + 1;
+            res[i].linear_iterations += iters[i];
+            if (!std::isfinite(rr[i])) { active[i] = 0; res[i].status = NSFV1_ERR_NONFINITE; }
+        }
+        if (herr & 2) {
+            // a singular diagonal block: report it on every active instance
+            for (int i : q) if (active[i]) { active[i] = 0; res[i].status = NSFV1_ERR_BREAKDOWN; }
+            cudaMemsetAsync(D.d_err, 0, sizeof(int), s);
+            break;
+        }
+        // per-instance backtracking line search on ||d||_2
+        for (int i = 0; i < nInst; ++i) { pend[i] = active[i]; lam[i] = 1.0; acc[i] = 0; }
+        cudaMemcpyAsync(W.Ut, u, n * 8, cudaMemcpyDeviceToDevice, s);
+        for (int k = 0; k <= p.line_search_steps; ++k) {
+            if (!D.cuda_ok(cudaMemcpyAsync(W.lambda, lam.data(), nInst * 8, cudaMemcpyHostToDevice, s), "lambda") ||
+                !upload_flags(pend, W.pending))
+                return D.status;
+            k_batch_trial<VT><<<g, 256, 0, s>>>(n, b, D.d_nodeInst, W.pending, W.lambda, u, (const VT*)W.x, W.Ut);
+            if (!upload_flags(pend, D.d_instActive)) return D.status;
+            if (!D.assemble_defect(W.Ut, u_old, dt, W.Dt, s)) return D.status;
+            if (!norms(W.Dt, ndt)) return D.status;
+            bool any = false;
+            std::fill(acc.begin(), acc.end(), 0);
+            for (int i = 0; i < nInst; ++i) {
+                if (!pend[i]) continue;
+                if (ndt[i] <= (1.0 - 1e-4 * lam[i]) * nd[i] || k == p.line_search_steps || !std::isfinite(ndt[i])) {
+                    acc[i] = 1; pend[i] = 0; nd[i] = ndt[i];
+                } else {
+                    lam[i] *= 0.5; any = true;
+                }
+            }
+            if (!upload_flags(acc, W.accepted)) return D.status;
+            k_batch_copy<<<g, 256, 0, s>>>(n, b, D.d_nodeInst, W.accepted, W.Dt, W.D);
+            if (!any) break;
+        }
+        // u <- Ut on the active instances
+        if (!upload_flags(active, W.accepted)) return D.status;
+        k_batch_copy<<<g, 256, 0, s>>>(n, b, D.d_nodeInst, W.accepted, W.Ut, u);
+        for (int i = 0; i < nInst; ++i) {
+            if (!active[i]) continue;
+            res[i].final_defect = nd[i];
+            if (!std::isfinite(nd[i])) { active[i] = 0; res[i].status = NSFV1_ERR_NONFINITE; }
+        }
+    }
+    for (int i = 0; i < nInst; ++i) {
+        res[i].final_defect = nd[i];
+        if (active[i] && (nd[i] <= p.rtol * nd0[i] || nd[i] <= p.atol)) res[i].status = NSFV1_OK;
+    }
+    D.instSkip = false;
+    std::vector<int32_t> all(nInst, 1);
+    upload_flags(all, D.d_instActive);
+    if (!D.cuda_ok(cudaStreamSynchronize(s), "batched newton")) return D.status;
+    int worst = NSFV1_OK;
+    for (int i = 0; i < nInst; ++i) if (res[i].status != NSFV1_OK) worst = res[i].status;
+    if (worst != NSFV1_OK) D.fail(worst, "batched Newton: some instances did not converge (see the per-instance results)");
+    return worst;
+}
+
+}  // namespace
+
+namespace nsfv1 {
+void batch_free(void* p) { delete static_cast<BatchState*>(p); }
+}  // namespace nsfv1
+
+extern "C" {
+
+int nsfv1_set_elem_viscosity(nsfv1_disc* h, const double* nu) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "set_elem_viscosity: no mesh"); return D->status; }
+    if (D->d_nuElem) { cudaFree(D->d_nuElem); D->d_nuElem = nullptr; }
+    if (!nu) return NSFV1_OK;
+    for (int64_t e = 0; e < D->nElems; ++e)
+        if (!(nu[e] > 0.0) || !std::isfinite(nu[e])) { D->fail(NSFV1_ERR_ARGUMENT, "set_elem_viscosity: viscosity must be positive"); return D->status; }
+    if (!D->cuda_ok(cudaMalloc((void**)&D->d_nuElem, sizeof(double) * D->nElems), "alloc viscosity") ||
+        !D->cuda_ok(cudaMemcpy(D->d_nuElem, nu, sizeof(double) * D->nElems, cudaMemcpyHostToDevice), "upload viscosity"))
+        return D->status;
+    D->viscoSet = true;
+    return NSFV1_OK;
+}
+
+int nsfv1_set_instances(nsfv1_disc* h, int n_inst, const int32_t* node_offsets) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "set_instances: no mesh"); return D->status; }
+    if (n_inst <= 0 || !node_offsets || node_offsets[0] != 0 || node_offsets[n_inst] != D->nNodes) {
+        D->fail(NSFV1_ERR_ARGUMENT, "set_instances: offsets must start at 0 and end at the node count");
+        return D->status;
+    }
+    std::vector<int32_t> nodeInst(D->nNodes), elemInst(D->nElems);
+    for (int i = 0; i < n_inst; ++i) {
+        if (node_offsets[i + 1] <= node_offsets[i]) { D->fail(NSFV1_ERR_ARGUMENT, "set_instances: empty or decreasing range"); return D->status; }
+        for (int32_t v = node_offsets[i]; v < node_offsets[i + 1]; ++v) nodeInst[v] = i;
+    }
+    const int nsh = D->nsh;
+    std::vector<int32_t> conn;   // host copy of the connectivity is needed for the check
+    conn.resize((size_t)D->nElems * nsh);
+    if (!D->cuda_ok(cudaMemcpy(conn.data(), D->d_conn, conn.size() * 4, cudaMemcpyDeviceToHost), "read conn")) return D->status;
+    for (int64_t e = 0; e < D->nElems; ++e) {
+        const int i = nodeInst[conn[e * nsh]];
+        for (int k = 1; k < nsh; ++k)
+            if (nodeInst[conn[e * nsh + k]] != i) { D->fail(NSFV1_ERR_ARGUMENT, "set_instances: an element spans two instances"); return D->status; }
+        elemInst[e] = i;
+    }
+    auto up = [&](int32_t*& dst, const int32_t* src, size_t cnt) {
+        if (dst) cudaFree(dst);
+        dst = nullptr;
+        return D->cuda_ok(cudaMalloc((void**)&dst, cnt * 4), "alloc instances") &&
+               D->cuda_ok(cudaMemcpy(dst, src, cnt * 4, cudaMemcpyHostToDevice), "upload instances");
+    };
+    std::vector<int32_t> ones(n_inst, 1);
+    if (!up(D->d_instNode0, node_offsets, n_inst + 1) || !up(D->d_nodeInst, nodeInst.data(), nodeInst.size()) ||
+        !up(D->d_elemInst, elemInst.data(), elemInst.size()) || !up(D->d_instActive, ones.data(), n_inst))
+        return D->status;
+    D->nInst = n_inst;
+    D->instNode0.assign(node_offsets, node_offsets + n_inst + 1);
+    D->instSkip = false;
+    return NSFV1_OK;
+}
+
+int nsfv1_newton_solve_batched(nsfv1_disc* h, double* u, const double* u_old, double dt, const nsfv1_newton_params* p,
+                               const nsfv1_batch_options* opt, nsfv1_newton_result* results, void* stream) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (!D->hasMesh || D->nInst <= 0) { D->fail(NSFV1_ERR_STATE, "newton_solve_batched: no mesh or no instances"); return D->status; }
+    if (!u || !p || !results) { D->fail(NSFV1_ERR_ARGUMENT, "newton_solve_batched: null argument"); return D->status; }
+    nsfv1_batch_options o{};
+    if (opt) o = *opt;
+    if (o.cluster_size < 0 || o.cluster_size > 16) { D->fail(NSFV1_ERR_ARGUMENT, "newton_solve_batched: cluster size must be 1..16"); return D->status; }
+    if (p->jacobian_prec == NSFV1_F64) return batched_newton<double>(*D, u, u_old, dt, *p, o, results, (cudaStream_t)stream);
+    if (p->jacobian_prec == NSFV1_F32) return batched_newton<float>(*D, u, u_old, dt, *p, o, results, (cudaStream_t)stream);
+    D->fail(NSFV1_ERR_ARGUMENT, "newton_solve_batched: bad precision");
+    return D->status;
+}
+
+}  // extern "C"

@@ -76,12 +76,15 @@ template <class T> static cudaError_t dupload(T*& dst, const T* src, size_t n) {
 
 void Disc::free_mesh() {
     dfree(d_coords); dfree(d_conn); dfree(d_elemBlk); dfree(d_colorElems); dfree(d_rowPtr); dfree(d_colIdx);
-    dfree(d_dirRow); dfree(d_dirVal); dfree(d_diagPos); dfree(d_bjDinv);
+    dfree(d_dirRow); dfree(d_dirVal); dfree(d_diagPos); dfree(d_bjDinv); dfree(d_nuElem);
+    dfree(d_instNode0); dfree(d_elemInst); dfree(d_nodeInst); dfree(d_instActive);
+    nInst = 0; instNode0.clear(); instSkip = false;
 }
 
 Disc::~Disc() {
     free_mesh();
     free_workspace();
+    if (batch) { batch_free(batch); batch = nullptr; }
     dfree(d_err);
 }
 
@@ -470,7 +473,8 @@ bool Disc::assemble_defect(const double* u, const double* u_old, double dt, doub
     const int b = dim + 1;
     if (!cuda_ok(cudaMemsetAsync(d, 0, sizeof(double) * nNodes * b, s), "memset defect")) return false;
     for (int c = 0; c < nColors; ++c) {
-        AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, d, nullptr};
+        AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, d, nullptr,
+                  d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive};
         if (!cuda_ok(launch_defect(roid, P, a, s), "defect kernel")) return false;
     }
     if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, d, nullptr, 0, s), "dirichlet")) return false;
@@ -487,7 +491,8 @@ bool Disc::assemble_jacobian(const double* u, const double* u_old, double dt, vo
     const size_t bytes = colIdx.size() * b * b * (prec == NSFV1_F64 ? sizeof(double) : sizeof(float));
     if (!cuda_ok(cudaMemsetAsync(vals, 0, bytes, s), "memset jacobian")) return false;
     for (int c = 0; c < nColors; ++c) {
-        AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, nullptr, vals};
+        AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, nullptr, vals,
+                  d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive};
         if (!cuda_ok(launch_jacobian(roid, P, a, prec, s), "jacobian kernel")) return false;
     }
     if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, nullptr, vals, prec, s), "dirichlet")) return false;

@@ -670,7 +670,7 @@ struct IpState {
 template <int ROID, typename T>
 __device__ __forceinline__ void ip_state(const DiscParams& P, const Elem<ROID, T>& E, const IpGeo<T>& G, const int ip,
                                          const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh], const T corMinN, const T corMinD, const T corAvgN,
-                                         IpState<ROID, T>& S) {
+                                         const T nuEl, IpState<ROID, T>& S) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh;
     S.ok = true;
@@ -730,7 +730,7 @@ __device__ __forceinline__ void ip_state(const DiscParams& P, const Elem<ROID, T
     S.nuL = T(0); S.nsvcl = T(0); S.nsvdl = T(0); S.diag = T(1);
     if (P.stab == STAB_WITHOUT) return;
     const T Linv = diff_len_sq_inv<ROID, T>(P.diffLen, E, G, corMinN, corMinD, corAvgN);
-    S.nuL = T(P.nu) * Linv;
+    S.nuL = nuEl * Linv;
     if (!stokes) {
         S.nsvcl = norm / Lup;
         if (P.stab == STAB_FLOW) S.nsvdl = norm / (Ldown + Lup);
@@ -763,19 +763,19 @@ __device__ __forceinline__ T peclet_blend(const IpGeo<T>& G, const T* StdVel, T 
 // ---------------------------------------------------------------------------
 template <int ROID, typename T, class DSink>
 __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
-                                           const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], DSink& sink) {
+                                           const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], DSink& sink, const T nu) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, Pc = dim, nip = R::nip;
     T corMinN = T(0), corMinD = T(0), corAvgN = T(1);
     if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, T>(E, corMinN, corMinD, corAvgN);
-    const T rho = T(P.rho), nu = T(P.nu);
+    const T rho = T(P.rho);
     bool ok = true;
 #pragma unroll 1
     for (int ip = 0; ip < nip; ++ip) {
         IpGeo<T> G;
         ip_geom<ROID, T>(E, ip, G);
         IpState<ROID, T> S;
-        ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, S);
+        ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
         ok &= S.ok;
         // velocity and pressure gradients: local gradients first, then one J^-T
         // (grad_k = J^-T lgrad_k, so sum_k u_k grad_k = J^-T sum_k u_k lgrad_k)
@@ -905,12 +905,12 @@ __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID,
 // ---------------------------------------------------------------------------
 template <int ROID, typename T, class Sink>
 __device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
-                                           const T scale, Sink& sink) {
+                                           const T scale, Sink& sink, const T nu) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, b = R::b, Pc = dim;
     T corMinN = T(0), corMinD = T(0), corAvgN = T(1);
     if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, T>(E, corMinN, corMinD, corAvgN);
-    const T rho = T(P.rho), nu = T(P.nu);
+    const T rho = T(P.rho);
     const T mnr = T(-1.0) * nu * rho;
     bool ok = true;
 #pragma unroll 1
@@ -918,7 +918,7 @@ __device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID,
         IpGeo<T> G;
         ip_geom<ROID, T>(E, ip, G);
         IpState<ROID, T> S;
-        ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, S);
+        ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
         ok &= S.ok;
         T UpwindVel[3] = {T(0), T(0), T(0)};
         T w = T(1), prod = T(0), Vn = T(0);

@@ -43,6 +43,15 @@ struct Disc {
     double* d_coords = nullptr;
     int32_t *d_conn = nullptr, *d_elemBlk = nullptr, *d_colorElems = nullptr, *d_rowPtr = nullptr, *d_colIdx = nullptr;
     int32_t* d_diagPos = nullptr;   // block index of each row's diagonal block
+    double* d_nuElem = nullptr;     // per-element viscosity (nsfv1_set_elem_viscosity), or null
+    // independent instances (nsfv1_set_instances): node ranges, element -> instance
+    int nInst = 0;
+    std::vector<int32_t> instNode0;          // [nInst + 1] first node of each instance
+    int32_t* d_instNode0 = nullptr;
+    int32_t* d_elemInst = nullptr;
+    int32_t* d_nodeInst = nullptr;
+    int32_t* d_instActive = nullptr;         // per-instance active flag (assembly skips inactive ones)
+    bool instSkip = false;                   // assembly honours d_instActive
     double* d_bjDinv = nullptr;     // nsfv1_block_jacobi scratch: inverted diagonal blocks
     int32_t* d_dirRow = nullptr;
     double* d_dirVal = nullptr;
@@ -50,6 +59,7 @@ struct Disc {
     int* d_err = nullptr;
 
     Workspace ws;
+    void* batch = nullptr;   // workspace of the batched solver
 
     int status = 0;
     std::string lastError;
@@ -64,7 +74,10 @@ struct Disc {
     bool assemble_defect(const double* u, const double* u_old, double dt, double* d, cudaStream_t s);
     bool assemble_jacobian(const double* u, const double* u_old, double dt, void* vals, int prec, cudaStream_t s, bool sync = true);
     bool ensure_workspace(int prec, int gmresM);
+    bool set_dirichlet_values(double* u, cudaStream_t s);   // u[dof] = g for every Dirichlet row
 };
+
+void batch_free(void* p);
 
 // point-block Jacobi on a caller's Jacobian with Dinv as scratch (nNodes*b*b
 // doubles): shared by nsfv1_block_jacobi and its variant without allocation

@@ -20,6 +20,9 @@ struct AsmArgs {
     const double* Uold;       // [nNodes][b] or null
     double* D;                // defect [nNodes][b]
     void* vals;               // BSR values (double or float)
+    const double* nuElem;     // per-element kinematic viscosity, or null (the disc's constant)
+    const int32_t* elemInst;  // per-element instance id, or null (no instance skipping)
+    const int32_t* instActive;// per-instance flag: elements of inactive instances are skipped
 };
 
 // Batched element-local callbacks (no global scatter).

@@ -11,6 +11,7 @@
 #include <vector>
 #include "nsfv1_internal.h"
 #include "nsfv1_host.h"
+#include "nsfv1_linalg.cuh"
 #include "../../include/nsfv1_gb300.h"
 
 namespace nsfv1 {
@@ -60,40 +61,7 @@ template <typename VT, typename OT, int b>
 __global__ void k_block_inv(int64_t nRows, const int32_t* __restrict__ diagPos, const VT* __restrict__ vals, OT* __restrict__ Dinv, int* err) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nRows) return;
-    double M[b][2 * b];
-    const VT* A = vals + (int64_t)diagPos[r] * b * b;
-#pragma unroll
-    for (int i = 0; i < b; ++i)
-#pragma unroll
-        for (int j = 0; j < b; ++j) { M[i][j] = (double)A[i * b + j]; M[i][b + j] = (i == j) ? 1.0 : 0.0; }
-    bool ok = true;
-#pragma unroll
-    for (int c = 0; c < b; ++c) {
-        int p = c;
-#pragma unroll
-        for (int q = c + 1; q < b; ++q) if (fabs(M[q][c]) > fabs(M[p][c])) p = q;
-        if (M[p][c] == 0.0) { ok = false; break; }
-        if (p != c) {
-#pragma unroll
-            for (int j = 0; j < 2 * b; ++j) { const double t = M[p][j]; M[p][j] = M[c][j]; M[c][j] = t; }
-        }
-        const double piv = 1.0 / M[c][c];
-#pragma unroll
-        for (int j = 0; j < 2 * b; ++j) M[c][j] *= piv;
-#pragma unroll
-        for (int q = 0; q < b; ++q) {
-            if (q == c) continue;
-            const double f = M[q][c];
-#pragma unroll
-            for (int j = 0; j < 2 * b; ++j) M[q][j] -= f * M[c][j];
-        }
-    }
-    if (!ok) { atomicOr(err, 2); return; }
-    OT* O = Dinv + r * b * b;
-#pragma unroll
-    for (int i = 0; i < b; ++i)
-#pragma unroll
-        for (int j = 0; j < b; ++j) O[i * b + j] = (OT)M[i][b + j];
+    if (!block_inverse<b>(vals + (int64_t)diagPos[r] * b * b, Dinv + r * b * b)) atomicOr(err, 2);
 }
 
 template <typename VT, int b>
@@ -624,6 +592,11 @@ static int newton_impl(Disc& D, double* u, const double* u_old, double dt, const
 }  // namespace
 
 namespace nsfv1 {
+bool Disc::set_dirichlet_values(double* u, cudaStream_t s) {
+    if (nDir > 0) k_set_dirichlet<<<grid_for(nDir), 256, 0, s>>>(nDir, d_dirRow, d_dirVal, u);
+    return cuda_ok(cudaGetLastError(), "dirichlet values");
+}
+
 // point-block Jacobi on a caller's Jacobian: Dinv (FP64 scratch) = inverse
 // diagonal blocks, z = Dinv r.
 bool block_jacobi_run(Disc& D, const void* vals, int prec, const double* r, double* z, double* Dinv, cudaStream_t s) {

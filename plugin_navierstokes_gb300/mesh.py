@@ -130,3 +130,36 @@ def solenoidal_state(coords: np.ndarray, seed: int = 1, n_modes: int = 8, kmax: 
     v = G[0][:, 2] - G[2][:, 0]
     w = G[1][:, 0] - G[0][:, 1]
     return np.stack([u, v, w, p], axis=1)
+
+
+CAVITY_SIZES = (32, 48, 64, 96, 128, 192, 256)
+
+
+def draw_cavity_params(n_inst: int, seed: int = 3, sizes=CAVITY_SIZES, re_range=(10.0, 1000.0), lid_range=(0.5, 2.0)):
+    """Seeded draws of the batched-cavity workload: mesh side N uniform over
+    ``sizes``, Re log-uniform in ``re_range``, lid speed uniform in ``lid_range``;
+    the viscosity of the unit cavity is nu = lid / Re."""
+    r = uniform(seed, 3 * n_inst).reshape(n_inst, 3)
+    N = np.array(sizes)[np.minimum((r[:, 0] * len(sizes)).astype(int), len(sizes) - 1)]
+    Re = np.exp(np.log(re_range[0]) + r[:, 1] * (np.log(re_range[1]) - np.log(re_range[0])))
+    lid = lid_range[0] + r[:, 2] * (lid_range[1] - lid_range[0])
+    return N, Re, lid
+
+
+def cavity_batch(sizes, Re, lid):
+    """Independent lid-driven cavities (unit squares, quadrilaterals) as one mesh:
+    returns dict(elem_type, coords, conn, node_offsets, nu_elem, dofs, values)."""
+    coords, conns, offs, nus, dofs, vals = [], [], [0], [], [], []
+    for N, re, u0 in zip(sizes, Re, lid):
+        _, X, C = structured_quads(int(N))
+        d, v = cavity_dirichlet(X, float(u0))
+        base = offs[-1]
+        coords.append(X)
+        conns.append(C + base)
+        dofs.append(d + base * 3)
+        vals.append(v)
+        nus.append(np.full(C.shape[0], float(u0) / float(re)))
+        offs.append(base + X.shape[0])
+    return {"elem_type": QUADRILATERAL, "coords": np.concatenate(coords), "conn": np.concatenate(conns).astype(np.int32),
+            "node_offsets": np.array(offs, np.int32), "nu_elem": np.concatenate(nus),
+            "dofs": np.concatenate(dofs).astype(np.int32), "values": np.concatenate(vals)}

@@ -181,6 +181,35 @@ class NavierStokesFV1:
             raise NSFV1Error(st, self._lib.nsfv1_last_error(self._h).decode() + f" {res}")
         return res
 
+    def set_elem_viscosity(self, nu) -> None:
+        """Per-element kinematic viscosity (None: back to the constant)."""
+        if nu is None:
+            self._c(self._lib.nsfv1_set_elem_viscosity(self._h, None))
+            return
+        a = np.ascontiguousarray(nu, dtype=np.float64)
+        self._c(self._lib.nsfv1_set_elem_viscosity(self._h, a.ctypes.data))
+
+    def set_instances(self, node_offsets) -> None:
+        a = np.ascontiguousarray(node_offsets, dtype=np.int32)
+        self._c(self._lib.nsfv1_set_instances(self._h, a.size - 1, a.ctypes.data))
+        self.n_inst = a.size - 1
+
+    def newton_solve_batched(self, u, u_old=None, dt: float = 0.0, rtol: float = 1e-8, atol: float = 0.0, max_iter: int = 100,
+                             lin_rtol: float = 1e-3, lin_max_iter: int = 3000, line_search_steps: int = 6,
+                             jacobian_prec: str = "f64", gmres_restart: int = 30, cluster_size: int = 4, max_clusters: int = 0,
+                             stream=None, raise_on_error: bool = True) -> list[dict]:
+        p = _capi.NewtonParams(rtol, atol, max_iter, lin_rtol, lin_max_iter, line_search_steps,
+                               _capi.F64 if jacobian_prec == "f64" else _capi.F32, _capi.GMRES, gmres_restart)
+        o = _capi.BatchOptions(cluster_size, max_clusters)
+        res = (_capi.NewtonResult * self.n_inst)()
+        st = self._lib.nsfv1_newton_solve_batched(self._h, _ptr(u), _ptr(u_old), float(dt), ctypes.byref(p), ctypes.byref(o),
+                                                  ctypes.addressof(res), _stream_ptr(stream))
+        out = [{"status": r.status, "iterations": r.iterations, "linear_iterations": r.linear_iterations,
+                "initial_defect": r.initial_defect, "final_defect": r.final_defect} for r in res]
+        if st not in (_capi.OK,) and raise_on_error:
+            raise NSFV1Error(st, self._lib.nsfv1_last_error(self._h).decode())
+        return out
+
     def last_error(self) -> str:
         return self._lib.nsfv1_last_error(self._h).decode()
 
