@@ -208,9 +208,21 @@ int nsfv1_set_elem_viscosity(nsfv1_disc* h, const double* nu);
  * n_nodes); no element may span two instances. */
 int nsfv1_set_instances(nsfv1_disc* h, int n_inst, const int32_t* node_offsets);
 
+/* Declares every instance a structured square grid of cells[i] x cells[i]
+ * quadrilaterals (lexicographic nodes, ugcore corner order) and builds the
+ * geometric multigrid hierarchy used as the GMRES preconditioner of
+ * nsfv1_newton_solve_batched: vertex-nested coarse levels down to 4 cells per
+ * side (rediscretised Jacobians at the injected state, bilinear prolongation,
+ * restriction = its transpose, damped point-block Jacobi smoothing). */
+int nsfv1_set_instance_grids(nsfv1_disc* h, const int32_t* cells);
+
 typedef struct {
-    int cluster_size;   /* CTAs per thread-block cluster working on one instance (1..16; 0 = 4) */
-    int max_clusters;   /* upper bound on concurrently resident clusters (0 = as many as fit)  */
+    int cluster_size;    /* CTAs per thread-block cluster working on one instance (1..16; 0 = 4)   */
+    int max_clusters;    /* upper bound on concurrently resident clusters (0 = as many as fit)     */
+    int mg_levels;       /* 0: point-block Jacobi only; otherwise the multigrid V-cycle (if built)  */
+    int smooth_steps;    /* V-cycle pre/post smoothing sweeps (0 = 2)                               */
+    int coarse_steps;    /* sweeps on the coarsest level (0 = 20)                                   */
+    double smooth_omega; /* damping of the smoother (0 = 0.7)                                       */
 } nsfv1_batch_options;
 
 /* Newton on every instance at once (each to its own ||d_i|| <= rtol ||d_i,0||):

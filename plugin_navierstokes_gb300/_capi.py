@@ -57,7 +57,8 @@ class NewtonResult(ctypes.Structure):
 
 
 class BatchOptions(ctypes.Structure):
-    _fields_ = [("cluster_size", c_int), ("max_clusters", c_int)]
+    _fields_ = [("cluster_size", c_int), ("max_clusters", c_int), ("mg_levels", c_int), ("smooth_steps", c_int),
+                ("coarse_steps", c_int), ("smooth_omega", c_double)]
 
 
 class NSFV1Error(RuntimeError):
@@ -100,6 +101,7 @@ _SIGS = {
     "nsfv1_newton_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(NewtonResult), c_void_p]),
     "nsfv1_set_elem_viscosity": (c_int, [c_void_p, c_void_p]),
     "nsfv1_set_instances": (c_int, [c_void_p, c_int, c_void_p]),
+    "nsfv1_set_instance_grids": (c_int, [c_void_p, c_void_p]),
     "nsfv1_newton_solve_batched": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(BatchOptions),
                                            c_void_p, c_void_p]),
     "nsfv1_ref_tables": (c_int, [c_int, POINTER(c_int), POINTER(c_int), c_void_p, POINTER(c_int), c_void_p, c_void_p, c_void_p]),

@@ -28,6 +28,32 @@ static constexpr int kGT = 256;      // threads per CTA of the GMRES kernel
 static constexpr int kMaxM = 32;     // largest restart length
 static constexpr int kWarps = kGT / 32;
 
+static constexpr int kMaxLevels = 8;
+
+// one level of the geometric multigrid hierarchy (level 0 = the fine mesh)
+template <typename VT>
+struct MgLevel {
+    const int32_t* rowPtr;
+    const int32_t* colIdx;
+    const VT* vals;
+    const VT* Dinv;
+    const int32_t* node0;   // [nInst] first node of each instance on this level, -1 if absent
+    const uint8_t* mask;    // [dofs] 1 = free row, 0 = Dirichlet row
+    VT* x;                  // level correction
+    VT* r;                  // level right-hand side
+    VT* s;                  // residual scratch
+};
+
+template <typename VT>
+struct MgArgs {
+    int nLevels;            // 0: point-block Jacobi preconditioner
+    const int32_t* cells0;  // [nInst] cells per side on level 0
+    int nu;                 // pre/post smoothing sweeps
+    int nuCoarse;           // sweeps on the coarsest level
+    double omega;           // damping of the point-block Jacobi smoother
+    MgLevel<VT> lv[kMaxLevels];
+};
+
 template <typename VT>
 struct GmresBatchArgs {
     const int32_t* queue;      // instance ids, largest first
@@ -48,6 +74,8 @@ struct GmresBatchArgs {
     int maxit;
     int* itersOut;
     double* relresOut;
+    VT* q;                     // extra vector [nTot] (V y before the final preconditioning)
+    MgArgs<VT> mg;
 };
 
 // warp-level part of a reduction: the warp sum of v goes to wred[warp][k]
@@ -141,9 +169,9 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                 }
             }
         };
-        // out = Dinv in (per node)
-        auto precond = [&](const VT* __restrict__ in, VT* __restrict__ out) {
-            for (int64_t nd = ctid; nd < nNode; nd += cth) {
+        // point-block Jacobi: out = Dm (in) (per node, optionally damped / accumulated)
+        auto jacobi = [&](const VT* __restrict__ Dm, int64_t nn, const VT* __restrict__ in, VT* __restrict__ out, VT w, bool accumulate) {
+            for (int64_t nd = ctid; nd < nn; nd += cth) {
                 VT xi[b];
 #pragma unroll
                 for (int j = 0; j < b; ++j) xi[j] = in[nd * b + j];
@@ -151,8 +179,139 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                 for (int i = 0; i < b; ++i) {
                     VT a = VT(0);
 #pragma unroll
-                    for (int j = 0; j < b; ++j) a += Dinv[nd * b * b + i * b + j] * xi[j];
-                    out[nd * b + i] = a;
+                    for (int j = 0; j < b; ++j) a += Dm[nd * b * b + i * b + j] * xi[j];
+                    out[nd * b + i] = accumulate ? out[nd * b + i] + w * a : w * a;
+                }
+            }
+        };
+        // level SpMV with residual epilogue: res = rhs - M_l x  (rhs == nullptr: res = M_l x)
+        auto lspmv = [&](const MgLevel<VT>& L, int64_t n0, int64_t nn, const VT* __restrict__ xin, const VT* __restrict__ rhsl,
+                         VT* __restrict__ res) {
+            const int lane = ctid % G;
+            const int64_t trips = (nn + nGroups - 1) / nGroups;
+            const int64_t ol = n0 * b;
+            for (int64_t it = 0; it < trips; ++it) {
+                const int64_t lr = ctid / G + it * nGroups;
+                const bool valid = lr < nn;
+                const int64_t row = n0 + lr;
+                const int64_t q0 = valid ? L.rowPtr[row] : 0, q1 = valid ? L.rowPtr[row + 1] : 0;
+                VT acc[b];
+#pragma unroll
+                for (int i = 0; i < b; ++i) acc[i] = VT(0);
+                for (int64_t idx = q0 * b * b + lane; idx < q1 * b * b; idx += G) {
+                    const int64_t q = idx / (b * b);
+                    const int w = (int)(idx - q * (b * b));
+                    const int i = w / b, j = w - (w / b) * b;
+                    const VT v = L.vals[idx] * xin[(int64_t)L.colIdx[q] * b + j - ol];
+#pragma unroll
+                    for (int r = 0; r < b; ++r)
+                        if (r == i) acc[r] += v;
+                }
+#pragma unroll
+                for (int off = G / 2; off > 0; off >>= 1)
+#pragma unroll
+                    for (int r = 0; r < b; ++r) acc[r] += __shfl_down_sync(0xffffffffu, acc[r], off, G);
+                if (valid && lane == 0) {
+#pragma unroll
+                    for (int r = 0; r < b; ++r) res[lr * b + r] = rhsl ? rhsl[lr * b + r] - acc[r] : acc[r];
+                }
+            }
+        };
+        // instance levels: cells per side, first node on each level
+        const int nLev = A.mg.nLevels;
+        int myLev = 0;
+        int64_t ln0[kMaxLevels];
+        int lcell[kMaxLevels];
+        for (int l = 0; l < nLev; ++l) {
+            const int32_t v = A.mg.lv[l].node0[inst];
+            if (v < 0) break;
+            ln0[l] = v;
+            lcell[l] = A.mg.cells0[inst] >> l;
+            myLev = l + 1;
+        }
+        // V-cycle: out = M^-1 in on level 0 (in/out instance-local); point-block
+        // Jacobi when the instance has no coarse level
+        auto precond = [&](const VT* __restrict__ in, VT* __restrict__ out) {
+            if (myLev <= 1) { jacobi(Dinv, nNode, in, out, VT(1), false); return; }
+            const VT om = (VT)A.mg.omega;
+            auto lx = [&](int l) { return l == 0 ? out : A.mg.lv[l].x + ln0[l] * b; };
+            auto lr = [&](int l) { return l == 0 ? in : (const VT*)(A.mg.lv[l].r + ln0[l] * b); };
+            auto ls = [&](int l) { return A.mg.lv[l].s + ln0[l] * b; };
+            auto lD = [&](int l) { return A.mg.lv[l].Dinv + ln0[l] * b * b; };
+            auto lnn = [&](int l) { return (int64_t)(lcell[l] + 1) * (lcell[l] + 1); };
+            for (int l = 0; l < myLev; ++l) {
+                const MgLevel<VT>& L = A.mg.lv[l];
+                const int64_t nn = lnn(l);
+                const int sweeps = (l == myLev - 1) ? A.mg.nuCoarse : A.mg.nu;
+                jacobi(lD(l), nn, lr(l), lx(l), om, false);
+                cl.sync();
+                for (int k = 1; k < sweeps; ++k) {
+                    lspmv(L, ln0[l], nn, lx(l), lr(l), ls(l));
+                    cl.sync();
+                    jacobi(lD(l), nn, ls(l), lx(l), om, true);
+                    cl.sync();
+                }
+                if (l == myLev - 1) break;
+                lspmv(L, ln0[l], nn, lx(l), lr(l), ls(l));
+                cl.sync();
+                // restriction (transpose of bilinear interpolation), masked on both levels
+                const int nf = lcell[l], nc = lcell[l + 1];
+                const int64_t mf = nf + 1, mc = nc + 1;
+                const uint8_t* mkf = L.mask + ln0[l] * b;
+                const uint8_t* mkc = A.mg.lv[l + 1].mask + ln0[l + 1] * b;
+                VT* rc = A.mg.lv[l + 1].r + ln0[l + 1] * b;
+                const VT* sf = ls(l);
+                for (int64_t c = ctid; c < mc * mc; c += cth) {
+                    const int64_t I = c % mc, J = c / mc;
+                    VT acc[b];
+#pragma unroll
+                    for (int f = 0; f < b; ++f) acc[f] = VT(0);
+#pragma unroll
+                    for (int dj = -1; dj <= 1; ++dj)
+#pragma unroll
+                        for (int di = -1; di <= 1; ++di) {
+                            const int64_t fi = 2 * I + di, fj = 2 * J + dj;
+                            if (fi < 0 || fj < 0 || fi >= mf || fj >= mf) continue;
+                            const VT w = (di == 0 ? VT(1) : VT(0.5)) * (dj == 0 ? VT(1) : VT(0.5));
+                            const int64_t fn = fj * mf + fi;
+#pragma unroll
+                            for (int f = 0; f < b; ++f)
+                                if (mkf[fn * b + f]) acc[f] += w * sf[fn * b + f];
+                        }
+#pragma unroll
+                    for (int f = 0; f < b; ++f) rc[c * b + f] = mkc[c * b + f] ? acc[f] : VT(0);
+                }
+                cl.sync();
+            }
+            for (int l = myLev - 2; l >= 0; --l) {
+                const MgLevel<VT>& L = A.mg.lv[l];
+                const int64_t nn = lnn(l);
+                // prolongation (bilinear) of the coarse correction, masked
+                const int nf = lcell[l];
+                const int64_t mf = nf + 1, mc = lcell[l + 1] + 1;
+                const uint8_t* mkf = L.mask + ln0[l] * b;
+                const VT* xc = lx(l + 1);
+                VT* xf = lx(l);
+                for (int64_t fnode = ctid; fnode < mf * mf; fnode += cth) {
+                    const int64_t I = fnode % mf, J = fnode / mf;
+                    const int64_t i0 = I / 2, j0 = J / 2;
+                    const int64_t i1 = (I & 1) ? i0 + 1 : i0, j1 = (J & 1) ? j0 + 1 : j0;
+                    const VT wi = (I & 1) ? VT(0.5) : VT(1), wj = (J & 1) ? VT(0.5) : VT(1);
+#pragma unroll
+                    for (int f = 0; f < b; ++f) {
+                        VT v = wi * wj * xc[(j0 * mc + i0) * b + f];
+                        if (I & 1) v += wi * wj * xc[(j0 * mc + i1) * b + f];
+                        if (J & 1) v += wi * wj * xc[(j1 * mc + i0) * b + f];
+                        if ((I & 1) && (J & 1)) v += wi * wj * xc[(j1 * mc + i1) * b + f];
+                        if (mkf[fnode * b + f]) xf[fnode * b + f] += v;
+                    }
+                }
+                cl.sync();
+                for (int k = 0; k < A.mg.nu; ++k) {
+                    lspmv(L, ln0[l], nn, lx(l), lr(l), ls(l));
+                    cl.sync();
+                    jacobi(lD(l), nn, ls(l), lx(l), om, true);
+                    cl.sync();
                 }
             }
         };
@@ -243,21 +402,16 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                     }
                 }
                 __syncthreads();
+                VT* qv = A.q + o;
                 for (int64_t e = ctid; e < n; e += cth) {
                     VT a = VT(0);
                     for (int k = 0; k < j; ++k) a += (VT)yv[k] * Vk(k)[e];
-                    t[e] = a;
+                    qv[e] = a;
                 }
                 cl.sync();
-                for (int64_t nd = ctid; nd < nNode; nd += cth) {
-#pragma unroll
-                    for (int i = 0; i < b; ++i) {
-                        VT a = x[nd * b + i];
-#pragma unroll
-                        for (int jj = 0; jj < b; ++jj) a += Dinv[nd * b * b + i * b + jj] * t[nd * b + jj];
-                        x[nd * b + i] = a;
-                    }
-                }
+                precond(qv, t);
+                cl.sync();
+                for (int64_t e = ctid; e < n; e += cth) x[e] += t[e];
                 cl.sync();
                 if (done || total >= A.maxit || !isfinite(relres)) break;
                 // restart: V_0 = rhs - M x
@@ -303,6 +457,13 @@ __global__ void k_block_inv_active(int64_t nRows, const int32_t* __restrict__ di
     if (!block_inverse<b>(vals + (int64_t)diagPos[r] * b * b, Dinv + r * b * b)) atomicOr(err, 2);
 }
 
+template <typename VT, int b>
+__global__ void k_block_inv_all(int64_t nRows, const int32_t* __restrict__ diagPos, const VT* __restrict__ vals, VT* __restrict__ Dinv, int* err) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nRows) return;
+    if (!block_inverse<b>(vals + (int64_t)diagPos[r] * b * b, Dinv + r * b * b)) atomicOr(err, 2);
+}
+
 // trial iterate: ut = u - lambda[inst] du on the nodes of pending instances
 template <typename VT>
 __global__ void k_batch_trial(int64_t n, int b, const int32_t* __restrict__ nodeInst, const int32_t* __restrict__ pending,
@@ -312,6 +473,12 @@ __global__ void k_batch_trial(int64_t n, int b, const int32_t* __restrict__ node
     if (e >= n) return;
     const int inst = nodeInst[e / b];
     if (pending[inst]) ut[e] = u[e] - lambda[inst] * (double)du[e];
+}
+
+// state of a coarse level: u_c[node] = u_f[inj[node]]
+__global__ void k_inject(int64_t nc, int b, const int32_t* __restrict__ inj, const double* __restrict__ uf, double* __restrict__ uc) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < nc * b) uc[e] = uf[(int64_t)inj[e / b] * b + e % b];
 }
 
 // copy the rows of flagged instances: dst[e] = src[e]
@@ -374,12 +541,12 @@ struct BatchWs {
     int prec = -1, m = 0;
     int64_t n = 0;
     double *D = nullptr, *Dt = nullptr, *Ut = nullptr, *nrm = nullptr, *lambda = nullptr, *relres = nullptr;
-    void *J = nullptr, *Dinv = nullptr, *V = nullptr, *t = nullptr, *x = nullptr;
+    void *J = nullptr, *Dinv = nullptr, *V = nullptr, *t = nullptr, *x = nullptr, *q = nullptr, *s = nullptr;
     int32_t *queue = nullptr, *head = nullptr, *pending = nullptr, *accepted = nullptr, *iters = nullptr;
     ~BatchWs() { release(); }
     void release() {
         auto f = [](auto*& p) { if (p) cudaFree((void*)p); p = nullptr; };
-        f(D); f(Dt); f(Ut); f(nrm); f(lambda); f(relres); f(J); f(Dinv); f(V); f(t); f(x);
+        f(D); f(Dt); f(Ut); f(nrm); f(lambda); f(relres); f(J); f(Dinv); f(V); f(t); f(x); f(q); f(s);
         f(queue); f(head); f(pending); f(accepted); f(iters);
         prec = -1;
     }
@@ -399,8 +566,37 @@ void batch_free(void* p);
 
 namespace {
 
+// a coarse level of the structured-instance hierarchy
+struct Level {
+    Disc* disc = nullptr;          // the level mesh (all instances that have this level)
+    std::vector<int32_t> node0;    // [nInst] first node of each instance on this level, -1 if absent
+    int32_t* d_node0 = nullptr;
+    int32_t* d_inj = nullptr;      // [level nodes] node of the next finer level at the same point
+    uint8_t* d_mask = nullptr;     // [level dofs] 1 = free row
+    double* d_u = nullptr;         // injected state
+    void *J = nullptr, *Dinv = nullptr, *x = nullptr, *r = nullptr, *s = nullptr;
+    int prec = -1;
+    void release() {
+        auto f = [](auto*& p) { if (p) cudaFree((void*)p); p = nullptr; };
+        f(d_node0); f(d_inj); f(d_mask); f(d_u); f(J); f(Dinv); f(x); f(r); f(s);
+        delete disc; disc = nullptr;
+        prec = -1;
+    }
+};
+
 struct BatchState {
     BatchWs ws;
+    std::vector<Level> levels;     // levels[0] unused (the handle's own mesh); levels[l], l >= 1
+    uint8_t* d_mask0 = nullptr;    // Dirichlet mask of the fine level
+    int32_t* d_cells = nullptr;    // [nInst] cells per side
+    ~BatchState() { clear_levels(); }
+    void clear_levels() {
+        for (auto& L : levels) L.release();
+        levels.clear();
+        if (d_mask0) cudaFree(d_mask0);
+        if (d_cells) cudaFree(d_cells);
+        d_mask0 = nullptr; d_cells = nullptr;
+    }
 };
 
 BatchState* batch_state(Disc& D) {
@@ -423,7 +619,8 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
         auto al = [&](auto*& ptr, size_t bytes) { return D.cuda_ok(cudaMalloc((void**)&ptr, bytes), "batch workspace"); };
         if (!al(W.D, n * 8) || !al(W.Dt, n * 8) || !al(W.Ut, n * 8) || !al(W.nrm, nInst * 8) || !al(W.lambda, nInst * 8) ||
             !al(W.relres, nInst * 8) || !al(W.J, D.colIdx.size() * b * b * vt) || !al(W.Dinv, (size_t)D.nNodes * b * b * vt) ||
-            !al(W.V, (size_t)(m + 1) * n * vt) || !al(W.t, n * vt) || !al(W.x, n * vt) || !al(W.queue, nInst * 4) ||
+            !al(W.V, (size_t)(m + 1) * n * vt) || !al(W.t, n * vt) || !al(W.x, n * vt) || !al(W.q, n * vt) || !al(W.s, n * vt) ||
+            !al(W.queue, nInst * 4) ||
             !al(W.head, 4) || !al(W.pending, nInst * 4) || !al(W.accepted, nInst * 4) || !al(W.iters, nInst * 4))
             return D.status;
         W.prec = prec; W.n = n; W.m = m;
@@ -477,6 +674,35 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
         cudaMemsetAsync(D.d_err, 0, sizeof(int), s);
         if (b == 4) k_block_inv_active<VT, 4><<<(int)((D.nNodes + 127) / 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, D.d_nodeInst, D.d_instActive, (VT*)W.J, (VT*)W.Dinv, D.d_err);
         else k_block_inv_active<VT, 3><<<(int)((D.nNodes + 127) / 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, D.d_nodeInst, D.d_instActive, (VT*)W.J, (VT*)W.Dinv, D.d_err);
+        // coarse levels: inject the state, assemble, invert the diagonal blocks
+        BatchState* BS = batch_state(D);
+        const bool useMG = opt.mg_levels != 0 && BS->levels.size() > 1;
+        if (useMG) {
+            const double* uf = u;
+            for (size_t l = 1; l < BS->levels.size(); ++l) {
+                Level& L = BS->levels[l];
+                Disc& C = *L.disc;
+                const int64_t nc = C.nNodes;
+                if (L.prec != prec) {
+                    auto f = [](auto*& p) { if (p) cudaFree((void*)p); p = nullptr; };
+                    f(L.J); f(L.Dinv); f(L.x); f(L.r); f(L.s);
+                    const size_t vt = sizeof(VT);
+                    if (!D.cuda_ok(cudaMalloc(&L.J, C.colIdx.size() * b * b * vt), "level J") ||
+                        !D.cuda_ok(cudaMalloc(&L.Dinv, (size_t)nc * b * b * vt), "level Dinv") ||
+                        !D.cuda_ok(cudaMalloc(&L.x, (size_t)nc * b * vt), "level x") ||
+                        !D.cuda_ok(cudaMalloc(&L.r, (size_t)nc * b * vt), "level r") ||
+                        !D.cuda_ok(cudaMalloc(&L.s, (size_t)nc * b * vt), "level s"))
+                        return D.status;
+                    L.prec = prec;
+                }
+                k_inject<<<(int)((nc * b + 255) / 256), 256, 0, s>>>(nc, b, L.d_inj, uf, L.d_u);
+                if (!C.assemble_jacobian(L.d_u, nullptr, dt, L.J, prec, s, false)) { D.fail(C.status, C.lastError); return D.status; }
+                cudaMemsetAsync(C.d_err, 0, sizeof(int), s);
+                if (b == 4) k_block_inv_all<VT, 4><<<(int)((nc + 127) / 128), 128, 0, s>>>(nc, C.d_diagPos, (VT*)L.J, (VT*)L.Dinv, D.d_err);
+                else k_block_inv_all<VT, 3><<<(int)((nc + 127) / 128), 128, 0, s>>>(nc, C.d_diagPos, (VT*)L.J, (VT*)L.Dinv, D.d_err);
+                uf = L.d_u;
+            }
+        }
         // queue: active instances, largest first
         std::vector<int32_t> q;
         for (int i = 0; i < nInst; ++i) if (active[i]) q.push_back(i);
@@ -484,7 +710,22 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
         if (!D.cuda_ok(cudaMemcpyAsync(W.queue, q.data(), q.size() * 4, cudaMemcpyHostToDevice, s), "queue")) return D.status;
         cudaMemsetAsync(W.head, 0, 4, s);
         GmresBatchArgs<VT> a{W.queue, (int)q.size(), W.head, D.d_instNode0, D.d_rowPtr, D.d_colIdx, (const VT*)W.J, (const VT*)W.Dinv,
-                             W.D, (VT*)W.x, (VT*)W.V, (VT*)W.t, n, m, p.lin_rtol, p.lin_max_iter, W.iters, W.relres};
+                             W.D, (VT*)W.x, (VT*)W.V, (VT*)W.t, n, m, p.lin_rtol, p.lin_max_iter, W.iters, W.relres, (VT*)W.q, {}};
+        a.mg.nLevels = 0;
+        if (useMG) {
+            a.mg.nLevels = (int)BS->levels.size();
+            a.mg.cells0 = BS->d_cells;
+            a.mg.nu = opt.smooth_steps > 0 ? opt.smooth_steps : 2;
+            a.mg.nuCoarse = opt.coarse_steps > 0 ? opt.coarse_steps : 20;
+            a.mg.omega = opt.smooth_omega > 0.0 ? opt.smooth_omega : 0.7;
+            a.mg.lv[0] = MgLevel<VT>{D.d_rowPtr, D.d_colIdx, (const VT*)W.J, (const VT*)W.Dinv, D.d_instNode0, BS->d_mask0,
+                                     (VT*)W.t, nullptr, (VT*)W.s};
+            for (size_t l = 1; l < BS->levels.size(); ++l) {
+                Level& L = BS->levels[l];
+                a.mg.lv[l] = MgLevel<VT>{L.disc->d_rowPtr, L.disc->d_colIdx, (const VT*)L.J, (const VT*)L.Dinv, L.d_node0, L.d_mask,
+                                         (VT*)L.x, (VT*)L.r, (VT*)L.s};
+            }
+        }
         cudaError_t le = (b == 4) ? launch_gmres_batch<VT, 4>(a, clusterSize, std::min(nClusters, (int)q.size()), s)
                                   : launch_gmres_batch<VT, 3>(a, clusterSize, std::min(nClusters, (int)q.size()), s);
         if (!D.cuda_ok(le, "batched GMRES launch")) return D.status;
@@ -567,12 +808,14 @@ int nsfv1_set_elem_viscosity(nsfv1_disc* h, const double* nu) {
     D->status = NSFV1_OK;
     if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "set_elem_viscosity: no mesh"); return D->status; }
     if (D->d_nuElem) { cudaFree(D->d_nuElem); D->d_nuElem = nullptr; }
+    D->nuElemHost.clear();
     if (!nu) return NSFV1_OK;
     for (int64_t e = 0; e < D->nElems; ++e)
         if (!(nu[e] > 0.0) || !std::isfinite(nu[e])) { D->fail(NSFV1_ERR_ARGUMENT, "set_elem_viscosity: viscosity must be positive"); return D->status; }
     if (!D->cuda_ok(cudaMalloc((void**)&D->d_nuElem, sizeof(double) * D->nElems), "alloc viscosity") ||
         !D->cuda_ok(cudaMemcpy(D->d_nuElem, nu, sizeof(double) * D->nElems, cudaMemcpyHostToDevice), "upload viscosity"))
         return D->status;
+    D->nuElemHost.assign(nu, nu + D->nElems);
     D->viscoSet = true;
     return NSFV1_OK;
 }
@@ -614,6 +857,118 @@ int nsfv1_set_instances(nsfv1_disc* h, int n_inst, const int32_t* node_offsets) 
     D->nInst = n_inst;
     D->instNode0.assign(node_offsets, node_offsets + n_inst + 1);
     D->instSkip = false;
+    return NSFV1_OK;
+}
+
+int nsfv1_set_instance_grids(nsfv1_disc* h, const int32_t* cells) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (!D->hasMesh || D->nInst <= 0) { D->fail(NSFV1_ERR_STATE, "set_instance_grids: set the mesh and the instances first"); return D->status; }
+    if (D->roid != ROID_QUADRILATERAL) { D->fail(NSFV1_ERR_ARGUMENT, "set_instance_grids: structured quadrilateral instances only"); return D->status; }
+    const int nInst = D->nInst, b = D->dim + 1;
+    for (int i = 0; i < nInst; ++i) {
+        const int64_t m = (int64_t)cells[i] + 1;
+        if (cells[i] <= 0 || m * m != D->instNode0[i + 1] - D->instNode0[i]) {
+            D->fail(NSFV1_ERR_ARGUMENT, "set_instance_grids: node count of an instance is not (cells+1)^2");
+            return D->status;
+        }
+    }
+    BatchState* BS = batch_state(*D);
+    BS->clear_levels();
+    D->instCells.assign(cells, cells + nInst);
+    // fine-level Dirichlet mask and the cells per side
+    std::vector<uint8_t> mask0((size_t)D->nNodes * b, 1);
+    for (int32_t r : D->dirRowHost) mask0[r] = 0;
+    if (!D->cuda_ok(cudaMalloc((void**)&BS->d_mask0, mask0.size()), "mg mask") ||
+        !D->cuda_ok(cudaMemcpy(BS->d_mask0, mask0.data(), mask0.size(), cudaMemcpyHostToDevice), "mg mask") ||
+        !D->cuda_ok(cudaMalloc((void**)&BS->d_cells, nInst * 4), "mg cells") ||
+        !D->cuda_ok(cudaMemcpy(BS->d_cells, cells, nInst * 4, cudaMemcpyHostToDevice), "mg cells"))
+        return D->status;
+    BS->levels.resize(1);
+    // finer-level data of the current step (level 0 = this handle)
+    std::vector<double> fCoords = D->coordsHost;
+    std::vector<int32_t> fNode0(D->instNode0.begin(), D->instNode0.end() - 1);
+    std::vector<int> fCells(cells, cells + nInst);
+    std::vector<uint8_t> fDir(mask0.size());
+    std::vector<double> fDirVal(mask0.size(), 0.0);
+    for (size_t k = 0; k < D->dirRowHost.size(); ++k) { fDir[D->dirRowHost[k]] = 1; fDirVal[D->dirRowHost[k]] = D->dirValHost[k]; }
+    std::vector<double> instNu(nInst, D->nu);
+    if (!D->nuElemHost.empty()) {
+        std::vector<int32_t> firstElem(nInst, -1);
+        for (int64_t e = D->nElems - 1; e >= 0; --e) {
+            const int32_t nd = D->connHost[e * D->nsh];
+            const int i = (int)(std::upper_bound(D->instNode0.begin(), D->instNode0.end(), nd) - D->instNode0.begin()) - 1;
+            firstElem[i] = (int32_t)e;
+        }
+        for (int i = 0; i < nInst; ++i) instNu[i] = D->nuElemHost[firstElem[i]];
+    }
+    for (int l = 1; l < kMaxLevels; ++l) {
+        // instances that coarsen once more (even cells, at least 4 coarse cells)
+        std::vector<int32_t> cNode0(nInst, -1);
+        std::vector<double> coords;
+        std::vector<int32_t> conn, inj, dirRow;
+        std::vector<double> dirVal, nuE;
+        std::vector<int32_t> instOff{0};
+        int32_t nn = 0;
+        for (int i = 0; i < nInst; ++i) {
+            if (fNode0[i] < 0 || fCells[i] % 2 != 0 || fCells[i] / 2 < 4) continue;
+            const int nc = fCells[i] / 2, mc = nc + 1, mf = fCells[i] + 1;
+            cNode0[i] = nn;
+            for (int J = 0; J < mc; ++J)
+                for (int I = 0; I < mc; ++I) {
+                    const int64_t fnode = fNode0[i] + (int64_t)(2 * J) * mf + 2 * I;
+                    coords.push_back(fCoords[fnode * 2]); coords.push_back(fCoords[fnode * 2 + 1]);
+                    inj.push_back((int32_t)fnode);
+                    for (int f = 0; f < b; ++f)
+                        if (fDir[fnode * b + f]) { dirRow.push_back((nn + J * mc + I) * b + f); dirVal.push_back(fDirVal[fnode * b + f]); }
+                }
+            for (int J = 0; J < nc; ++J)
+                for (int I = 0; I < nc; ++I) {
+                    const int32_t n0 = nn + J * mc + I;
+                    conn.push_back(n0); conn.push_back(n0 + 1); conn.push_back(n0 + mc + 1); conn.push_back(n0 + mc);
+                    nuE.push_back(instNu[i]);
+                }
+            nn += mc * mc;
+            instOff.push_back(nn);
+        }
+        if (nn == 0) break;
+        Level L;
+        L.disc = new Disc();
+        Disc& C = *L.disc;
+        C.dim = D->dim; C.nu = D->nu; C.rho = D->rho; C.fullNewton = D->fullNewton;
+        for (int d = 0; d < 3; ++d) C.src[d] = D->src[d];
+        C.hasSource = D->hasSource; C.stokes = D->stokes; C.laplace = D->laplace; C.peclet = D->peclet;
+        C.viscoSet = D->viscoSet; C.stabSet = D->stabSet; C.convUpwindSet = D->convUpwindSet; C.stabSharesConv = D->stabSharesConv;
+        C.convUpwindType = D->convUpwindType; C.stabUpwindType = D->stabUpwindType; C.stabType = D->stabType; C.diffLen = D->diffLen;
+        nsfv1_disc* ch = reinterpret_cast<nsfv1_disc*>(&C);
+        int st = nsfv1_set_mesh(ch, ROID_QUADRILATERAL, nn, coords.data(), (int64_t)conn.size() / 4, conn.data());
+        if (st == NSFV1_OK) st = nsfv1_set_elem_viscosity(ch, nuE.data());
+        if (st == NSFV1_OK) st = nsfv1_set_dirichlet(ch, (int64_t)dirRow.size(), dirRow.data(), dirVal.data());
+        if (st != NSFV1_OK) { D->fail(st, "multigrid level " + std::to_string(l) + ": " + C.lastError); L.release(); return D->status; }
+        std::vector<uint8_t> mask((size_t)nn * b, 1);
+        for (int32_t r : dirRow) mask[r] = 0;
+        if (!D->cuda_ok(cudaMalloc((void**)&L.d_node0, nInst * 4), "level") ||
+            !D->cuda_ok(cudaMemcpy(L.d_node0, cNode0.data(), nInst * 4, cudaMemcpyHostToDevice), "level") ||
+            !D->cuda_ok(cudaMalloc((void**)&L.d_inj, inj.size() * 4), "level") ||
+            !D->cuda_ok(cudaMemcpy(L.d_inj, inj.data(), inj.size() * 4, cudaMemcpyHostToDevice), "level") ||
+            !D->cuda_ok(cudaMalloc((void**)&L.d_mask, mask.size()), "level") ||
+            !D->cuda_ok(cudaMemcpy(L.d_mask, mask.data(), mask.size(), cudaMemcpyHostToDevice), "level") ||
+            !D->cuda_ok(cudaMalloc((void**)&L.d_u, (size_t)nn * b * 8), "level")) {
+            L.release();
+            return D->status;
+        }
+        L.node0 = cNode0;
+        BS->levels.push_back(std::move(L));
+        // this level becomes the finer level of the next one
+        fCoords = coords;
+        std::vector<int> nCells(nInst, 0);
+        for (int i = 0; i < nInst; ++i) nCells[i] = cNode0[i] >= 0 ? fCells[i] / 2 : 0;
+        std::vector<uint8_t> nDir((size_t)nn * b, 0);
+        std::vector<double> nDirVal((size_t)nn * b, 0.0);
+        for (size_t k = 0; k < dirRow.size(); ++k) { nDir[dirRow[k]] = 1; nDirVal[dirRow[k]] = dirVal[k]; }
+        fNode0 = cNode0; fCells = nCells; fDir = nDir; fDirVal = nDirVal;
+    }
     return NSFV1_OK;
 }
 

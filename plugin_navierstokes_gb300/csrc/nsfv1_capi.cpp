@@ -301,6 +301,9 @@ int nsfv1_set_mesh(nsfv1_disc* h, int elem_type, int64_t n_nodes, const double* 
         D->free_mesh();
         D->hasMesh = false;
         D->roid = elem_type; D->nsh = nsh; D->nNodes = n_nodes; D->nElems = n_elems;
+        D->coordsHost.assign(coords, coords + n_nodes * dim);
+        D->connHost.assign(conn, conn + n_elems * nsh);
+        D->nuElemHost.clear(); D->dirRowHost.clear(); D->dirValHost.clear(); D->instCells.clear();
         build_pattern(nsh, n_nodes, n_elems, conn, D->rowPtr, D->colIdx, D->elemBlk);
         D->nColors = build_coloring(nsh, n_nodes, n_elems, conn, D->color);
         if (D->nColors < 0) { D->fail(NSFV1_ERR_ARGUMENT, "too many element colours"); return D->status; }
@@ -405,6 +408,8 @@ int nsfv1_set_dirichlet(nsfv1_disc* h, int64_t n, const int32_t* dofs, const dou
         !D->cuda_ok(dupload(D->d_dirVal, values, (size_t)n), "upload dirichlet values"))
         return D->status;
     D->nDir = n;
+    D->dirRowHost.assign(dofs, dofs + n);
+    D->dirValHost.assign(values, values + n);
     return NSFV1_OK;
 }
 

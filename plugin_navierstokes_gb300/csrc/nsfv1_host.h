@@ -52,6 +52,10 @@ struct Disc {
     int32_t* d_nodeInst = nullptr;
     int32_t* d_instActive = nullptr;         // per-instance active flag (assembly skips inactive ones)
     bool instSkip = false;                   // assembly honours d_instActive
+    // host copies used to build coarse multigrid levels of structured instances
+    std::vector<double> coordsHost, nuElemHost, dirValHost;
+    std::vector<int32_t> connHost, dirRowHost;
+    std::vector<int32_t> instCells;          // cells per side of each structured instance (nsfv1_set_instance_grids)
     double* d_bjDinv = nullptr;     // nsfv1_block_jacobi scratch: inverted diagonal blocks
     int32_t* d_dirRow = nullptr;
     double* d_dirVal = nullptr;

@@ -194,13 +194,19 @@ class NavierStokesFV1:
         self._c(self._lib.nsfv1_set_instances(self._h, a.size - 1, a.ctypes.data))
         self.n_inst = a.size - 1
 
+    def set_instance_grids(self, cells) -> None:
+        """Structured square instances (cells per side) -> multigrid hierarchy."""
+        a = np.ascontiguousarray(cells, dtype=np.int32)
+        self._c(self._lib.nsfv1_set_instance_grids(self._h, a.ctypes.data))
+
     def newton_solve_batched(self, u, u_old=None, dt: float = 0.0, rtol: float = 1e-8, atol: float = 0.0, max_iter: int = 100,
                              lin_rtol: float = 1e-3, lin_max_iter: int = 3000, line_search_steps: int = 6,
                              jacobian_prec: str = "f64", gmres_restart: int = 30, cluster_size: int = 4, max_clusters: int = 0,
+                             multigrid: bool = True, smooth_steps: int = 2, coarse_steps: int = 20, smooth_omega: float = 0.7,
                              stream=None, raise_on_error: bool = True) -> list[dict]:
         p = _capi.NewtonParams(rtol, atol, max_iter, lin_rtol, lin_max_iter, line_search_steps,
                                _capi.F64 if jacobian_prec == "f64" else _capi.F32, _capi.GMRES, gmres_restart)
-        o = _capi.BatchOptions(cluster_size, max_clusters)
+        o = _capi.BatchOptions(cluster_size, max_clusters, 1 if multigrid else 0, smooth_steps, coarse_steps, smooth_omega)
         res = (_capi.NewtonResult * self.n_inst)()
         st = self._lib.nsfv1_newton_solve_batched(self._h, _ptr(u), _ptr(u_old), float(dt), ctypes.byref(p), ctypes.byref(o),
                                                   ctypes.addressof(res), _stream_ptr(stream))
