@@ -223,6 +223,10 @@ typedef struct {
     int smooth_steps;    /* V-cycle pre/post smoothing sweeps (0 = 2)                               */
     int coarse_steps;    /* sweeps on the coarsest level (0 = 20)                                   */
     double smooth_omega; /* damping of the smoother (0 = 0.7)                                       */
+    int defect_reference;/* 0: rtol relative to each instance's initial iterate; 1: relative to the   */
+                         /*    defect of the zero iterate (Dirichlet values, 0 elsewhere)             */
+    int zero_fallback;   /* with defect_reference 1: an instance whose initial defect exceeds the     */
+                         /*    zero iterate's restarts from the zero iterate                          */
 } nsfv1_batch_options;
 
 /* Newton on every instance at once (each to its own ||d_i|| <= rtol ||d_i,0||):
@@ -233,6 +237,62 @@ typedef struct {
  * receives each instance's iterations, linear iterations, defects and status. */
 int nsfv1_newton_solve_batched(nsfv1_disc* h, double* u, const double* u_old, double dt, const nsfv1_newton_params* p,
                                const nsfv1_batch_options* opt, nsfv1_newton_result* results, void* stream);
+
+/* ---- learned warm start: coordinate MLP on the tensor cores --------------- *
+ * (no reference counterpart: the reference starts Newton from the caller's
+ * iterate). Features [sin, cos](pi k x), [sin, cos](pi k y), k = 1..16; four
+ * FiLM-conditioned SiLU layers of width 256; head 256 -> 3 predicting
+ * (u/lid, v/lid, p/lid^2). BF16 GEMM operands, FP32 accumulation (tcgen05),
+ * FP32 master weights and Adam. Points come in contiguous slots (one
+ * conditioning each): slot_ptr[n_slots+1] on the host, from 0 to n_points. */
+typedef struct nsfv1_mlp nsfv1_mlp;
+typedef struct {
+    int max_points;      /* point capacity of one forward / training batch */
+    int max_slots;       /* slots (instances) per batch */
+} nsfv1_mlp_config;
+typedef struct {
+    int64_t n_train;     /* training instances, all on one mesh */
+    int64_t n_nodes;     /* nodes of that mesh */
+    const float* coords; /* device [n_nodes x 2] */
+    const float* targets;/* device [n_train x n_nodes x 3], normalised (nsfv1_mlp_targets) */
+    const float* cond;   /* device [n_train x 2], nsfv1_mlp_condition of each instance */
+} nsfv1_mlp_dataset;
+typedef struct {
+    int steps;           /* Adam steps */
+    int slots;           /* instances per minibatch */
+    int points_per_slot; /* nodes drawn per instance */
+    float lr, lr_final;  /* cosine schedule from lr to lr_final */
+    uint64_t seed;
+    int64_t step_offset; /* first step index of the sampler (to continue a run) */
+} nsfv1_mlp_train_params;
+
+int nsfv1_mlp_create(const nsfv1_mlp_config* cfg, nsfv1_mlp** out);
+void nsfv1_mlp_destroy(nsfv1_mlp* m);
+const char* nsfv1_mlp_last_error(const nsfv1_mlp* m);
+int64_t nsfv1_mlp_num_params(const nsfv1_mlp* m);
+/* conditioning of one cavity: c = ((ln Re - ln 100) / ln 10, (lid - 1.25) / 0.75) */
+void nsfv1_mlp_condition(double re, double lid, float* c2);
+int nsfv1_mlp_init(nsfv1_mlp* m, uint64_t seed);
+int nsfv1_mlp_get_params(nsfv1_mlp* m, float* host, int64_t n);
+int nsfv1_mlp_set_params(nsfv1_mlp* m, const float* host, int64_t n);
+/* out[n x 3] (device) = network output at xy[n x 2] (device); cond host [n_slots x 2] */
+int nsfv1_mlp_forward(nsfv1_mlp* m, int64_t n_points, const float* xy, int n_slots, const int32_t* slot_ptr, const float* cond,
+                      float* out, void* stream);
+/* loss (host) and the gradient of every parameter (device [num_params]) against target[n x 3] (device) */
+int nsfv1_mlp_loss_grad(nsfv1_mlp* m, int64_t n_points, const float* xy, int n_slots, const int32_t* slot_ptr, const float* cond,
+                        const float* target, double* loss, float* grad, void* stream);
+/* Adam training on minibatches drawn on the device; loss_history[steps] (host) may be NULL */
+int nsfv1_mlp_train(nsfv1_mlp* m, const nsfv1_mlp_dataset* data, const nsfv1_mlp_train_params* tp, float* loss_history, void* stream);
+/* normalised targets of n_instances solutions on one mesh: u device [n_instances x n_nodes x 3] (FP64), lid device [n_instances] */
+int nsfv1_mlp_targets(int64_t n_instances, int64_t n_nodes, const double* u, const double* lid, float* targets, void* stream);
+/* Newton initial iterate: u[n x 3] (device, FP64) = (lid out_0, lid out_1, lid^2 out_2); cond, lid host per slot */
+int nsfv1_mlp_predict(nsfv1_mlp* m, int64_t n_points, const float* xy, int n_slots, const int32_t* slot_ptr, const float* cond,
+                      const float* lid, double* u, void* stream);
+/* the tensor-core GEMM itself: C[splits][M][N] (FP32) = A[M x K] * B[N x K]^T over K
+ * chunks (BF16 row-major operands; M % 128 == 0, K % 64 == 0, N = 64, 128 or a multiple of 256) */
+int nsfv1_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* C, int splits, void* stream);
+/* the number of K chunks nsfv1_gemm_bf16 uses for K and a requested split count */
+int nsfv1_gemm_bf16_splits(int K, int splits);
 
 /* reference-element tables used by the kernels (for the table-consistency test):
  * edges[2*nedge], sides[4*nside] (unused slots -1), side_nco[nside], edge_face[2*nedge] */

@@ -58,7 +58,21 @@ class NewtonResult(ctypes.Structure):
 
 class BatchOptions(ctypes.Structure):
     _fields_ = [("cluster_size", c_int), ("max_clusters", c_int), ("mg_levels", c_int), ("smooth_steps", c_int),
-                ("coarse_steps", c_int), ("smooth_omega", c_double)]
+                ("coarse_steps", c_int), ("smooth_omega", c_double), ("defect_reference", c_int), ("zero_fallback", c_int)]
+
+
+class MlpConfig(ctypes.Structure):
+    _fields_ = [("max_points", c_int), ("max_slots", c_int)]
+
+
+class MlpDataset(ctypes.Structure):
+    _fields_ = [("n_train", ctypes.c_int64), ("n_nodes", ctypes.c_int64), ("coords", c_void_p), ("targets", c_void_p),
+                ("cond", c_void_p)]
+
+
+class MlpTrainParams(ctypes.Structure):
+    _fields_ = [("steps", c_int), ("slots", c_int), ("points_per_slot", c_int), ("lr", ctypes.c_float),
+                ("lr_final", ctypes.c_float), ("seed", ctypes.c_uint64), ("step_offset", ctypes.c_int64)]
 
 
 class NSFV1Error(RuntimeError):
@@ -105,6 +119,22 @@ _SIGS = {
     "nsfv1_newton_solve_batched": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(BatchOptions),
                                            c_void_p, c_void_p]),
     "nsfv1_ref_tables": (c_int, [c_int, POINTER(c_int), POINTER(c_int), c_void_p, POINTER(c_int), c_void_p, c_void_p, c_void_p]),
+    "nsfv1_mlp_create": (c_int, [POINTER(MlpConfig), POINTER(c_void_p)]),
+    "nsfv1_mlp_destroy": (None, [c_void_p]),
+    "nsfv1_mlp_last_error": (c_char_p, [c_void_p]),
+    "nsfv1_mlp_num_params": (ctypes.c_int64, [c_void_p]),
+    "nsfv1_mlp_condition": (None, [c_double, c_double, c_void_p]),
+    "nsfv1_mlp_init": (c_int, [c_void_p, ctypes.c_uint64]),
+    "nsfv1_mlp_get_params": (c_int, [c_void_p, c_void_p, ctypes.c_int64]),
+    "nsfv1_mlp_set_params": (c_int, [c_void_p, c_void_p, ctypes.c_int64]),
+    "nsfv1_mlp_forward": (c_int, [c_void_p, ctypes.c_int64, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "nsfv1_mlp_loss_grad": (c_int, [c_void_p, ctypes.c_int64, c_void_p, c_int, c_void_p, c_void_p, c_void_p, POINTER(c_double),
+                                    c_void_p, c_void_p]),
+    "nsfv1_mlp_train": (c_int, [c_void_p, POINTER(MlpDataset), POINTER(MlpTrainParams), c_void_p, c_void_p]),
+    "nsfv1_mlp_targets": (c_int, [ctypes.c_int64, ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "nsfv1_mlp_predict": (c_int, [c_void_p, ctypes.c_int64, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "nsfv1_gemm_bf16": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "nsfv1_gemm_bf16_splits": (c_int, [c_int, c_int]),
 }
 
 

@@ -654,11 +654,32 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
     if (!D.assemble_defect(u, u_old, dt, W.D, s)) return D.status;
     if (!norms(W.D, nd0)) return D.status;
     nd = nd0;
+    if (opt.defect_reference == 1) {
+        // reference defect of the zero iterate (Dirichlet values, 0 elsewhere)
+        std::vector<double> ndz(nInst, 0.0);
+        cudaMemsetAsync(W.Ut, 0, n * 8, s);
+        if (!D.set_dirichlet_values(W.Ut, s)) return D.status;
+        if (!D.assemble_defect(W.Ut, u_old, dt, W.Dt, s)) return D.status;
+        if (!norms(W.Dt, ndz)) return D.status;
+        if (opt.zero_fallback) {
+            for (int i = 0; i < nInst; ++i) acc[i] = !(nd0[i] <= ndz[i]);   // also restarts a non-finite iterate
+            if (!upload_flags(acc, W.accepted)) return D.status;
+            k_batch_copy<<<g, 256, 0, s>>>(n, b, D.d_nodeInst, W.accepted, W.Ut, u);
+            k_batch_copy<<<g, 256, 0, s>>>(n, b, D.d_nodeInst, W.accepted, W.Dt, W.D);
+            for (int i = 0; i < nInst; ++i) if (acc[i]) nd[i] = ndz[i];
+            std::fill(acc.begin(), acc.end(), 0);
+        }
+        for (int i = 0; i < nInst; ++i) {
+            res[i].initial_defect = nd[i];
+            nd0[i] = ndz[i];
+        }
+    } else {
+        for (int i = 0; i < nInst; ++i) res[i].initial_defect = nd0[i];
+    }
     for (int i = 0; i < nInst; ++i) {
-        res[i].initial_defect = nd0[i];
-        res[i].final_defect = nd0[i];
-        if (!std::isfinite(nd0[i])) { active[i] = 0; res[i].status = NSFV1_ERR_NONFINITE; }
-        else if (nd0[i] == 0.0) { active[i] = 0; res[i].status = NSFV1_OK; }
+        res[i].final_defect = nd[i];
+        if (!std::isfinite(nd[i]) || !std::isfinite(nd0[i])) { active[i] = 0; res[i].status = NSFV1_ERR_NONFINITE; }
+        else if (nd[i] == 0.0) { active[i] = 0; res[i].status = NSFV1_OK; }
     }
     for (int it = 0; it < p.max_iter; ++it) {
         int nAct = 0;
