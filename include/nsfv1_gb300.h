@@ -227,6 +227,10 @@ typedef struct {
                          /*    defect of the zero iterate (Dirichlet values, 0 elsewhere)             */
     int zero_fallback;   /* with defect_reference 1: an instance whose initial defect exceeds the     */
                          /*    zero iterate's restarts from the zero iterate                          */
+    double forcing_max;  /* > 0: Eisenstat-Walker linear tolerance per instance and step, within     */
+                         /*    [p->lin_rtol, forcing_max]; 0: p->lin_rtol throughout                   */
+    int graph;           /* 1: each step's fixed device work (Jacobians on all levels, block         */
+                         /*    inverses, the GMRES launch) replays one captured CUDA graph            */
 } nsfv1_batch_options;
 
 /* Newton on every instance at once (each to its own ||d_i|| <= rtol ||d_i,0||):
@@ -293,6 +297,13 @@ int nsfv1_mlp_predict(nsfv1_mlp* m, int64_t n_points, const float* xy, int n_slo
 int nsfv1_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* C, int splits, void* stream);
 /* the number of K chunks nsfv1_gemm_bf16 uses for K and a requested split count */
 int nsfv1_gemm_bf16_splits(int K, int splits);
+
+/* Autotuner of the batched solve: times one Newton step from u (u is not
+ * changed) for every candidate cluster size (CTAs per instance) and writes the
+ * fastest into opt->cluster_size; ms[n_candidates] (host, may be NULL)
+ * receives each candidate's time of the second of two passes. */
+int nsfv1_batch_autotune(nsfv1_disc* h, const double* u, const double* u_old, double dt, const nsfv1_newton_params* p,
+                         nsfv1_batch_options* opt, const int* candidates, int n_candidates, double* ms, void* stream);
 
 /* reference-element tables used by the kernels (for the table-consistency test):
  * edges[2*nedge], sides[4*nside] (unused slots -1), side_nco[nside], edge_face[2*nedge] */

@@ -58,7 +58,8 @@ class NewtonResult(ctypes.Structure):
 
 class BatchOptions(ctypes.Structure):
     _fields_ = [("cluster_size", c_int), ("max_clusters", c_int), ("mg_levels", c_int), ("smooth_steps", c_int),
-                ("coarse_steps", c_int), ("smooth_omega", c_double), ("defect_reference", c_int), ("zero_fallback", c_int)]
+                ("coarse_steps", c_int), ("smooth_omega", c_double), ("defect_reference", c_int), ("zero_fallback", c_int),
+                ("forcing_max", c_double), ("graph", c_int)]
 
 
 class MlpConfig(ctypes.Structure):
@@ -118,6 +119,8 @@ _SIGS = {
     "nsfv1_set_instance_grids": (c_int, [c_void_p, c_void_p]),
     "nsfv1_newton_solve_batched": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(BatchOptions),
                                            c_void_p, c_void_p]),
+    "nsfv1_batch_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(BatchOptions), c_void_p,
+                                     c_int, c_void_p, c_void_p]),
     "nsfv1_ref_tables": (c_int, [c_int, POINTER(c_int), POINTER(c_int), c_void_p, POINTER(c_int), c_void_p, c_void_p, c_void_p]),
     "nsfv1_mlp_create": (c_int, [POINTER(MlpConfig), POINTER(c_void_p)]),
     "nsfv1_mlp_destroy": (None, [c_void_p]),

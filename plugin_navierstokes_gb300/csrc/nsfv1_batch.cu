@@ -76,6 +76,8 @@ struct GmresBatchArgs {
     double* relresOut;
     VT* q;                     // extra vector [nTot] (V y before the final preconditioning)
     MgArgs<VT> mg;
+    const int* nQueueDev;      // if set: queue length read from device memory (graph replays)
+    const double* rtolInst;    // if set: per-instance relative tolerance (adaptive forcing)
 };
 
 // warp-level part of a reduction: the warp sum of v goes to wred[warp][k]
@@ -103,6 +105,7 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
     const int ctid = crank * kGT + tid;
     const int cth = csize * kGT;
     const int m = A.m;
+    const int nQueue = A.nQueueDev ? *A.nQueueDev : A.nQueue;
 
     // sum over the cluster of K values that each thread deposited in wred[warp][k]
     auto cluster_sum = [&](int K) {
@@ -127,8 +130,9 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
         cl.sync();
         const int item = *cl.map_shared_rank(&s_item, 0);
         cl.sync();
-        if (item >= A.nQueue) break;
+        if (item >= nQueue) break;
         const int inst = A.queue[item];
+        const double rtol = A.rtolInst ? A.rtolInst[inst] : A.rtol;
         const int64_t node0 = A.instNode0[inst], nNode = A.instNode0[inst + 1] - node0;
         const int64_t o = node0 * b, n = nNode * b;
         VT* __restrict__ x = A.x + o;
@@ -391,7 +395,7 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                     }
                     cl.sync();
                     relres = red[kMaxM + 1];
-                    if (!(relres >= A.rtol) || hn == 0.0) { ++j; done = true; break; }   // converged (or NaN: stop)
+                    if (!(relres >= rtol) || hn == 0.0) { ++j; done = true; break; }   // converged (or NaN: stop)
                 }
                 // y = H^-1 g ; x += Dinv (V y)
                 if (tid == 0) {
@@ -421,7 +425,7 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                 cl.sync();
                 beta = sqrt(norm2(v0));
                 relres = beta / beta0;
-                if (!(relres >= A.rtol) || beta == 0.0) break;
+                if (!(relres >= rtol) || beta == 0.0) break;
             }
         }
         if (crank == 0 && tid == 0) { A.itersOut[inst] = total; A.relresOut[inst] = relres; }
@@ -542,12 +546,13 @@ struct BatchWs {
     int64_t n = 0;
     double *D = nullptr, *Dt = nullptr, *Ut = nullptr, *nrm = nullptr, *lambda = nullptr, *relres = nullptr;
     void *J = nullptr, *Dinv = nullptr, *V = nullptr, *t = nullptr, *x = nullptr, *q = nullptr, *s = nullptr;
-    int32_t *queue = nullptr, *head = nullptr, *pending = nullptr, *accepted = nullptr, *iters = nullptr;
+    int32_t *queue = nullptr, *head = nullptr, *pending = nullptr, *accepted = nullptr, *iters = nullptr, *nQueue = nullptr;
+    double* rtolInst = nullptr;
     ~BatchWs() { release(); }
     void release() {
         auto f = [](auto*& p) { if (p) cudaFree((void*)p); p = nullptr; };
         f(D); f(Dt); f(Ut); f(nrm); f(lambda); f(relres); f(J); f(Dinv); f(V); f(t); f(x); f(q); f(s);
-        f(queue); f(head); f(pending); f(accepted); f(iters);
+        f(queue); f(head); f(pending); f(accepted); f(iters); f(nQueue); f(rtolInst);
         prec = -1;
     }
 };
@@ -589,7 +594,21 @@ struct BatchState {
     std::vector<Level> levels;     // levels[0] unused (the handle's own mesh); levels[l], l >= 1
     uint8_t* d_mask0 = nullptr;    // Dirichlet mask of the fine level
     int32_t* d_cells = nullptr;    // [nInst] cells per side
-    ~BatchState() { clear_levels(); }
+    // CUDA graph of one Newton step's fixed device work (Jacobians, block inverses, GMRES launch)
+    cudaStream_t gs = nullptr;
+    cudaEvent_t evIn = nullptr, evOut = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    ~BatchState() {
+        clear_levels();
+        drop_graph();
+        if (evIn) cudaEventDestroy(evIn);
+        if (evOut) cudaEventDestroy(evOut);
+        if (gs) cudaStreamDestroy(gs);
+    }
+    void drop_graph() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
     void clear_levels() {
         for (auto& L : levels) L.release();
         levels.clear();
@@ -604,6 +623,21 @@ BatchState* batch_state(Disc& D) {
     return static_cast<BatchState*>(D.batch);
 }
 
+// Eisenstat-Walker forcing term ("choice 2", gamma 0.9, alpha 2) with the usual
+// safeguards: no sharp decrease while the previous term was large, at most
+// etaMax, at least etaMin, and no oversolving below half the remaining distance
+// to the Newton target.
+double ew_forcing(double nd, double ndPrev, double etaPrev, double etaMin, double etaMax, double target) {
+    const double gamma = 0.9;
+    double eta = gamma * (nd / ndPrev) * (nd / ndPrev);
+    const double keep = gamma * etaPrev * etaPrev;
+    if (keep > 0.1) eta = std::max(eta, keep);
+    eta = std::min(eta, etaMax);
+    eta = std::max(eta, 0.5 * target / nd);
+    eta = std::min(eta, etaMax);
+    return std::max(eta, etaMin);
+}
+
 template <typename VT>
 int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsfv1_newton_params& p, const nsfv1_batch_options& opt,
                    nsfv1_newton_result* res, cudaStream_t s) {
@@ -612,7 +646,9 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
     const int64_t n = D.nNodes * b;
     const int prec = std::is_same<VT, double>::value ? NSFV1_F64 : NSFV1_F32;
     const int m = std::min(std::max(p.gmres_restart, 2), kMaxM);
-    BatchWs& W = batch_state(D)->ws;
+    BatchState* BS = batch_state(D);
+    BatchWs& W = BS->ws;
+    BS->drop_graph();
     if (W.prec != prec || W.n != n || W.m != m) {
         W.release();
         const size_t vt = sizeof(VT);
@@ -620,8 +656,8 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
         if (!al(W.D, n * 8) || !al(W.Dt, n * 8) || !al(W.Ut, n * 8) || !al(W.nrm, nInst * 8) || !al(W.lambda, nInst * 8) ||
             !al(W.relres, nInst * 8) || !al(W.J, D.colIdx.size() * b * b * vt) || !al(W.Dinv, (size_t)D.nNodes * b * b * vt) ||
             !al(W.V, (size_t)(m + 1) * n * vt) || !al(W.t, n * vt) || !al(W.x, n * vt) || !al(W.q, n * vt) || !al(W.s, n * vt) ||
-            !al(W.queue, nInst * 4) ||
-            !al(W.head, 4) || !al(W.pending, nInst * 4) || !al(W.accepted, nInst * 4) || !al(W.iters, nInst * 4))
+            !al(W.queue, nInst * 4) || !al(W.head, 4) || !al(W.nQueue, 4) || !al(W.rtolInst, nInst * 8) ||
+            !al(W.pending, nInst * 4) || !al(W.accepted, nInst * 4) || !al(W.iters, nInst * 4))
             return D.status;
         W.prec = prec; W.n = n; W.m = m;
     }
@@ -629,9 +665,34 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
     int nClusters = (b == 4) ? max_clusters<VT, 4>(clusterSize) : max_clusters<VT, 3>(clusterSize);
     if (nClusters <= 0) { D.fail(NSFV1_ERR_ARGUMENT, "batched solve: cluster size not launchable"); return D.status; }
     if (opt.max_clusters > 0) nClusters = std::min(nClusters, opt.max_clusters);
+    nClusters = std::min(nClusters, nInst);
+    const bool useMG = opt.mg_levels != 0 && BS->levels.size() > 1;
+    const bool adaptive = opt.forcing_max > 0.0;
+    const bool useGraph = opt.graph != 0;
+
+    // coarse-level buffers of this precision (before any graph capture)
+    if (useMG) {
+        for (size_t l = 1; l < BS->levels.size(); ++l) {
+            Level& L = BS->levels[l];
+            if (L.prec == prec) continue;
+            Disc& C = *L.disc;
+            const int64_t nc = C.nNodes;
+            auto f = [](auto*& q) { if (q) cudaFree((void*)q); q = nullptr; };
+            f(L.J); f(L.Dinv); f(L.x); f(L.r); f(L.s);
+            const size_t vt = sizeof(VT);
+            if (!D.cuda_ok(cudaMalloc(&L.J, C.colIdx.size() * b * b * vt), "level J") ||
+                !D.cuda_ok(cudaMalloc(&L.Dinv, (size_t)nc * b * b * vt), "level Dinv") ||
+                !D.cuda_ok(cudaMalloc(&L.x, (size_t)nc * b * vt), "level x") ||
+                !D.cuda_ok(cudaMalloc(&L.r, (size_t)nc * b * vt), "level r") ||
+                !D.cuda_ok(cudaMalloc(&L.s, (size_t)nc * b * vt), "level s"))
+                return D.status;
+            L.prec = prec;
+        }
+    }
 
     std::vector<int32_t> active(nInst, 1), pend(nInst, 0), acc(nInst, 0), iters(nInst, 0);
     std::vector<double> nd0(nInst, 0.0), nd(nInst, 0.0), ndt(nInst, 0.0), lam(nInst, 1.0), rr(nInst, 0.0);
+    std::vector<double> eta(nInst, adaptive ? opt.forcing_max : p.lin_rtol), ndPrev(nInst, 0.0);
     std::vector<int64_t> size(nInst);
     for (int i = 0; i < nInst; ++i) size[i] = D.instNode0[i + 1] - D.instNode0[i];
     for (int i = 0; i < nInst; ++i) { res[i] = nsfv1_newton_result{}; res[i].status = NSFV1_ERR_NOT_CONVERGED; }
@@ -645,6 +706,74 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
         if (!D.cuda_ok(cudaStreamSynchronize(s), "norms")) return false;
         for (auto& x : out) x = std::sqrt(x);
         return true;
+    };
+
+    // GMRES arguments (fixed for the whole solve: every pointer stays put)
+    GmresBatchArgs<VT> ga{W.queue, 0, W.head, D.d_instNode0, D.d_rowPtr, D.d_colIdx, (const VT*)W.J, (const VT*)W.Dinv,
+                          W.D, (VT*)W.x, (VT*)W.V, (VT*)W.t, n, m, p.lin_rtol, p.lin_max_iter, W.iters, W.relres, (VT*)W.q, {},
+                          W.nQueue, W.rtolInst};
+    ga.mg.nLevels = 0;
+    if (useMG) {
+        ga.mg.nLevels = (int)BS->levels.size();
+        ga.mg.cells0 = BS->d_cells;
+        ga.mg.nu = opt.smooth_steps > 0 ? opt.smooth_steps : 2;
+        ga.mg.nuCoarse = opt.coarse_steps > 0 ? opt.coarse_steps : 20;
+        ga.mg.omega = opt.smooth_omega > 0.0 ? opt.smooth_omega : 0.7;
+        ga.mg.lv[0] = MgLevel<VT>{D.d_rowPtr, D.d_colIdx, (const VT*)W.J, (const VT*)W.Dinv, D.d_instNode0, BS->d_mask0,
+                                  (VT*)W.t, nullptr, (VT*)W.s};
+        for (size_t l = 1; l < BS->levels.size(); ++l) {
+            Level& L = BS->levels[l];
+            ga.mg.lv[l] = MgLevel<VT>{L.disc->d_rowPtr, L.disc->d_colIdx, (const VT*)L.J, (const VT*)L.Dinv, L.d_node0, L.d_mask,
+                                      (VT*)L.x, (VT*)L.r, (VT*)L.s};
+        }
+    }
+
+    // the fixed device work of one Newton step, enqueued on stream q: Jacobians of
+    // the active instances on every level, inverted diagonal blocks, one GMRES launch
+    auto enqueue_step = [&](cudaStream_t q) -> bool {
+        if (!D.assemble_jacobian(u, u_old, dt, W.J, prec, q, false)) return false;
+        cudaMemsetAsync(D.d_err, 0, sizeof(int), q);
+        if (b == 4) k_block_inv_active<VT, 4><<<(int)((D.nNodes + 127) / 128), 128, 0, q>>>(D.nNodes, D.d_diagPos, D.d_nodeInst, D.d_instActive, (VT*)W.J, (VT*)W.Dinv, D.d_err);
+        else k_block_inv_active<VT, 3><<<(int)((D.nNodes + 127) / 128), 128, 0, q>>>(D.nNodes, D.d_diagPos, D.d_nodeInst, D.d_instActive, (VT*)W.J, (VT*)W.Dinv, D.d_err);
+        if (useMG) {
+            const double* uf = u;
+            for (size_t l = 1; l < BS->levels.size(); ++l) {
+                Level& L = BS->levels[l];
+                Disc& C = *L.disc;
+                const int64_t nc = C.nNodes;
+                k_inject<<<(int)((nc * b + 255) / 256), 256, 0, q>>>(nc, b, L.d_inj, uf, L.d_u);
+                if (!C.assemble_jacobian(L.d_u, nullptr, dt, L.J, prec, q, false)) { D.fail(C.status, C.lastError); return false; }
+                if (b == 4) k_block_inv_all<VT, 4><<<(int)((nc + 127) / 128), 128, 0, q>>>(nc, C.d_diagPos, (VT*)L.J, (VT*)L.Dinv, D.d_err);
+                else k_block_inv_all<VT, 3><<<(int)((nc + 127) / 128), 128, 0, q>>>(nc, C.d_diagPos, (VT*)L.J, (VT*)L.Dinv, D.d_err);
+                uf = L.d_u;
+            }
+        }
+        cudaMemsetAsync(W.head, 0, 4, q);
+        cudaError_t le = (b == 4) ? launch_gmres_batch<VT, 4>(ga, clusterSize, nClusters, q) : launch_gmres_batch<VT, 3>(ga, clusterSize, nClusters, q);
+        return D.cuda_ok(le, "batched GMRES launch");
+    };
+    auto run_step = [&]() -> bool {
+        if (!useGraph) return enqueue_step(s);
+        if (!BS->gs) {
+            if (!D.cuda_ok(cudaStreamCreateWithFlags(&BS->gs, cudaStreamNonBlocking), "graph stream") ||
+                !D.cuda_ok(cudaEventCreateWithFlags(&BS->evIn, cudaEventDisableTiming), "graph event") ||
+                !D.cuda_ok(cudaEventCreateWithFlags(&BS->evOut, cudaEventDisableTiming), "graph event"))
+                return false;
+        }
+        if (!BS->graph) {
+            cudaGraph_t g = nullptr;
+            if (!D.cuda_ok(cudaStreamBeginCapture(BS->gs, cudaStreamCaptureModeRelaxed), "graph capture")) return false;
+            const bool ok = enqueue_step(BS->gs);
+            const cudaError_t ce = cudaStreamEndCapture(BS->gs, &g);
+            if (!ok) { if (g) cudaGraphDestroy(g); return false; }
+            if (!D.cuda_ok(ce, "graph capture")) return false;
+            const cudaError_t ie = cudaGraphInstantiate(&BS->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (!D.cuda_ok(ie, "graph instantiate")) { BS->graph = nullptr; return false; }
+        }
+        return D.cuda_ok(cudaEventRecord(BS->evIn, s), "graph event") && D.cuda_ok(cudaStreamWaitEvent(BS->gs, BS->evIn, 0), "graph event") &&
+               D.cuda_ok(cudaGraphLaunch(BS->graph, BS->gs), "graph launch") && D.cuda_ok(cudaEventRecord(BS->evOut, BS->gs), "graph event") &&
+               D.cuda_ok(cudaStreamWaitEvent(s, BS->evOut, 0), "graph event");
     };
 
     const int g = (int)((n + 255) / 256);
@@ -689,67 +818,25 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
             ++nAct;
         }
         if (nAct == 0) break;
-        D.instSkip = true;
-        if (!upload_flags(active, D.d_instActive)) return D.status;
-        if (!D.assemble_jacobian(u, u_old, dt, W.J, prec, s, false)) return D.status;
-        cudaMemsetAsync(D.d_err, 0, sizeof(int), s);
-        if (b == 4) k_block_inv_active<VT, 4><<<(int)((D.nNodes + 127) / 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, D.d_nodeInst, D.d_instActive, (VT*)W.J, (VT*)W.Dinv, D.d_err);
-        else k_block_inv_active<VT, 3><<<(int)((D.nNodes + 127) / 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, D.d_nodeInst, D.d_instActive, (VT*)W.J, (VT*)W.Dinv, D.d_err);
-        // coarse levels: inject the state, assemble, invert the diagonal blocks
-        BatchState* BS = batch_state(D);
-        const bool useMG = opt.mg_levels != 0 && BS->levels.size() > 1;
-        if (useMG) {
-            const double* uf = u;
-            for (size_t l = 1; l < BS->levels.size(); ++l) {
-                Level& L = BS->levels[l];
-                Disc& C = *L.disc;
-                const int64_t nc = C.nNodes;
-                if (L.prec != prec) {
-                    auto f = [](auto*& p) { if (p) cudaFree((void*)p); p = nullptr; };
-                    f(L.J); f(L.Dinv); f(L.x); f(L.r); f(L.s);
-                    const size_t vt = sizeof(VT);
-                    if (!D.cuda_ok(cudaMalloc(&L.J, C.colIdx.size() * b * b * vt), "level J") ||
-                        !D.cuda_ok(cudaMalloc(&L.Dinv, (size_t)nc * b * b * vt), "level Dinv") ||
-                        !D.cuda_ok(cudaMalloc(&L.x, (size_t)nc * b * vt), "level x") ||
-                        !D.cuda_ok(cudaMalloc(&L.r, (size_t)nc * b * vt), "level r") ||
-                        !D.cuda_ok(cudaMalloc(&L.s, (size_t)nc * b * vt), "level s"))
-                        return D.status;
-                    L.prec = prec;
-                }
-                k_inject<<<(int)((nc * b + 255) / 256), 256, 0, s>>>(nc, b, L.d_inj, uf, L.d_u);
-                if (!C.assemble_jacobian(L.d_u, nullptr, dt, L.J, prec, s, false)) { D.fail(C.status, C.lastError); return D.status; }
-                cudaMemsetAsync(C.d_err, 0, sizeof(int), s);
-                if (b == 4) k_block_inv_all<VT, 4><<<(int)((nc + 127) / 128), 128, 0, s>>>(nc, C.d_diagPos, (VT*)L.J, (VT*)L.Dinv, D.d_err);
-                else k_block_inv_all<VT, 3><<<(int)((nc + 127) / 128), 128, 0, s>>>(nc, C.d_diagPos, (VT*)L.J, (VT*)L.Dinv, D.d_err);
-                uf = L.d_u;
-            }
+        // linear tolerances of this step
+        for (int i = 0; i < nInst; ++i) {
+            if (!active[i]) continue;
+            if (adaptive && it > 0) eta[i] = ew_forcing(nd[i], ndPrev[i], eta[i], p.lin_rtol, opt.forcing_max, std::max(p.rtol * nd0[i], p.atol));
+            else if (!adaptive) eta[i] = p.lin_rtol;
+            ndPrev[i] = nd[i];
         }
         // queue: active instances, largest first
         std::vector<int32_t> q;
         for (int i = 0; i < nInst; ++i) if (active[i]) q.push_back(i);
         std::stable_sort(q.begin(), q.end(), [&](int a, int c) { return size[a] > size[c]; });
-        if (!D.cuda_ok(cudaMemcpyAsync(W.queue, q.data(), q.size() * 4, cudaMemcpyHostToDevice, s), "queue")) return D.status;
-        cudaMemsetAsync(W.head, 0, 4, s);
-        GmresBatchArgs<VT> a{W.queue, (int)q.size(), W.head, D.d_instNode0, D.d_rowPtr, D.d_colIdx, (const VT*)W.J, (const VT*)W.Dinv,
-                             W.D, (VT*)W.x, (VT*)W.V, (VT*)W.t, n, m, p.lin_rtol, p.lin_max_iter, W.iters, W.relres, (VT*)W.q, {}};
-        a.mg.nLevels = 0;
-        if (useMG) {
-            a.mg.nLevels = (int)BS->levels.size();
-            a.mg.cells0 = BS->d_cells;
-            a.mg.nu = opt.smooth_steps > 0 ? opt.smooth_steps : 2;
-            a.mg.nuCoarse = opt.coarse_steps > 0 ? opt.coarse_steps : 20;
-            a.mg.omega = opt.smooth_omega > 0.0 ? opt.smooth_omega : 0.7;
-            a.mg.lv[0] = MgLevel<VT>{D.d_rowPtr, D.d_colIdx, (const VT*)W.J, (const VT*)W.Dinv, D.d_instNode0, BS->d_mask0,
-                                     (VT*)W.t, nullptr, (VT*)W.s};
-            for (size_t l = 1; l < BS->levels.size(); ++l) {
-                Level& L = BS->levels[l];
-                a.mg.lv[l] = MgLevel<VT>{L.disc->d_rowPtr, L.disc->d_colIdx, (const VT*)L.J, (const VT*)L.Dinv, L.d_node0, L.d_mask,
-                                         (VT*)L.x, (VT*)L.r, (VT*)L.s};
-            }
-        }
-        cudaError_t le = (b == 4) ? launch_gmres_batch<VT, 4>(a, clusterSize, std::min(nClusters, (int)q.size()), s)
-                                  : launch_gmres_batch<VT, 3>(a, clusterSize, std::min(nClusters, (int)q.size()), s);
-        if (!D.cuda_ok(le, "batched GMRES launch")) return D.status;
+        const int nq = (int)q.size();
+        D.instSkip = true;
+        if (!upload_flags(active, D.d_instActive) ||
+            !D.cuda_ok(cudaMemcpyAsync(W.queue, q.data(), q.size() * 4, cudaMemcpyHostToDevice, s), "queue") ||
+            !D.cuda_ok(cudaMemcpyAsync(W.nQueue, &nq, 4, cudaMemcpyHostToDevice, s), "queue") ||
+            !D.cuda_ok(cudaMemcpyAsync(W.rtolInst, eta.data(), nInst * 8, cudaMemcpyHostToDevice, s), "tolerances"))
+            return D.status;
+        if (!run_step()) return D.status;
         int herr = 0;
         cudaMemcpyAsync(&herr, D.d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(iters.data(), W.iters, nInst * 4, cudaMemcpyDeviceToHost, s);
@@ -990,6 +1077,62 @@ int nsfv1_set_instance_grids(nsfv1_disc* h, const int32_t* cells) {
         for (size_t k = 0; k < dirRow.size(); ++k) { nDir[dirRow[k]] = 1; nDirVal[dirRow[k]] = dirVal[k]; }
         fNode0 = cNode0; fCells = nCells; fDir = nDir; fDirVal = nDirVal;
     }
+    return NSFV1_OK;
+}
+
+int nsfv1_batch_autotune(nsfv1_disc* h, const double* u, const double* u_old, double dt, const nsfv1_newton_params* p,
+                         nsfv1_batch_options* opt, const int* candidates, int n_candidates, double* ms, void* stream) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (!D->hasMesh || D->nInst <= 0) { D->fail(NSFV1_ERR_STATE, "batch_autotune: no mesh or no instances"); return D->status; }
+    if (!u || !p || !opt || !candidates || n_candidates <= 0) { D->fail(NSFV1_ERR_ARGUMENT, "batch_autotune: null argument"); return D->status; }
+    for (int c = 0; c < n_candidates; ++c)
+        if (candidates[c] < 1 || candidates[c] > 16) { D->fail(NSFV1_ERR_ARGUMENT, "batch_autotune: cluster sizes must be 1..16"); return D->status; }
+    if (p->jacobian_prec != NSFV1_F64 && p->jacobian_prec != NSFV1_F32) { D->fail(NSFV1_ERR_ARGUMENT, "batch_autotune: bad precision"); return D->status; }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t n = D->nNodes * (D->dim + 1);
+    double* tu = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (!D->cuda_ok(cudaMalloc(&tu, n * 8), "autotune") || !D->cuda_ok(cudaEventCreate(&e0), "autotune") ||
+        !D->cuda_ok(cudaEventCreate(&e1), "autotune")) {
+        if (tu) cudaFree(tu);
+        return D->status;
+    }
+    nsfv1_newton_params q = *p;
+    q.max_iter = 1;
+    std::vector<nsfv1_newton_result> r(D->nInst);
+    std::vector<double> t(n_candidates, 0.0);
+    int st = NSFV1_OK;
+    for (int pass = 0; pass < 2 && st == NSFV1_OK; ++pass) {
+        for (int c = 0; c < n_candidates && st == NSFV1_OK; ++c) {
+            nsfv1_batch_options o = *opt;
+            o.cluster_size = candidates[c];
+            cudaMemcpyAsync(tu, u, n * 8, cudaMemcpyDeviceToDevice, s);
+            cudaEventRecord(e0, s);
+            const int rs = q.jacobian_prec == NSFV1_F64 ? batched_newton<double>(*D, tu, u_old, dt, q, o, r.data(), s)
+                                                        : batched_newton<float>(*D, tu, u_old, dt, q, o, r.data(), s);
+            cudaEventRecord(e1, s);
+            if (rs == NSFV1_ERR_CUDA || rs == NSFV1_ERR_ARGUMENT || rs == NSFV1_ERR_STATE || rs == NSFV1_ERR_GEOMETRY) { st = rs; break; }
+            float msec = 0.f;
+            if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&msec, e0, e1) != cudaSuccess) {
+                D->fail(NSFV1_ERR_CUDA, "autotune timing");
+                st = NSFV1_ERR_CUDA;
+                break;
+            }
+            t[c] = msec;
+        }
+    }
+    cudaFree(tu);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != NSFV1_OK) return st;
+    int best = 0;
+    for (int c = 1; c < n_candidates; ++c) if (t[c] < t[best]) best = c;
+    opt->cluster_size = candidates[best];
+    if (ms) for (int c = 0; c < n_candidates; ++c) ms[c] = t[c];
+    D->status = NSFV1_OK;
+    D->lastError.clear();
     return NSFV1_OK;
 }
 

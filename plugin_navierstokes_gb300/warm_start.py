@@ -11,6 +11,10 @@ iterate any instance whose predicted iterate has a larger defect than zero.
 from __future__ import annotations
 
 import ctypes
+import json
+import os
+from collections import Counter
+from pathlib import Path
 
 import numpy as np
 
@@ -132,3 +136,117 @@ def gemm_bf16(A, B, splits: int = 1, stream=None):
     if st != _capi.OK:
         raise NSFV1Error(st, "nsfv1_gemm_bf16 failed")
     return C
+
+
+# ---- batched cavities with a learned initial iterate -------------------------
+
+class CavityBatch:
+    """Independent lid-driven cavities (structured quads, full upwind + FLOW, as
+    the batched workload) set up on one NavierStokesFV1 handle: per-element
+    viscosity nu = lid / Re, instance ranges, multigrid hierarchy."""
+
+    def __init__(self, N, Re, lid, upwind: str = "full", stabilization: str = "flow"):
+        import torch
+
+        from . import mesh
+        from .navier_stokes_fv1 import NavierStokesFV1
+
+        self.N = np.asarray(N, np.int32)
+        self.Re = np.asarray(Re, np.float64)
+        self.lid = np.asarray(lid, np.float64)
+        B = mesh.cavity_batch(self.N, self.Re, self.lid)
+        d = NavierStokesFV1("u,v,p", "Inner")
+        d.set_kinematic_viscosity(1.0)
+        d.set_upwind(upwind)
+        d.set_stabilization(stabilization)
+        d.set_mesh(B["elem_type"], B["coords"], B["conn"])
+        d.set_elem_viscosity(B["nu_elem"])
+        d.set_instances(B["node_offsets"])
+        d.set_dirichlet(B["dofs"], B["values"])
+        d.set_instance_grids(self.N)
+        self.disc = d
+        self.node_offsets = B["node_offsets"]
+        self.n_nodes = int(B["coords"].shape[0])
+        self.xy = torch.from_numpy(B["coords"].astype(np.float32)).cuda()
+        self.cond = np.stack([condition(r, l) for r, l in zip(self.Re, self.lid)])
+        self.cluster_size = 8
+
+    def autotune(self, jacobian_prec: str = "f32", candidates=(2, 4, 8, 16), cache_file: str | None = None, **kw) -> int:
+        """Picks the cluster size (CTAs per instance) of this batch by timing one
+        Newton step per candidate (nsfv1_batch_autotune); the choice is cached in
+        a JSON file keyed by device, precision and the multiset of mesh sizes
+        (default ~/.cache/nsfv1_gb300/autotune.json, or $NSFV1_AUTOTUNE_CACHE)."""
+        import torch
+
+        path = Path(cache_file or os.environ.get("NSFV1_AUTOTUNE_CACHE", Path.home() / ".cache" / "nsfv1_gb300" / "autotune.json"))
+        key = "|".join([torch.cuda.get_device_name(), jacobian_prec, ",".join(map(str, candidates)),
+                        ",".join(f"{n}x{c}" for n, c in sorted(Counter(self.N.tolist()).items()))])
+        cache = {}
+        if path.exists():
+            try:
+                cache = json.loads(path.read_text())
+            except (OSError, ValueError):
+                cache = {}
+        if key in cache:
+            self.cluster_size = int(cache[key]["cluster_size"])
+            return self.cluster_size
+        best, ms = self.disc.batch_autotune(self.zeros(), candidates=candidates, jacobian_prec=jacobian_prec, **kw)
+        self.cluster_size = best
+        cache[key] = {"cluster_size": best, "ms": dict(zip(map(str, candidates), ms))}
+        try:
+            path.parent.mkdir(parents=True, exist_ok=True)
+            path.write_text(json.dumps(cache, indent=1))
+        except OSError:
+            pass
+        return best
+
+    @property
+    def n_inst(self) -> int:
+        return int(self.N.size)
+
+    def zeros(self):
+        import torch
+
+        return torch.zeros(self.n_nodes * 3, dtype=torch.float64, device="cuda")
+
+    def predict(self, model: "CoordinateMLP", u=None):
+        """The network's initial iterate of every instance (FP64 device vector)."""
+        u = self.zeros() if u is None else u
+        model.predict(self.xy, self.node_offsets, self.cond, self.lid.astype(np.float32), u)
+        return u
+
+    def solve(self, u, jacobian_prec: str = "f32", rtol: float = 1e-8, defect_reference: str = "zero",
+              zero_fallback: bool = False, **kw):
+        """Batched Newton from u (in place); returns the per-instance results."""
+        opts = dict(lin_rtol=1e-3, lin_max_iter=400, max_iter=80, cluster_size=self.cluster_size, raise_on_error=False)
+        opts.update(kw)
+        return self.disc.newton_solve_batched(u, rtol=rtol, jacobian_prec=jacobian_prec, defect_reference=defect_reference,
+                                              zero_fallback=zero_fallback, **opts)
+
+
+def generate_training_set(Re, lid, N: int = 128, batch: int = 256, jacobian_prec: str = "f32", **solve_kw):
+    """Solves cavities of one mesh size (N x N cells) in batches with the batched
+    Newton and returns (coords [n_nodes, 2], targets [n, n_nodes, 3], cond [n, 2],
+    results) on the device, targets normalised as nsfv1_mlp_targets."""
+    import torch
+
+    Re = np.asarray(Re, np.float64)
+    lid = np.asarray(lid, np.float64)
+    n = Re.size
+    nn = (N + 1) ** 2
+    targets = torch.empty((n, nn, 3), dtype=torch.float32, device="cuda")
+    results = []
+    coords = None
+    for s in range(0, n, batch):
+        e = min(n, s + batch)
+        cb = CavityBatch(np.full(e - s, N), Re[s:e], lid[s:e])
+        u = cb.zeros()
+        results += cb.solve(u, jacobian_prec=jacobian_prec, **solve_kw)
+        lt = torch.from_numpy(lid[s:e]).cuda()
+        targets_from_solutions(u, lt, nn, targets[s:e])
+        if coords is None:
+            coords = cb.xy[:nn].clone()
+        del cb
+    cond = torch.from_numpy(np.stack([condition(r, l) for r, l in zip(Re, lid)])).cuda()
+    torch.cuda.synchronize()
+    return coords, targets, cond, results

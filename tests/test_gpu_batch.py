@@ -92,3 +92,81 @@ def test_multigrid_batched_newton(cuda, prec):
     # the V-cycle cuts the Krylov work by a large factor on the 48 x 48, Re 800 instance
     per_step_mg = res[3]["linear_iterations"] / max(res[3]["iterations"], 1)
     assert per_step_mg < 150, res[3]
+
+
+def test_graph_replay_matches_direct_launches(cuda):
+    """The captured per-step CUDA graph gives bit-identical iterates and counts."""
+    import torch
+    sizes = [16, 24, 32]
+    d, B = _batch(sizes, [100.0, 500.0, 1000.0], [1.0, 0.7, 1.8])
+    d.set_instance_grids(sizes)
+    out = []
+    for graph in (False, True):
+        u = torch.zeros(B["coords"].shape[0] * 3, dtype=torch.float64, device=cuda)
+        r = d.newton_solve_batched(u, rtol=1e-8, jacobian_prec="f32", graph=graph, max_iter=80)
+        out.append((u, r))
+    assert torch.equal(out[0][0], out[1][0])
+    assert [x["linear_iterations"] for x in out[0][1]] == [x["linear_iterations"] for x in out[1][1]]
+
+
+def test_adaptive_forcing_meets_the_oracle_target(cuda):
+    """Eisenstat-Walker tolerances: every instance still reaches the FP64 oracle
+    defect target, with fewer Krylov iterations than the fixed 1e-3 tolerance."""
+    import torch
+    sizes = [16, 32, 24]
+    Re, lid = [200.0, 1000.0, 50.0], [1.0, 1.5, 2.0]
+    d, B = _batch(sizes, Re, lid)
+    d.set_instance_grids(sizes)
+    lin = []
+    for fmax in (0.0, 0.3):
+        u = torch.zeros(B["coords"].shape[0] * 3, dtype=torch.float64, device=cuda)
+        res = d.newton_solve_batched(u, rtol=1e-8, lin_rtol=1e-3, jacobian_prec="f32", forcing_max=fmax, max_iter=100)
+        U = u.cpu().numpy()
+        offs = B["node_offsets"]
+        for i, (N, re, u0) in enumerate(zip(sizes, Re, lid)):
+            assert res[i]["status"] == 0, (fmax, i, res[i])
+            roid, X, C = mesh.structured_quads(N)
+            dofs, vals = mesh.cavity_dirichlet(X, u0)
+            o = oracle.Oracle(2); o.set_kinematic_viscosity(u0 / re); o.set_upwind("full"); o.set_stabilization("flow")
+            o.set_mesh(roid, X, C); o.set_dirichlet(dofs, vals)
+            D, _ = o.assemble(U[offs[i] * 3:offs[i + 1] * 3], jacobian=False)
+            assert np.linalg.norm(D) <= 1.01e-8 * res[i]["initial_defect"], (fmax, i, res[i])
+        lin.append(sum(r["linear_iterations"] for r in res))
+    assert lin[1] < lin[0], lin
+
+
+def test_zero_reference_and_fallback(cuda):
+    """defect_reference "zero": the target is relative to the zero iterate's
+    defect; with zero_fallback a worse iterate restarts from zero, a better one
+    is kept."""
+    import torch
+    sizes = [16, 16]
+    Re, lid = [100.0, 100.0], [1.0, 1.0]
+    d, B = _batch(sizes, Re, lid)
+    n = B["coords"].shape[0] * 3
+    u_ref = torch.zeros(n, dtype=torch.float64, device=cuda)
+    r0 = d.newton_solve_batched(u_ref, rtol=1e-10, jacobian_prec="f64")
+    zero_defect = r0[0]["initial_defect"]
+    # instance 0: a slightly perturbed solution (better than zero), instance 1: garbage (worse)
+    half = n // 2
+    u = u_ref.clone()
+    u[:half] += 1e-4 * torch.sin(torch.arange(half, dtype=torch.float64, device=cuda))
+    u[half:] = 50.0
+    res = d.newton_solve_batched(u, rtol=1e-8, jacobian_prec="f64", defect_reference="zero", zero_fallback=True)
+    assert res[0]["initial_defect"] < 1e-2 * zero_defect
+    assert abs(res[1]["initial_defect"] - r0[1]["initial_defect"]) <= 1e-12 * r0[1]["initial_defect"]
+    for r in res:
+        assert r["status"] == 0 and r["final_defect"] <= 1.0e-8 * zero_defect * 1.0000001
+    assert res[0]["iterations"] < res[1]["iterations"]
+
+
+def test_autotune_picks_a_candidate(cuda):
+    import torch
+    sizes = [16, 32, 24, 48]
+    d, B = _batch(sizes, [100.0, 1000.0, 300.0, 800.0], [1.0, 2.0, 0.5, 1.5])
+    d.set_instance_grids(sizes)
+    u = torch.zeros(B["coords"].shape[0] * 3, dtype=torch.float64, device=cuda)
+    best, ms = d.batch_autotune(u, candidates=(2, 4, 8))
+    assert best in (2, 4, 8) and len(ms) == 3 and all(t > 0 for t in ms)
+    assert ms[(2, 4, 8).index(best)] == min(ms)
+    assert torch.count_nonzero(u) == 0   # the iterate is untouched
