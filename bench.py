@@ -12,7 +12,22 @@ HBM (device-timed with CUDA events, L2 flushed between steps). e2e: the same
 through the C ABI with host buffers: H2D of u and D2H of the defect and the
 Jacobian values inside the timed region.
 
-python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Two more workloads print their own line (not the default run):
+--workload batched  256 lid-driven cavities, N ~ U{32,...,256}, Re ~ logU[10, 1000],
+                    lid ~ U[0.5, 2] (seed 3), full upwind + FLOW; one step = the whole
+                    batch solved by the batched Newton (FP32 Jacobian / FP64 defect,
+                    multigrid-preconditioned GMRES, one persistent launch per Newton
+                    step replayed from a CUDA graph) to ||d|| <= 1e-8 ||d(0)|| per instance.
+--workload transient  1024^2 jittered grid split into 2,097,152 triangles (seed 2), backward
+                    Euler dt 0.01 x 20 steps, nu 0.001, full upwind + FIELDS, cavity walls; each
+                    step one Newton solve to 1e-6 relative (FP32 Jacobian and block inverses,
+                    block-Jacobi BiCGStab to 1e-4 with FP64 Krylov vectors, FP64 defect /
+                    update / line search); the all-FP64 run beside it.
+--workload learned  the warm-start MLP trained on 2048 solves of 128^2 cavities (seed 4),
+                    then 256 held-out draws (seed 5); one step = the held-out batch solved
+                    from the network's iterate (FP32 Jacobian), plain FP64 from zero beside.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload assembly|batched|learned]
 """
 from __future__ import annotations
 
@@ -42,7 +57,7 @@ def workload():
 
 
 def config_dict(extra=None):
-    d = {"workload": f"FV1 defect+Jacobian assembly, {N_CELLS}^3 hexahedra (274625 nodes, b=4), "
+    d = {"workload": f"FV1 defect+Jacobian assembly, {N_CELLS}^3 hexahedra ({(N_CELLS + 1) ** 3} nodes, b=4), "
                      f"LPS upwind + FLOW, nu={NU}, solenoidal seeded state",
          "elements": N_CELLS ** 3, "nodes": (N_CELLS + 1) ** 3, "block_size": 4,
          "upwind": UPWIND, "stabilization": STAB, "l2": "flushed between timed steps (512 MiB write)"}
@@ -141,11 +156,21 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="assembly", choices=["assembly", "batched", "learned", "transient"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cells", type=int, default=64, help="assembly workload: cells per side (64 is the benchmark; smaller for profiling)")
     args = ap.parse_args()
+    global N_CELLS
+    N_CELLS = args.cells
+    if args.steps is None:
+        args.steps = 10 if args.workload == "assembly" else 3
+    if args.workload == "transient":
+        return run_transient(args)
+    if args.workload != "assembly":
+        return run_solves(args)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -295,6 +320,343 @@ def main():
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+# ---- solve workloads (batched cavities, learned warm start) ---------------------
+
+def cavity_draws(n, seed):
+    """(Re, lid) draws of the learned workload: Re ~ logU[10, 1000], lid ~ U[0.5, 2]."""
+    import numpy as np
+
+    from plugin_navierstokes_gb300 import mesh
+
+    r = mesh.uniform(seed, 2 * n).reshape(n, 2)
+    return np.exp(np.log(10.0) + r[:, 0] * (np.log(1000.0) - np.log(10.0))), 0.5 + 1.5 * r[:, 1]
+
+
+def _oracle_solves(N, Re, lid, budget_s=20.0):
+    """The oracle's serial Newton (block-Jacobi BiCGStab) on cavities of the list,
+    in order, until the time budget is spent: (solves/s, solves, seconds)."""
+    import numpy as np
+
+    import oracle
+    from plugin_navierstokes_gb300 import mesh
+
+    done, t0 = 0, time.perf_counter()
+    for n, re, u0 in zip(N, Re, lid):
+        roid, X, C = mesh.structured_quads(int(n))
+        dofs, vals = mesh.cavity_dirichlet(X, float(u0))
+        o = oracle.Oracle(2)
+        o.set_kinematic_viscosity(float(u0) / float(re))
+        o.set_upwind("full")
+        o.set_stabilization("flow")
+        o.set_mesh(roid, X, C)
+        o.set_dirichlet(dofs, vals)
+        o.newton(np.zeros(X.shape[0] * 3), rtol=1e-8, maxit=100, lin_rtol=1e-3, lin_maxit=20000)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return done / el, done, el
+
+
+def run_solves(args):
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from plugin_navierstokes_gb300 import mesh
+
+    if args.workload == "batched":
+        N, Re, lid = mesh.draw_cavity_params(256, seed=3)
+        wl = "256 lid-driven cavities, N ~ U{32,48,64,96,128,192,256}, Re ~ logU[10,1000], lid ~ U[0.5,2] (seed 3), full upwind + FLOW"
+    else:
+        Re, lid = cavity_draws(256, 5)
+        N = np.full(256, 128)
+        wl = "256 held-out lid-driven cavities on 128^2 quads, Re ~ logU[10,1000], lid ~ U[0.5,2] (seed 5), full upwind + FLOW; " \
+             "warm start trained on 2048 solves (seed 4)"
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        # bounded sample: the draws of the batch on 32^2 meshes (the smallest size of the batched workload)
+        v, k, el = _oracle_solves(np.full(len(N), 32), np.asarray(Re), np.asarray(lid), budget_s=20.0)
+        line = {"impl": "reference", "metric": "solves/s to rel defect 1e-8", "value": v, "unit": "solves/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / k, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": {"workload": wl},
+                "cpu_baseline": {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
+                                 "sample": f"first {k} (Re, lid) draws on 32^2 meshes, serial oracle Newton"},
+                "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        # instance sharding: every rank solves its own cost-balanced share
+        from plugin_navierstokes_gb300.sharding import shard_instances
+
+        mine = shard_instances((np.asarray(N) + 1) ** 2, world)[rank]
+        N, Re, lid = np.asarray(N)[mine], np.asarray(Re)[mine], np.asarray(lid)[mine]
+    from plugin_navierstokes_gb300 import build
+    from plugin_navierstokes_gb300.warm_start import CavityBatch, CoordinateMLP, generate_training_set
+
+    build.build()
+    extra = {}
+    model = None
+    if args.workload == "learned":
+        t0 = time.perf_counter()
+        tRe, tlid = cavity_draws(2048, 4)
+        coords, targets, cond, tres = generate_training_set(tRe, tlid, N=128, batch=256, cluster_size=16)
+        tgen = time.perf_counter() - t0
+        model = CoordinateMLP(max_points=65536, max_slots=64, seed=4)
+        t0 = time.perf_counter()
+        hist = model.train(coords, targets, cond, steps=6000, slots=64, points_per_slot=1024, lr=2e-3, lr_final=2e-5, seed=4)
+        torch.cuda.synchronize()
+        extra["training"] = {"solves": 2048, "converged": int(sum(r["status"] == 0 for r in tres)), "generate_s": round(tgen, 2),
+                             "train_steps": 6000, "train_s": round(time.perf_counter() - t0, 2), "final_loss": float(hist[-20:].mean())}
+        del coords, targets, cond
+    cb = CavityBatch(N, Re, lid)
+    n_inst = cb.n_inst
+    prec_main = "f32"
+    cb.autotune(prec_main)
+    cl32 = cb.cluster_size
+
+    def solve_once(prec, learned, cluster):
+        cb.cluster_size = cluster
+        u = cb.zeros()
+        if learned:
+            cb.predict(model, u)
+        res = cb.solve(u, prec, zero_fallback=learned)
+        return u, res
+
+    def timed(prec, learned, cluster, k):
+        ts, res = [], None
+        for _ in range(k):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            u, res = solve_once(prec, learned, cluster)
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return ts, res
+
+    learned = args.workload == "learned"
+    for _ in range(args.warmup):
+        solve_once(prec_main, learned, cl32)
+    if world > 1:
+        torch.distributed.barrier()
+    with ClockSampler(local) as clk:
+        ts, res = timed(prec_main, learned, cl32, args.steps)
+    sec = sum(ts) / len(ts)
+    if world > 1:
+        t = torch.tensor([sec], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        sec = float(t.item())
+    total_inst = 256
+    value = total_inst / sec
+    stats = lambda r: {"converged": int(sum(x["status"] == 0 for x in r)), "newton_its_mean": float(np.mean([x["iterations"] for x in r])),
+                       "newton_its_max": int(max(x["iterations"] for x in r)),
+                       "linear_its_mean": float(np.mean([x["linear_iterations"] for x in r]))}
+    extra["main"] = dict(stats(res), jacobian="f32", init="learned" if learned else "zero", cluster_size=cl32)
+    # plain FP64 from zero, and the ablations, on the same batch (one timed solve each after one warm-up)
+    cb.autotune("f64")
+    cl64 = cb.cluster_size
+    solve_once("f64", False, cl64)
+    t64, r64 = timed("f64", False, cl64, 1)
+    extra["plain_f64_zero"] = dict(stats(r64), solves_per_s=n_inst / t64[0], cluster_size=cl64)
+    if learned:
+        t32, r32 = timed("f32", False, cl32, 1)
+        extra["f32_zero"] = dict(stats(r32), solves_per_s=n_inst / t32[0])
+        tl64, rl64 = timed("f64", True, cl64, 1)
+        extra["learned_f64"] = dict(stats(rl64), solves_per_s=n_inst / tl64[0])
+    extra["speedup_vs_plain_f64"] = (n_inst / sec) / extra["plain_f64_zero"]["solves_per_s"]
+
+    # FP64-oracle defect of every instance's final iterate (rank 0, one solve of the main path)
+    u, res = solve_once(prec_main, learned, cl32)
+    U = u.cpu().numpy()
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle
+
+        worst = 0.0
+        offs = cb.node_offsets
+        for i in range(n_inst):
+            roid, X, C = mesh.structured_quads(int(N[i]))
+            dofs, vals = mesh.cavity_dirichlet(X, float(lid[i]))
+            o = oracle.Oracle(2)
+            o.set_kinematic_viscosity(float(lid[i]) / float(Re[i]))
+            o.set_upwind("full")
+            o.set_stabilization("flow")
+            o.set_mesh(roid, X, C)
+            o.set_dirichlet(dofs, vals)
+            D, _ = o.assemble(U[offs[i] * 3:offs[i + 1] * 3], jacobian=False, nthreads=os.cpu_count() or 1)
+            x0 = np.zeros(X.shape[0] * 3)
+            x0[dofs] = vals
+            D0, _ = o.assemble(x0, jacobian=False, nthreads=os.cpu_count() or 1)
+            worst = max(worst, float(np.linalg.norm(D) / np.linalg.norm(D0)))
+        extra["oracle_rel_defect_max"] = worst
+
+    # e2e through the public API with host buffers: H2D of the initial iterate, D2H of the solutions
+    hu0 = torch.zeros(cb.n_nodes * 3, dtype=torch.float64).pin_memory()
+    hu = torch.empty_like(hu0).pin_memory()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    cb.cluster_size = cl32
+    ud = hu0.to(dev, non_blocking=True)
+    if learned:
+        cb.predict(model, ud)
+    cb.solve(ud, prec_main, zero_fallback=learned)
+    hu.copy_(ud, non_blocking=True)
+    e1.record()
+    e1.synchronize()
+    e2e_s = e0.elapsed_time(e1) * 1e-3
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # bounded sample: the draws of the batch on 32^2 meshes (the smallest size of the batched workload)
+        k32 = np.full(len(N), 32)
+        v, k, el = _oracle_solves(k32, np.asarray(Re), np.asarray(lid), budget_s=20.0)
+        cpu = {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"first {k} (Re, lid) draws of the batch on 32^2 meshes, serial oracle Newton (block-Jacobi BiCGStab), {el:.1f} s"}
+    if rank == 0:
+        line = {"metric": "solves/s to rel defect 1e-8", "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * sec, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64 defect / f32 jacobian", "data": "synthetic (seeded cavity draws)",
+                "config": {"workload": wl, "instances": total_inst, "l2": "inputs larger than L2 (" + str(cb.n_nodes) + " nodes)", **extra},
+                "e2e": {"value": n_inst * world / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": hu0.numel() * 8,
+                        "d2h_bytes_per_step": hu.numel() * 8},
+                "roofline": None, "cpu_baseline": cpu, "gpu_launches": None, "clocks": clk.summary()}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+# Newton tolerance of each backward-Euler step: full upwinding makes the defect
+# only piecewise smooth, and the Newton iteration stalls at an upwind kink (near
+# 2e-7 relative from rest, near 1e-9 absolute later), in FP64 as well, so each
+# step stops at 1e-6 relative to its initial defect or at 1e-5 of the first
+# step's initial defect, whichever comes first.
+RTOL_STEP = 1e-6
+ATOL_FRACTION = 1e-5
+
+
+def run_transient(args):
+    import numpy as np
+    import torch
+
+    from plugin_navierstokes_gb300 import NavierStokesFV1, build, mesh
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    n_cells, n_steps, dt, nu = args.cells if args.cells != 64 else 1024, 20, 0.01, 0.001
+    wl = (f"{n_cells}^2 jittered grid (+-0.2h, seed 2) split into {2 * n_cells * n_cells} triangles, backward Euler dt={dt} x {n_steps}, "
+          f"nu={nu}, full upwind + FIELDS, lid-driven cavity walls")
+    roid, X, C = mesh.jittered_triangles(n_cells, seed=2)
+    dofs, vals = mesh.cavity_dirichlet(X, 1.0)
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        import oracle
+
+        # bounded sample: the first time step on a 128^2 grid of the same construction, scaled by elements
+        rs, rX, rC = mesh.jittered_triangles(128, seed=2)
+        rd, rv = mesh.cavity_dirichlet(rX, 1.0)
+        o = oracle.Oracle(2)
+        o.set_kinematic_viscosity(nu)
+        o.set_upwind("full")
+        o.set_stabilization("fields")
+        o.set_mesh(rs, rX, rC)
+        o.set_dirichlet(rd, rv)
+        U0 = np.zeros(rX.shape[0] * 3)
+        U0[rd] = rv
+        t0 = time.perf_counter()
+        o.newton(U0.copy(), U_old=U0, dt=dt, rtol=1e-8, lin_rtol=1e-4, lin_maxit=20000)
+        el = time.perf_counter() - t0
+        v = (rC.shape[0] / C.shape[0]) / el
+        line = {"impl": "reference", "metric": "time steps/s", "value": v, "unit": "steps/s", "n_gpus": args.gpus, "steps": 1,
+                "warmup": 0, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": wl},
+                "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
+                                 "sample": f"first time step on the 128^2 grid of the same construction ({el:.1f} s), scaled by elements"},
+                "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    build.build()
+    d = NavierStokesFV1("u,v,p", "Inner")
+    d.set_kinematic_viscosity(nu)
+    d.set_upwind("full")
+    d.set_stabilization("fields")
+    d.set_mesh(roid, X, C)
+    d.set_dirichlet(dofs, vals)
+    n = X.shape[0] * 3
+    u0 = torch.zeros(n, dtype=torch.float64, device=dev)
+    u0[torch.from_numpy(dofs.astype(np.int64)).to(dev)] = torch.from_numpy(vals).to(dev)
+
+    D0 = torch.empty_like(u0)
+    d.assemble_defect(u0, D0, u0, dt)
+    atol = ATOL_FRACTION * float(D0.norm().item())
+
+    def march(prec, k):
+        u = u0.clone()
+        its, lin, times = [], [], []
+        for _ in range(k):
+            uo = u.clone()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = d.newton_solve(u, uo, dt=dt, rtol=RTOL_STEP, atol=atol, lin_rtol=1e-4, lin_max_iter=5000, jacobian_prec=prec,
+                               linear_solver="bicgstab")
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+            its.append(r["iterations"])
+            lin.append(r["linear_iterations"])
+        return u, its, lin, times
+
+    march("f32", min(max(args.warmup, 3), n_steps))
+    with ClockSampler(local) as clk:
+        u32, its32, lin32, t32 = march("f32", n_steps)
+    u64, its64, lin64, t64 = march("f64", n_steps)
+    # the mixed run's final state against the all-FP64 run
+    rel_diff = float(((u32 - u64).norm() / u64.norm()).item())
+    sec = sum(t32)
+    value = n_steps / sec
+    # e2e: host iterate in, 20 steps, host solution out
+    hu = u0.cpu().pin_memory()
+    hout = torch.empty_like(hu).pin_memory()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    u = hu.to(dev, non_blocking=True)
+    for _ in range(n_steps):
+        uo = u.clone()
+        d.newton_solve(u, uo, dt=dt, rtol=RTOL_STEP, atol=atol, lin_rtol=1e-4, lin_max_iter=5000, jacobian_prec="f32",
+                       linear_solver="bicgstab")
+    hout.copy_(u, non_blocking=True)
+    e1.record()
+    e1.synchronize()
+    e2e = n_steps / (e0.elapsed_time(e1) * 1e-3)
+    line = {"metric": "time steps/s", "value": value, "unit": "steps/s", "n_gpus": 1, "steps": n_steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": 1e3 * sec / n_steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 defect / f32 jacobian", "data": "synthetic (seeded jittered grid)",
+            "config": {"workload": wl, "triangles": int(C.shape[0]), "nodes": int(X.shape[0]),
+                       "l2": "inputs larger than L2",
+                       "mixed": {"newton_its": its32, "linear_its": lin32, "seconds": sec},
+                       "all_f64": {"newton_its": its64, "linear_its": lin64, "seconds": sum(t64), "steps_per_s": n_steps / sum(t64)},
+                       "final_state_rel_diff_vs_all_f64": rel_diff},
+            "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": hu.numel() * 8 / n_steps,
+                    "d2h_bytes_per_step": hout.numel() * 8 / n_steps},
+            "roofline": None, "cpu_baseline": None, "gpu_launches": None, "clocks": clk.summary()}
+    print(json.dumps(line))
     return 0
 
 

@@ -175,7 +175,8 @@ typedef struct {
     double lin_rtol;        /* relative residual reduction of the linear solve            */
     int lin_max_iter;       /* linear iterations per Newton step                          */
     int line_search_steps;  /* backtracking halvings (0 = full steps)                     */
-    int jacobian_prec;      /* NSFV1_F64 (plain method) or NSFV1_F32 (FP32 Jacobian)      */
+    int jacobian_prec;      /* NSFV1_F64 (plain method) or NSFV1_F32: Jacobian and its    */
+                            /* block inverses stored in FP32, Krylov vectors FP64         */
     int linear_solver;      /* NSFV1_BICGSTAB or NSFV1_GMRES                              */
     int gmres_restart;      /* GMRES restart length (<= 64)                               */
 } nsfv1_newton_params;

@@ -89,6 +89,25 @@ struct ClusterRed {
     }
 };
 
+// acc += the block row [q0, q1) of (vals, colIdx) applied to x (x indexed by
+// global column minus xoff): lane takes blocks lane, lane+G, ...; one fused
+// multiply-add per matrix entry
+template <typename VT, int b, int G>
+__device__ __forceinline__ void block_row_acc(const VT* __restrict__ vals, const int32_t* __restrict__ colIdx, int64_t q0, int64_t q1,
+                                              int lane, const VT* __restrict__ x, int64_t xoff, VT (&acc)[b]) {
+    for (int64_t q = q0 + lane; q < q1; q += G) {
+        const VT* blk = vals + q * (b * b);
+        const VT* xc = x + (int64_t)colIdx[q] * b - xoff;
+        VT xv[b];
+#pragma unroll
+        for (int j = 0; j < b; ++j) xv[j] = xc[j];
+#pragma unroll
+        for (int i = 0; i < b; ++i)
+#pragma unroll
+            for (int j = 0; j < b; ++j) acc[i] = fma(blk[i * b + j], xv[j], acc[i]);
+    }
+}
+
 template <typename VT, int b, int G>
 __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A) {
     cg::cluster_group cl = cg::this_cluster();
@@ -154,15 +173,7 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                 VT acc[b];
 #pragma unroll
                 for (int i = 0; i < b; ++i) acc[i] = VT(0);
-                for (int64_t idx = q0 * b * b + lane; idx < q1 * b * b; idx += G) {
-                    const int64_t q = idx / (b * b);
-                    const int w = (int)(idx - q * (b * b));
-                    const int i = w / b, j = w - (w / b) * b;
-                    const VT v = A.vals[idx] * xin[(int64_t)A.colIdx[q] * b + j - o];
-#pragma unroll
-                    for (int r = 0; r < b; ++r)
-                        if (r == i) acc[r] += v;
-                }
+                block_row_acc<VT, b, G>(A.vals, A.colIdx, q0, q1, lane, xin, o, acc);
 #pragma unroll
                 for (int off = G / 2; off > 0; off >>= 1)
 #pragma unroll
@@ -202,15 +213,7 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                 VT acc[b];
 #pragma unroll
                 for (int i = 0; i < b; ++i) acc[i] = VT(0);
-                for (int64_t idx = q0 * b * b + lane; idx < q1 * b * b; idx += G) {
-                    const int64_t q = idx / (b * b);
-                    const int w = (int)(idx - q * (b * b));
-                    const int i = w / b, j = w - (w / b) * b;
-                    const VT v = L.vals[idx] * xin[(int64_t)L.colIdx[q] * b + j - ol];
-#pragma unroll
-                    for (int r = 0; r < b; ++r)
-                        if (r == i) acc[r] += v;
-                }
+                block_row_acc<VT, b, G>(L.vals, L.colIdx, q0, q1, lane, xin, ol, acc);
 #pragma unroll
                 for (int off = G / 2; off > 0; off >>= 1)
 #pragma unroll

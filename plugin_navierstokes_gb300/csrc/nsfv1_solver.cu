@@ -1,10 +1,10 @@
 // Device linear algebra on the handle's block-CSR pattern and the Newton
 // driver: block SpMV, point-block Jacobi (inverted b x b diagonal blocks),
 // right-preconditioned BiCGStab and restarted GMRES, FP64 defect norms.
-// Krylov vectors and the Jacobian share one value type VT (double for the
-// plain method, float for the FP32-Jacobian mode); reductions accumulate in
-// FP64 with a fixed grid and a fixed summation tree, so results are bitwise
-// reproducible run to run.
+// The Jacobian and its block inverses are stored in MT (double for the plain
+// method, float for the FP32-Jacobian mode); Krylov vectors are FP64 in both;
+// reductions accumulate in FP64 with a fixed grid and a fixed summation tree,
+// so results are bitwise reproducible run to run.
 #include <cmath>
 #include <cstring>
 #include <type_traits>
@@ -20,43 +20,167 @@ static constexpr int kRedBlocks = 608;   // 4 x 152 SMs
 static constexpr int kRedThreads = 256;
 
 // ---------------------------------------------------------------------------
-// block SpMV: one group of G lanes per block row; lane l takes entries l, l+G,
-// ... of the row's contiguous b*b-blocks (coalesced over the values), then the
-// group reduces the b row sums with shuffles in a fixed order.
+// block SpMV y = A x: one group of G lanes per block row; lane l takes the
+// blocks l, l+G, ... of the row (consecutive lanes read consecutive blocks)
+// and applies each whole b x b block to the b entries of x it multiplies, so
+// every matrix entry costs one fused multiply-add; the group then reduces its
+// b row sums with shuffles in a fixed order.
+//
+// GB300 issues only two FP64 instructions per clock per SM, so the FP32-matrix
+// variant keeps its arithmetic off the FP64 pipe: x (FP64) is split into two
+// floats by integer operations (xh = the leading 24 bits, xl = the next ones),
+// and the products are accumulated in double-float (TwoSum of the FP32
+// products plus their exact FMA errors), converted to FP64 once per row. The
+// result is accurate to about 1e-13 of sum |a x|, far below the FP32 rounding
+// of the matrix itself, at a handful of FP32/INT operations per entry.
 // ---------------------------------------------------------------------------
+struct DFloat {
+    float hi, lo;
+};
+
+// x = xh + xl (+ |x| 2^-47): both floats from the bits of x, no FP64 instruction
+__device__ __forceinline__ void split_double(double x, float& xh, float& xl) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned e = (unsigned)(u >> 52) & 0x7FFu;
+    const unsigned sgn = (unsigned)(u >> 63) << 31;
+    if (e < 897u || e > 1150u) {   // 0, subnormal, tiny, huge, inf or nan: one conversion
+        xh = (float)x;
+        xl = 0.f;
+        return;
+    }
+    const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+    xh = __uint_as_float(sgn | ((e - 896u) << 23) | (unsigned)(m >> 29));
+    const unsigned r = (unsigned)(m & 0x1FFFFFFFull);   // the 29 mantissa bits below xh
+    if (e < 949u || r == 0u) {
+        xl = 0.f;   // |x| < 2^-74: the remainder is below float range
+        return;
+    }
+    const float scale = __uint_as_float((e - 1075u + 127u) << 23);   // 2^(e - 1075)
+    xl = __uint_as_float(__float_as_uint((float)r * scale) | sgn);
+}
+
+// a + b exactly as s + err (Knuth's TwoSum; _rn intrinsics keep the compiler
+// from contracting or reassociating the error-free steps)
+__device__ __forceinline__ float two_sum(float a, float b, float& err) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+
+template <typename MT, typename XT, int b>
+struct RowAcc;
+
+template <typename XT, int b>
+struct RowAcc<double, XT, b> {
+    double v[b];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int i = 0; i < b; ++i) v[i] = 0.0;
+    }
+    __device__ __forceinline__ void block(const double* __restrict__ blk, const XT* __restrict__ xc) {
+        double x[b];
+#pragma unroll
+        for (int j = 0; j < b; ++j) x[j] = (double)__ldg(xc + j);
+#pragma unroll
+        for (int i = 0; i < b; ++i)
+#pragma unroll
+            for (int j = 0; j < b; ++j) v[i] = fma(__ldg(blk + i * b + j), x[j], v[i]);
+    }
+    template <int G>
+    __device__ __forceinline__ void reduce() {
+#pragma unroll
+        for (int off = G / 2; off > 0; off >>= 1)
+#pragma unroll
+            for (int i = 0; i < b; ++i) v[i] += __shfl_down_sync(0xffffffffu, v[i], off, G);
+    }
+    __device__ __forceinline__ double value(int i) const { return v[i]; }
+};
+
+template <int b>
+struct RowAcc<float, double, b> {
+    DFloat v[b];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int i = 0; i < b; ++i) v[i] = DFloat{0.f, 0.f};
+    }
+    __device__ __forceinline__ void block(const float* __restrict__ blk, const double* __restrict__ xc) {
+        float xh[b], xl[b];
+#pragma unroll
+        for (int j = 0; j < b; ++j) split_double(__ldg(xc + j), xh[j], xl[j]);
+#pragma unroll
+        for (int i = 0; i < b; ++i)
+#pragma unroll
+            for (int j = 0; j < b; ++j) {
+                const float a = __ldg(blk + i * b + j);
+                const float p = __fmul_rn(a, xh[j]);
+                const float pe = fmaf(a, xh[j], -p);   // a xh = p + pe exactly
+                float e;
+                v[i].hi = two_sum(v[i].hi, p, e);
+                v[i].lo += e + fmaf(a, xl[j], pe);
+            }
+    }
+    template <int G>
+    __device__ __forceinline__ void reduce() {
+#pragma unroll
+        for (int off = G / 2; off > 0; off >>= 1)
+#pragma unroll
+            for (int i = 0; i < b; ++i) {
+                const float oh = __shfl_down_sync(0xffffffffu, v[i].hi, off, G);
+                const float ol = __shfl_down_sync(0xffffffffu, v[i].lo, off, G);
+                float e;
+                v[i].hi = two_sum(v[i].hi, oh, e);
+                v[i].lo += e + ol;
+            }
+    }
+    __device__ __forceinline__ double value(int i) const { return (double)v[i].hi + (double)v[i].lo; }
+};
+
+template <int b>
+struct RowAcc<float, float, b> {
+    float v[b];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int i = 0; i < b; ++i) v[i] = 0.f;
+    }
+    __device__ __forceinline__ void block(const float* __restrict__ blk, const float* __restrict__ xc) {
+        float x[b];
+#pragma unroll
+        for (int j = 0; j < b; ++j) x[j] = __ldg(xc + j);
+#pragma unroll
+        for (int i = 0; i < b; ++i)
+#pragma unroll
+            for (int j = 0; j < b; ++j) v[i] = fmaf(__ldg(blk + i * b + j), x[j], v[i]);
+    }
+    template <int G>
+    __device__ __forceinline__ void reduce() {
+#pragma unroll
+        for (int off = G / 2; off > 0; off >>= 1)
+#pragma unroll
+            for (int i = 0; i < b; ++i) v[i] += __shfl_down_sync(0xffffffffu, v[i], off, G);
+    }
+    __device__ __forceinline__ float value(int i) const { return v[i]; }
+};
+
 template <typename VT, typename XT, int b, int G>
 __global__ void __launch_bounds__(256) k_bsr_mv(int64_t nRows, const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx,
                                                 const VT* __restrict__ vals, const XT* __restrict__ x, XT* __restrict__ y) {
-    constexpr int bb = b * b;
     const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t row = gid / G;
     const int lane = threadIdx.x % G;
     // rows past the end run the (empty) loop so every lane reaches the shuffles
     const bool valid = row < nRows;
     const int64_t q0 = valid ? rowPtr[row] : 0, q1 = valid ? rowPtr[row + 1] : 0;
-    double acc[b];
-#pragma unroll
-    for (int i = 0; i < b; ++i) acc[i] = 0.0;
-    for (int64_t idx = q0 * bb + lane; idx < q1 * bb; idx += G) {
-        const int64_t q = idx / bb;
-        const int w = (int)(idx - q * bb);
-        const int i = w / b, j = w - (w / b) * b;
-        const double v = (double)__ldg(vals + idx) * (double)__ldg(x + (int64_t)__ldg(colIdx + q) * b + j);
-#pragma unroll
-        for (int r = 0; r < b; ++r)
-            if (r == i) acc[r] += v;
-    }
-#pragma unroll
-    for (int off = G / 2; off > 0; off >>= 1)
-#pragma unroll
-        for (int r = 0; r < b; ++r) acc[r] += __shfl_down_sync(0xffffffffu, acc[r], off, G);
+    RowAcc<VT, XT, b> acc;
+    acc.zero();
+    for (int64_t q = q0 + lane; q < q1; q += G) acc.block(vals + q * (b * b), x + (int64_t)__ldg(colIdx + q) * b);
+    acc.template reduce<G>();
     if (valid && lane == 0) {
 #pragma unroll
-        for (int r = 0; r < b; ++r) y[row * b + r] = (XT)acc[r];
+        for (int r = 0; r < b; ++r) y[row * b + r] = (XT)acc.value(r);
     }
 }
 
-// inverse of the diagonal blocks (Gauss-Jordan, partial pivoting); err bit 2 on a zero pivot
 template <typename VT, typename OT, int b>
 __global__ void k_block_inv(int64_t nRows, const int32_t* __restrict__ diagPos, const VT* __restrict__ vals, OT* __restrict__ Dinv, int* err) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -64,19 +188,20 @@ __global__ void k_block_inv(int64_t nRows, const int32_t* __restrict__ diagPos, 
     if (!block_inverse<b>(vals + (int64_t)diagPos[r] * b * b, Dinv + r * b * b)) atomicOr(err, 2);
 }
 
-template <typename VT, int b>
-__global__ void k_prec(int64_t nRows, const VT* __restrict__ Dinv, const VT* __restrict__ in, VT* __restrict__ out) {
+// out = Dinv in per node block (Dinv of type MT, vectors of type VT, products in VT)
+template <typename MT, typename VT, int b>
+__global__ void k_prec(int64_t nRows, const MT* __restrict__ Dinv, const VT* __restrict__ in, VT* __restrict__ out) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nRows) return;
     VT x[b];
 #pragma unroll
     for (int j = 0; j < b; ++j) x[j] = in[r * b + j];
-    const VT* M = Dinv + r * b * b;
+    const MT* M = Dinv + r * b * b;
 #pragma unroll
     for (int i = 0; i < b; ++i) {
         VT a = VT(0);
 #pragma unroll
-        for (int j = 0; j < b; ++j) a += M[i * b + j] * x[j];
+        for (int j = 0; j < b; ++j) a += (VT)M[i * b + j] * x[j];
         out[r * b + i] = a;
     }
 }
@@ -153,18 +278,21 @@ __global__ void k_bicg_beta(const double* partials, int nb, double* S) {
     block_sum_partials<1>(partials, nb, v);
     if (threadIdx.x == 0) {
         S[S_RHO1] = v[0];
-        S[S_BETA] = (v[0] / S[S_RHO]) * (S[S_ALPHA] / S[S_OMEGA]);
-        if (v[0] == 0.0) S[S_FLAG] = 1.0;
+        double beta = (v[0] / S[S_RHO]) * (S[S_ALPHA] / S[S_OMEGA]);
+        // (near) breakdown: rho1 negligible against ||r0|| ||r||, or a non-finite beta
+        if (!(fabs(v[0]) > 1e-14 * sqrt(S[S_NR02] * S[S_NR2])) || !(fabs(beta) < 1e10)) { S[S_FLAG] = 1.0; beta = 0.0; }
+        S[S_BETA] = beta;
     }
 }
-// alpha = rho1 / (r0, v)
+// alpha = rho1 / (r0, v); near breakdown when (r0, v) is negligible against ||r0|| ||v||
 __global__ void k_bicg_alpha(const double* partials, int nb, double* S) {
-    double v[1];
-    block_sum_partials<1>(partials, nb, v);
+    double v[2];
+    block_sum_partials<2>(partials, nb, v);
     if (threadIdx.x == 0) {
         S[S_R0V] = v[0];
-        S[S_ALPHA] = (v[0] != 0.0) ? S[S_RHO1] / v[0] : 0.0;
-        if (v[0] == 0.0) S[S_FLAG] = 1.0;
+        double alpha = (v[0] != 0.0) ? S[S_RHO1] / v[0] : 0.0;
+        if (!(fabs(v[0]) > 1e-12 * sqrt(S[S_NR02] * v[1])) || !isfinite(alpha)) { S[S_FLAG] = 1.0; alpha = 0.0; }
+        S[S_ALPHA] = alpha;
     }
 }
 // omega = (t, s) / (t, t)
@@ -173,7 +301,8 @@ __global__ void k_bicg_omega(const double* partials, int nb, double* S) {
     block_sum_partials<2>(partials, nb, v);
     if (threadIdx.x == 0) {
         S[S_TS] = v[0]; S[S_TT] = v[1];
-        S[S_OMEGA] = (v[1] != 0.0) ? v[0] / v[1] : 0.0;
+        const double omega = (v[1] != 0.0) ? v[0] / v[1] : 0.0;
+        S[S_OMEGA] = isfinite(omega) ? omega : 0.0;
     }
 }
 // ||r||^2 and rho <- rho1
@@ -213,6 +342,12 @@ template <typename A, typename B>
 __global__ void k_convert(int64_t n, const A* __restrict__ a, B* __restrict__ b) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] = (B)a[i];
+}
+// b = scale * a (the Newton right-hand side normalised to unit norm before the solve)
+template <typename A, typename B>
+__global__ void k_convert_scaled(int64_t n, const A* __restrict__ a, B* __restrict__ b, double scale) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (B)(scale * (double)a[i]);
 }
 template <typename VT>
 __global__ void k_fill(int64_t n, VT* a, VT v) {
@@ -293,24 +428,24 @@ __global__ void k_multi_axpy_add(int64_t n, int m, const double* __restrict__ y,
 
 static inline int grid_for(int64_t n, int t = 256) { return (int)((n + t - 1) / t); }
 
-template <typename VT>
-static cudaError_t spmv(const Disc& D, const VT* vals, const VT* x, VT* y, cudaStream_t s) {
+template <typename MT, typename VT>
+static cudaError_t spmv(const Disc& D, const MT* vals, const VT* x, VT* y, cudaStream_t s) {
     const int64_t nR = D.nNodes;
     const int b = D.dim + 1;
     if (b == 4) {
         constexpr int G = 16;
-        k_bsr_mv<VT, VT, 4, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y);
+        k_bsr_mv<MT, VT, 4, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y);
     } else {
         constexpr int G = 8;
-        k_bsr_mv<VT, VT, 3, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y);
+        k_bsr_mv<MT, VT, 3, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y);
     }
     return cudaGetLastError();
 }
 
-template <typename VT>
-static void prec_apply(const Disc& D, const VT* Dinv, const VT* in, VT* out, cudaStream_t s) {
-    if (D.dim == 3) k_prec<VT, 4><<<grid_for(D.nNodes), 256, 0, s>>>(D.nNodes, Dinv, in, out);
-    else k_prec<VT, 3><<<grid_for(D.nNodes), 256, 0, s>>>(D.nNodes, Dinv, in, out);
+template <typename MT, typename VT>
+static void prec_apply(const Disc& D, const MT* Dinv, const VT* in, VT* out, cudaStream_t s) {
+    if (D.dim == 3) k_prec<MT, VT, 4><<<grid_for(D.nNodes), 256, 0, s>>>(D.nNodes, Dinv, in, out);
+    else k_prec<MT, VT, 3><<<grid_for(D.nNodes), 256, 0, s>>>(D.nNodes, Dinv, in, out);
 }
 
 template <typename VT, int K>
@@ -351,7 +486,7 @@ bool Disc::ensure_workspace(int prec, int gmresM) {
     auto al = [&](auto*& p, size_t bytes) { return cuda_ok(cudaMalloc((void**)&p, bytes), "workspace alloc"); };
     if (!al(ws.D, n * 8) || !al(ws.Dt, n * 8) || !al(ws.Ut, n * 8) || !al(ws.du, n * 8) ||
         !al(ws.J, colIdx.size() * b * b * vt) || !al(ws.Dinv, (size_t)nNodes * b * b * vt) ||
-        !al(ws.vec, (size_t)nvec * n * vt) || !al(ws.red, sizeof(double) * kRedBlocks * 80) ||
+        !al(ws.vec, (size_t)nvec * n * sizeof(double)) || !al(ws.red, sizeof(double) * kRedBlocks * 80) ||
         !al(ws.scal, sizeof(double) * 256))
         return false;
     if (!cuda_ok(cudaMallocHost((void**)&ws.hscal, sizeof(double) * 256), "pinned alloc")) return false;
@@ -371,8 +506,13 @@ static bool read_scal(Disc& D, int first, int k, cudaStream_t s) {
 
 // BiCGStab on J x = rhs (right point-block-Jacobi preconditioning), x = 0 start.
 // Returns iterations, or -1 on breakdown / failure (D.status set on CUDA errors).
-template <typename VT>
-static int bicgstab(Disc& D, const VT* J, const VT* Dinv, const VT* rhs, VT* x, double rtol, int maxit, double* relres, cudaStream_t s) {
+static constexpr int kMaxBicgRestarts = 20;
+// The Krylov vectors are FP64 whatever the precision MT of the stored Jacobian:
+// an FP32 matrix then only perturbs the operator (relative 6e-8 per entry),
+// while FP32 vectors would let the recursive residual drift from the true one.
+template <typename MT>
+static int bicgstab(Disc& D, const MT* J, const MT* Dinv, const double* rhs, double* x, double rtol, int maxit, double* relres, cudaStream_t s) {
+    using VT = double;
     Workspace& W = D.ws;
     const int64_t n = W.n;
     VT* V = (VT*)W.vec;
@@ -397,17 +537,18 @@ static int bicgstab(Disc& D, const VT* J, const VT* Dinv, const VT* rhs, VT* x, 
     const double nr0 = std::sqrt(W.hscal[S_NR02]);
     *relres = 1.0;
     if (nr0 == 0.0) return 0;
+    int restarts = 0;
     for (int it = 1; it <= maxit; ++it) {
         { const VT* a[1] = {r0}; const VT* c[1] = {r}; dots<VT, 1>(n, a, c, W.red, s); }
         k_bicg_beta<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
         k_bicg_p<VT><<<g, 256, 0, s>>>(n, S, r, v, p);
-        prec_apply<VT>(D, Dinv, p, ph, s);
-        spmv<VT>(D, J, ph, v, s);
-        { const VT* a[1] = {r0}; const VT* c[1] = {v}; dots<VT, 1>(n, a, c, W.red, s); }
+        prec_apply<MT, VT>(D, Dinv, p, ph, s);
+        spmv<MT, VT>(D, J, ph, v, s);
+        { const VT* a[2] = {r0, v}; const VT* c[2] = {v, v}; dots<VT, 2>(n, a, c, W.red, s); }
         k_bicg_alpha<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
         k_bicg_s<VT><<<g, 256, 0, s>>>(n, S, r, v, sv);
-        prec_apply<VT>(D, Dinv, sv, shv, s);
-        spmv<VT>(D, J, shv, t, s);
+        prec_apply<MT, VT>(D, Dinv, sv, shv, s);
+        spmv<MT, VT>(D, J, shv, t, s);
         { const VT* a[2] = {t, t}; const VT* c[2] = {sv, t}; dots<VT, 2>(n, a, c, W.red, s); }
         k_bicg_omega<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
         k_bicg_x<VT><<<g, 256, 0, s>>>(n, S, ph, shv, sv, t, x, r);
@@ -419,17 +560,29 @@ static int bicgstab(Disc& D, const VT* J, const VT* Dinv, const VT* rhs, VT* x, 
         *relres = nr / nr0;
         if (!std::isfinite(nr)) return -1;   // hard failure: x is not usable
         if (*relres < rtol) return it;
-        // breakdown (rho = 0, (r0, v) = 0 or omega = 0): stop with the last
-        // finite iterate and let the Newton line search judge it
-        if (W.hscal[S_FLAG] != 0.0 || W.hscal[S_OMEGA] == 0.0) return it;
+        // (near) breakdown (rho1 or (r0, v) negligible, omega = 0): restart with
+        // the current residual as the shadow vector; after too many restarts
+        // stop with the last finite iterate and let the Newton line search judge it
+        if (W.hscal[S_FLAG] != 0.0 || W.hscal[S_OMEGA] == 0.0) {
+            if (++restarts > kMaxBicgRestarts) return it;
+            cudaMemcpyAsync(r0, r, n * sizeof(VT), cudaMemcpyDeviceToDevice, s);
+            k_fill<VT><<<g, 256, 0, s>>>(n, p, VT(0));
+            k_fill<VT><<<g, 256, 0, s>>>(n, v, VT(0));
+            double re[S_NSCAL];
+            std::memcpy(re, W.hscal, sizeof(re));
+            re[S_RHO] = 1.0; re[S_ALPHA] = 1.0; re[S_OMEGA] = 1.0; re[S_FLAG] = 0.0; re[S_NR02] = re[S_NR2];
+            std::memcpy(W.hscal, re, sizeof(re));
+            cudaMemcpyAsync(S, W.hscal, sizeof(re), cudaMemcpyHostToDevice, s);
+        }
     }
     return maxit;
 }
 
 // restarted GMRES(m), right preconditioned, classical Gram-Schmidt with one
 // re-orthogonalisation pass; Hessenberg least squares (Givens) on the host.
-template <typename VT>
-static int gmres(Disc& D, const VT* J, const VT* Dinv, const VT* rhs, VT* x, double rtol, int maxit, int m, double* relres, cudaStream_t s) {
+template <typename MT>
+static int gmres(Disc& D, const MT* J, const MT* Dinv, const double* rhs, double* x, double rtol, int maxit, int m, double* relres, cudaStream_t s) {
+    using VT = double;
     Workspace& W = D.ws;
     const int64_t n = W.n;
     VT* base = (VT*)W.vec;
@@ -445,7 +598,7 @@ static int gmres(Disc& D, const VT* J, const VT* Dinv, const VT* rhs, VT* x, dou
     *relres = 1.0;
     while (it < maxit) {
         // V_0 = rhs - J x
-        spmv<VT>(D, J, x, w, s);
+        spmv<MT, VT>(D, J, x, w, s);
         cudaMemcpyAsync(Vb, rhs, n * sizeof(VT), cudaMemcpyDeviceToDevice, s);
         W.hscal[40] = 1.0;
         cudaMemcpyAsync(hdev, W.hscal + 40, sizeof(double), cudaMemcpyHostToDevice, s);
@@ -468,8 +621,8 @@ static int gmres(Disc& D, const VT* J, const VT* Dinv, const VT* rhs, VT* x, dou
         for (; j < m && it < maxit; ++j) {
             ++it;
             VT* Zj = Zb + (int64_t)j * n;
-            prec_apply<VT>(D, Dinv, Vb + (int64_t)j * n, Zj, s);
-            spmv<VT>(D, J, Zj, w, s);
+            prec_apply<MT, VT>(D, Dinv, Vb + (int64_t)j * n, Zj, s);
+            spmv<MT, VT>(D, J, Zj, w, s);
             double hcol[66] = {0};
             for (int pass = 0; pass < 2; ++pass) {
                 k_multidot_partial<VT><<<kRedBlocks, kRedThreads, 0, s>>>(n, j + 1, Vb, w, W.red);
@@ -520,18 +673,19 @@ static int gmres(Disc& D, const VT* J, const VT* Dinv, const VT* rhs, VT* x, dou
     return it;
 }
 
-template <typename VT>
+template <typename MT>
 static int newton_impl(Disc& D, double* u, const double* u_old, double dt, const nsfv1_newton_params& p, nsfv1_newton_result& res,
                        cudaStream_t s) {
-    const int prec = std::is_same<VT, double>::value ? NSFV1_F64 : NSFV1_F32;
+    using VT = double;   // Krylov vectors
+    const int prec = std::is_same<MT, double>::value ? NSFV1_F64 : NSFV1_F32;
     const int m = std::min(std::max(p.gmres_restart, 1), 64);
     if (!D.ensure_workspace(prec, p.linear_solver == NSFV1_GMRES ? m : 0)) return D.status;
     Workspace& W = D.ws;
     const int64_t n = W.n;
     const int g = grid_for(n);
     const int b = D.dim + 1;
-    VT* J = (VT*)W.J;
-    VT* Dinv = (VT*)W.Dinv;
+    MT* J = (MT*)W.J;
+    MT* Dinv = (MT*)W.Dinv;
     VT* Vv = (VT*)W.vec;
     VT* rhsV = Vv + (int64_t)(W.nvec - 2) * n;   // rhs of the linear solve (VT)
     VT* xsol = Vv + (int64_t)(W.nvec - 1) * n;   // its solution du (VT)
@@ -552,24 +706,25 @@ static int newton_impl(Disc& D, double* u, const double* u_old, double dt, const
         ++it;
         if (!D.assemble_jacobian(u, u_old, dt, J, prec, s, false)) return D.status;
         cudaMemsetAsync(D.d_err, 0, sizeof(int), s);
-        if (b == 4) k_block_inv<VT, VT, 4><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, J, Dinv, D.d_err);
-        else k_block_inv<VT, VT, 3><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, J, Dinv, D.d_err);
+        if (b == 4) k_block_inv<MT, MT, 4><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, J, Dinv, D.d_err);
+        else k_block_inv<MT, MT, 3><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, J, Dinv, D.d_err);
         int herr = 0;
         cudaMemcpyAsync(&herr, D.d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (!D.cuda_ok(cudaStreamSynchronize(s), "jacobian")) return D.status;
         if (herr & 1) { D.fail(NSFV1_ERR_GEOMETRY, "upwind: cannot find cut side"); cudaMemsetAsync(D.d_err, 0, sizeof(int), s); return D.status; }
         if (herr & 2) { status = NSFV1_ERR_BREAKDOWN; D.fail(NSFV1_ERR_BREAKDOWN, "singular diagonal block"); cudaMemsetAsync(D.d_err, 0, sizeof(int), s); break; }
-        k_convert<double, VT><<<g, 256, 0, s>>>(n, W.D, rhsV);
+        // unit-norm right-hand side: the Krylov vectors stay O(1) in FP32 whatever the defect's size
+        k_convert_scaled<double, VT><<<g, 256, 0, s>>>(n, W.D, rhsV, 1.0 / nd);
         double rr = 0;
         int li;
-        if (p.linear_solver == NSFV1_GMRES) li = gmres<VT>(D, J, Dinv, rhsV, xsol, p.lin_rtol, p.lin_max_iter, m, &rr, s);
-        else li = bicgstab<VT>(D, J, Dinv, rhsV, xsol, p.lin_rtol, p.lin_max_iter, &rr, s);
+        if (p.linear_solver == NSFV1_GMRES) li = gmres<MT>(D, J, Dinv, rhsV, xsol, p.lin_rtol, p.lin_max_iter, m, &rr, s);
+        else li = bicgstab<MT>(D, J, Dinv, rhsV, xsol, p.lin_rtol, p.lin_max_iter, &rr, s);
         if (D.status == NSFV1_ERR_CUDA) return D.status;
         if (li < 0) { status = NSFV1_ERR_BREAKDOWN; D.fail(NSFV1_ERR_BREAKDOWN, "linear solver breakdown"); break; }
         res.linear_iterations += li;
         double lambda = 1.0, ndt = 0.0;
         for (int k = 0; k <= p.line_search_steps; ++k) {
-            k_newton_update<VT><<<g, 256, 0, s>>>(n, u, xsol, lambda, W.Ut);
+            k_newton_update<VT><<<g, 256, 0, s>>>(n, u, xsol, lambda * nd, W.Ut);
             if (!D.assemble_defect(W.Ut, u_old, dt, W.Dt, s)) return D.status;
             norm2sq(n, W.Dt, W.red, W.scal + 100, s);
             if (!read_scal(D, 100, 1, s)) return D.status;
@@ -611,8 +766,8 @@ bool block_jacobi_run(Disc& D, const void* vals, int prec, const double* r, doub
         if (b == 4) k_block_inv<float, double, 4><<<g, 128, 0, s>>>(nR, D.d_diagPos, (const float*)vals, Dinv, D.d_err);
         else k_block_inv<float, double, 3><<<g, 128, 0, s>>>(nR, D.d_diagPos, (const float*)vals, Dinv, D.d_err);
     }
-    if (b == 4) k_prec<double, 4><<<grid_for(nR), 256, 0, s>>>(nR, Dinv, r, z);
-    else k_prec<double, 3><<<grid_for(nR), 256, 0, s>>>(nR, Dinv, r, z);
+    if (b == 4) k_prec<double, double, 4><<<grid_for(nR), 256, 0, s>>>(nR, Dinv, r, z);
+    else k_prec<double, double, 3><<<grid_for(nR), 256, 0, s>>>(nR, Dinv, r, z);
     if (!D.cuda_ok(cudaGetLastError(), "block_jacobi launch")) return false;
     int err = 0;
     if (!D.cuda_ok(cudaMemcpyAsync(&err, D.d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "block_jacobi")) return false;

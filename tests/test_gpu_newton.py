@@ -87,3 +87,25 @@ def test_newton_reports_nonfinite(cuda):
     d.set_dirichlet(dofs, vals)
     r = d.newton_solve(u, rtol=1e-6, lin_rtol=1e-3)
     assert r["status"] == 0
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_transient_newton_on_jittered_triangles(cuda, prec):
+    """Backward Euler on jittered triangles (the transient workload's construction
+    at 32^2): every step reaches its Newton target, and the FP64 oracle defect of
+    the end state of each step (with the previous state as u_old) meets it."""
+    import torch
+    roid, X, C = mesh.jittered_triangles(32, seed=2)
+    dofs, vals = mesh.cavity_dirichlet(X, 1.0)
+    d = NavierStokesFV1("u,v,p", "Inner")
+    d.set_kinematic_viscosity(0.001); d.set_upwind("full"); d.set_stabilization("fields")
+    d.set_mesh(roid, X, C); d.set_dirichlet(dofs, vals)
+    o = oracle.Oracle(2); o.set_kinematic_viscosity(0.001); o.set_upwind("full"); o.set_stabilization("fields")
+    o.set_mesh(roid, X, C); o.set_dirichlet(dofs, vals)
+    u = torch.zeros(X.shape[0] * 3, dtype=torch.float64, device=cuda)
+    for _ in range(3):
+        uo = u.clone()
+        r = d.newton_solve(u, uo, dt=0.01, rtol=1e-6, lin_rtol=1e-4, lin_max_iter=5000, jacobian_prec=prec)
+        assert r["status"] == 0, r
+        D, _ = o.assemble(u.cpu().numpy(), uo.cpu().numpy(), 0.01, jacobian=False)
+        assert np.linalg.norm(D) <= 1.01e-6 * r["initial_defect"], (np.linalg.norm(D), r)
