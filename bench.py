@@ -162,6 +162,7 @@ def main():
     ap.add_argument("--workload", default="assembly", choices=["assembly", "batched", "learned", "transient"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cells", type=int, default=64, help="assembly workload: cells per side (64 is the benchmark; smaller for profiling)")
+    ap.add_argument("--time-steps", type=int, default=20, help="transient workload: backward-Euler steps (20 is the benchmark)")
     args = ap.parse_args()
     global N_CELLS
     N_CELLS = args.cells
@@ -210,6 +211,9 @@ def main():
         d.assemble_defect(tu, D, stream=stream)
         d.assemble_jacobian(tu, J, stream=stream)
 
+    # CTA size of the colour launches from the assembly autotuner
+    asm_threads, asm_ms = d.assembly_autotune(tu, "f64", (32, 64, 128), stream=stream)
+    torch.cuda.synchronize()
     ev = lambda: torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -305,6 +309,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded solenoidal state)",
             "config": config_dict({"defect_ms": sum(tdef64) / args.steps, "jacobian_ms": jac_ms,
+                                   "assembly_cta_threads": asm_threads,
+                                   "autotune_ms": dict(zip(("32", "64", "128"), [round(x, 3) for x in asm_ms])),
                                    "fp32_jacobian_mode": {"value": world * n_el / (ms32 * 1e-3), "ms_per_step": ms32,
                                                           "defect_ms": sum(tdef32) / args.steps,
                                                           "jacobian_ms": sum(tjac32) / args.steps}}),
@@ -361,6 +367,13 @@ def _oracle_solves(N, Re, lid, budget_s=20.0):
     return done / el, done, el
 
 
+# Newton options of the fast (mixed) path: the reference's exact-Jacobian
+# factor 1 (set_exact_jacobian, navier_stokes_base.h:194-196) and Eisenstat-
+# Walker linear tolerances up to 0.3; the plain path keeps the reference's
+# defaults (factor 0) and a fixed linear tolerance of 1e-3.
+FAST_EXACT, FAST_FORCING = 1.0, 0.3
+
+
 def run_solves(args):
     import numpy as np
     import torch
@@ -394,6 +407,7 @@ def run_solves(args):
 
     dev = torch.device(f"cuda:{local}")
     torch.cuda.set_device(dev)
+    total_inst = len(N)
     if world > 1:
         import torch.distributed as dist
 
@@ -409,7 +423,8 @@ def run_solves(args):
     build.build()
     extra = {}
     model = None
-    if args.workload == "learned":
+    learned = args.workload == "learned"
+    if learned:
         t0 = time.perf_counter()
         tRe, tlid = cavity_draws(2048, 4)
         coords, targets, cond, tres = generate_training_set(tRe, tlid, N=128, batch=256, cluster_size=16)
@@ -421,71 +436,80 @@ def run_solves(args):
         extra["training"] = {"solves": 2048, "converged": int(sum(r["status"] == 0 for r in tres)), "generate_s": round(tgen, 2),
                              "train_steps": 6000, "train_s": round(time.perf_counter() - t0, 2), "final_loss": float(hist[-20:].mean())}
         del coords, targets, cond
-    cb = CavityBatch(N, Re, lid)
-    n_inst = cb.n_inst
-    prec_main = "f32"
-    cb.autotune(prec_main)
-    cl32 = cb.cluster_size
+    cb_fast = CavityBatch(N, Re, lid, exact_jacobian=FAST_EXACT)
+    cb_plain = CavityBatch(N, Re, lid)
+    n_inst = cb_fast.n_inst
 
-    def solve_once(prec, learned, cluster):
-        cb.cluster_size = cluster
+    def setting(cb, prec, init, forcing):
+        tune = cb.autotune(prec, forcing_max=forcing)
+        return {"cb": cb, "prec": prec, "init": init, "forcing": forcing, "tune": tune}
+
+    def solve_once(st):
+        cb = st["cb"]
+        cb.cluster_size, cb.smooth_steps, cb.coarse_steps = st["tune"]["cluster_size"], st["tune"]["smooth_steps"], st["tune"]["coarse_steps"]
         u = cb.zeros()
-        if learned:
+        if st["init"] == "learned":
             cb.predict(model, u)
-        res = cb.solve(u, prec, zero_fallback=learned)
+        res = cb.solve(u, st["prec"], zero_fallback=st["init"] == "learned", forcing_max=st["forcing"])
         return u, res
 
-    def timed(prec, learned, cluster, k):
+    def timed(st, k):
         ts, res = [], None
         for _ in range(k):
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            u, res = solve_once(prec, learned, cluster)
+            u, res = solve_once(st)
             e1.record()
             e1.synchronize()
             ts.append(e0.elapsed_time(e1) * 1e-3)
         return ts, res
 
-    learned = args.workload == "learned"
+    stats = lambda r: {"converged": int(sum(x["status"] == 0 for x in r)), "newton_its_mean": float(np.mean([x["iterations"] for x in r])),
+                       "newton_its_max": int(max(x["iterations"] for x in r)),
+                       "linear_its_mean": float(np.mean([x["linear_iterations"] for x in r]))}
+    # learned workload: warm start + FP32 Jacobian + exact Jacobian + adaptive tolerances; the uneven
+    # batch: FP32 Jacobian with the reference's Newton options (the exact-Jacobian variant costs
+    # more on its 192^2 and 256^2 instances, see the ablation)
+    main = setting(cb_fast, "f32", "learned", FAST_FORCING) if learned else setting(cb_plain, "f32", "zero", 0.0)
     for _ in range(args.warmup):
-        solve_once(prec_main, learned, cl32)
+        solve_once(main)
     if world > 1:
         torch.distributed.barrier()
     with ClockSampler(local) as clk:
-        ts, res = timed(prec_main, learned, cl32, args.steps)
+        ts, res = timed(main, args.steps)
     sec = sum(ts) / len(ts)
     if world > 1:
         t = torch.tensor([sec], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         sec = float(t.item())
-    total_inst = 256
     value = total_inst / sec
-    stats = lambda r: {"converged": int(sum(x["status"] == 0 for x in r)), "newton_its_mean": float(np.mean([x["iterations"] for x in r])),
-                       "newton_its_max": int(max(x["iterations"] for x in r)),
-                       "linear_its_mean": float(np.mean([x["linear_iterations"] for x in r]))}
-    extra["main"] = dict(stats(res), jacobian="f32", init="learned" if learned else "zero", cluster_size=cl32)
-    # plain FP64 from zero, and the ablations, on the same batch (one timed solve each after one warm-up)
-    cb.autotune("f64")
-    cl64 = cb.cluster_size
-    solve_once("f64", False, cl64)
-    t64, r64 = timed("f64", False, cl64, 1)
-    extra["plain_f64_zero"] = dict(stats(r64), solves_per_s=n_inst / t64[0], cluster_size=cl64)
-    if learned:
-        t32, r32 = timed("f32", False, cl32, 1)
-        extra["f32_zero"] = dict(stats(r32), solves_per_s=n_inst / t32[0])
-        tl64, rl64 = timed("f64", True, cl64, 1)
-        extra["learned_f64"] = dict(stats(rl64), solves_per_s=n_inst / tl64[0])
-    extra["speedup_vs_plain_f64"] = (n_inst / sec) / extra["plain_f64_zero"]["solves_per_s"]
+    extra["main"] = dict(stats(res), jacobian="f32", init=main["init"], exact_jacobian=main["cb"].exact_jacobian,
+                         forcing_max=main["forcing"], **main["tune"])
+    # the plain FP64 method from zero, and ablations, on the same instances (one warm-up and one timed solve each)
+    ablations = [("plain_f64", setting(cb_plain, "f64", "zero", 0.0)),
+                 ("f64_exact_forcing", setting(cb_fast, "f64", "zero", FAST_FORCING))]
+    if not learned:
+        ablations += [("f32_exact_forcing", setting(cb_fast, "f32", "zero", FAST_FORCING))]
+    else:
+        ablations += [("f32_plain_newton", setting(cb_plain, "f32", "zero", 0.0))]
+        ablations += [("f32_exact_forcing_zero_init", setting(cb_fast, "f32", "zero", FAST_FORCING)),
+                      ("learned_f32_plain_newton", setting(cb_plain, "f32", "learned", 0.0)),
+                      ("learned_f64_exact_forcing", setting(cb_fast, "f64", "learned", FAST_FORCING))]
+    for name, st in ablations:
+        solve_once(st)
+        t1, r1 = timed(st, 1)
+        extra[name] = dict(stats(r1), solves_per_s=n_inst / t1[0], **st["tune"])
+    extra["speedup_vs_plain_f64"] = (n_inst / sec) / extra["plain_f64"]["solves_per_s"]
 
     # FP64-oracle defect of every instance's final iterate (rank 0, one solve of the main path)
-    u, res = solve_once(prec_main, learned, cl32)
+    u, res = solve_once(main)
     U = u.cpu().numpy()
     if rank == 0 and not args.no_cpu_baseline:
         import oracle
 
         worst = 0.0
-        offs = cb.node_offsets
+        offs = main["cb"].node_offsets
         for i in range(n_inst):
             roid, X, C = mesh.structured_quads(int(N[i]))
             dofs, vals = mesh.cavity_dirichlet(X, float(lid[i]))
@@ -503,16 +527,17 @@ def run_solves(args):
         extra["oracle_rel_defect_max"] = worst
 
     # e2e through the public API with host buffers: H2D of the initial iterate, D2H of the solutions
+    cb = main["cb"]
     hu0 = torch.zeros(cb.n_nodes * 3, dtype=torch.float64).pin_memory()
     hu = torch.empty_like(hu0).pin_memory()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    cb.cluster_size = cl32
     ud = hu0.to(dev, non_blocking=True)
     if learned:
         cb.predict(model, ud)
-    cb.solve(ud, prec_main, zero_fallback=learned)
+    cb.cluster_size, cb.smooth_steps, cb.coarse_steps = main["tune"]["cluster_size"], main["tune"]["smooth_steps"], main["tune"]["coarse_steps"]
+    cb.solve(ud, "f32", zero_fallback=learned, forcing_max=main["forcing"])
     hu.copy_(ud, non_blocking=True)
     e1.record()
     e1.synchronize()
@@ -529,7 +554,8 @@ def run_solves(args):
         line = {"metric": "solves/s to rel defect 1e-8", "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * sec, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64 defect / f32 jacobian", "data": "synthetic (seeded cavity draws)",
-                "config": {"workload": wl, "instances": total_inst, "l2": "inputs larger than L2 (" + str(cb.n_nodes) + " nodes)", **extra},
+                "config": {"workload": wl, "instances": total_inst, "l2": "inputs larger than L2 (" + str(cb.n_nodes) + " nodes)",
+                           "target": "||d_i|| <= 1e-8 ||d_i(zero iterate)|| per instance", **extra},
                 "e2e": {"value": n_inst * world / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": hu0.numel() * 8,
                         "d2h_bytes_per_step": hu.numel() * 8},
                 "roofline": None, "cpu_baseline": cpu, "gpu_launches": None, "clocks": clk.summary()}
@@ -556,7 +582,7 @@ def run_transient(args):
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     rank = int(os.environ.get("RANK", "0"))
-    n_cells, n_steps, dt, nu = args.cells if args.cells != 64 else 1024, 20, 0.01, 0.001
+    n_cells, n_steps, dt, nu = args.cells if args.cells != 64 else 1024, args.time_steps, 0.01, 0.001
     wl = (f"{n_cells}^2 jittered grid (+-0.2h, seed 2) split into {2 * n_cells * n_cells} triangles, backward Euler dt={dt} x {n_steps}, "
           f"nu={nu}, full upwind + FIELDS, lid-driven cavity walls")
     roid, X, C = mesh.jittered_triangles(n_cells, seed=2)

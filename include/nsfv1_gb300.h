@@ -232,6 +232,8 @@ typedef struct {
                          /*    [p->lin_rtol, forcing_max]; 0: p->lin_rtol throughout                   */
     int graph;           /* 1: each step's fixed device work (Jacobians on all levels, block         */
                          /*    inverses, the GMRES launch) replays one captured CUDA graph            */
+    int tail_clusters;   /* 1: while active instances x cluster_size leave SMs idle, the step uses    */
+                         /*    clusters of 2x, 4x ... (at most 16 CTAs) for the remaining instances   */
 } nsfv1_batch_options;
 
 /* Newton on every instance at once (each to its own ||d_i|| <= rtol ||d_i,0||):
@@ -298,6 +300,16 @@ int nsfv1_mlp_predict(nsfv1_mlp* m, int64_t n_points, const float* xy, int n_slo
 int nsfv1_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* C, int splits, void* stream);
 /* the number of K chunks nsfv1_gemm_bf16 uses for K and a requested split count */
 int nsfv1_gemm_bf16_splits(int K, int splits);
+
+/* CTA size of the assembly colour launches (32, 64, 96 or 128; default 32):
+ * the element kernels use up to 255 registers per thread, so small CTAs
+ * spread each colour evenly over the SMs. (No reference counterpart.) */
+int nsfv1_set_assembly_threads(nsfv1_disc* h, int threads);
+int nsfv1_get_assembly_threads(const nsfv1_disc* h);
+/* Assembly autotuner: times one defect + Jacobian assembly at u (device) for
+ * every candidate CTA size, in precision prec, and keeps the fastest;
+ * ms[n_candidates] (host, may be NULL) receives the second pass's times. */
+int nsfv1_assembly_autotune(nsfv1_disc* h, const double* u, int prec, const int* candidates, int n_candidates, double* ms, void* stream);
 
 /* Autotuner of the batched solve: times one Newton step from u (u is not
  * changed) for every candidate cluster size (CTAs per instance) and writes the

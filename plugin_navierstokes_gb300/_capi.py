@@ -59,7 +59,7 @@ class NewtonResult(ctypes.Structure):
 class BatchOptions(ctypes.Structure):
     _fields_ = [("cluster_size", c_int), ("max_clusters", c_int), ("mg_levels", c_int), ("smooth_steps", c_int),
                 ("coarse_steps", c_int), ("smooth_omega", c_double), ("defect_reference", c_int), ("zero_fallback", c_int),
-                ("forcing_max", c_double), ("graph", c_int)]
+                ("forcing_max", c_double), ("graph", c_int), ("tail_clusters", c_int)]
 
 
 class MlpConfig(ctypes.Structure):
@@ -119,6 +119,9 @@ _SIGS = {
     "nsfv1_set_instance_grids": (c_int, [c_void_p, c_void_p]),
     "nsfv1_newton_solve_batched": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(BatchOptions),
                                            c_void_p, c_void_p]),
+    "nsfv1_set_assembly_threads": (c_int, [c_void_p, c_int]),
+    "nsfv1_get_assembly_threads": (c_int, [c_void_p]),
+    "nsfv1_assembly_autotune": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
     "nsfv1_batch_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(BatchOptions), c_void_p,
                                      c_int, c_void_p, c_void_p]),
     "nsfv1_ref_tables": (c_int, [c_int, POINTER(c_int), POINTER(c_int), c_void_p, POINTER(c_int), c_void_p, c_void_p, c_void_p]),

@@ -306,22 +306,29 @@ static cudaError_t dispatch_roid(int roid, F&& f) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_defect(int roid, const DiscParams& P, const AsmArgs& a, cudaStream_t s) {
+// The element kernels hold up to 255 registers per thread, so an SM runs only
+// a few CTAs of a colour at once; small CTAs spread a colour evenly over the
+// 152 SMs (the block size is a per-handle parameter picked by the autotuner).
+static int clamp_threads(int t) { return (t >= 32 && t <= kThreads && t % 32 == 0) ? t : kThreads; }
+
+cudaError_t launch_defect(int roid, const DiscParams& P, const AsmArgs& a, cudaStream_t s, int threads) {
     if (a.count <= 0) return cudaSuccess;
-    const int grid = (a.count + kThreads - 1) / kThreads;
+    const int t = clamp_threads(threads);
+    const int grid = (a.count + t - 1) / t;
     return dispatch_roid(roid, [&](auto r) {
-        if (P.transient) k_defect<decltype(r)::value, true><<<grid, kThreads, 0, s>>>(P, a);
-        else k_defect<decltype(r)::value, false><<<grid, kThreads, 0, s>>>(P, a);
+        if (P.transient) k_defect<decltype(r)::value, true><<<grid, t, 0, s>>>(P, a);
+        else k_defect<decltype(r)::value, false><<<grid, t, 0, s>>>(P, a);
     });
 }
 
-cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s) {
+cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s, int threads) {
     if (a.count <= 0) return cudaSuccess;
-    const int grid = (a.count + kThreads - 1) / kThreads;
+    const int t = clamp_threads(threads);
+    const int grid = (a.count + t - 1) / t;
     return dispatch_roid(roid, [&](auto r) {
         constexpr int RO = decltype(r)::value;
-        if (prec == 0) k_jacobian<RO, double, double><<<grid, kThreads, 0, s>>>(P, a);
-        else k_jacobian<RO, float, float><<<grid, kThreads, 0, s>>>(P, a);
+        if (prec == 0) k_jacobian<RO, double, double><<<grid, t, 0, s>>>(P, a);
+        else k_jacobian<RO, float, float><<<grid, t, 0, s>>>(P, a);
     });
 }
 

@@ -600,7 +600,7 @@ struct BatchState {
     // CUDA graph of one Newton step's fixed device work (Jacobians, block inverses, GMRES launch)
     cudaStream_t gs = nullptr;
     cudaEvent_t evIn = nullptr, evOut = nullptr;
-    cudaGraphExec_t graph = nullptr;
+    std::vector<std::pair<int, cudaGraphExec_t>> graphs;   // one per cluster size in use
     ~BatchState() {
         clear_levels();
         drop_graph();
@@ -609,8 +609,12 @@ struct BatchState {
         if (gs) cudaStreamDestroy(gs);
     }
     void drop_graph() {
-        if (graph) cudaGraphExecDestroy(graph);
-        graph = nullptr;
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        graphs.clear();
+    }
+    cudaGraphExec_t* graph_for(int cs) {
+        for (auto& g : graphs) if (g.first == cs) return &g.second;
+        return nullptr;
     }
     void clear_levels() {
         for (auto& L : levels) L.release();
@@ -664,11 +668,25 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
             return D.status;
         W.prec = prec; W.n = n; W.m = m;
     }
-    const int clusterSize = opt.cluster_size > 0 ? opt.cluster_size : 4;
-    int nClusters = (b == 4) ? max_clusters<VT, 4>(clusterSize) : max_clusters<VT, 3>(clusterSize);
-    if (nClusters <= 0) { D.fail(NSFV1_ERR_ARGUMENT, "batched solve: cluster size not launchable"); return D.status; }
-    if (opt.max_clusters > 0) nClusters = std::min(nClusters, opt.max_clusters);
-    nClusters = std::min(nClusters, nInst);
+    const int baseCluster = opt.cluster_size > 0 ? opt.cluster_size : 4;
+    int numSMs = 0;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev);
+    }
+    // resident clusters per cluster size (computed on first use)
+    int clustersFor[17] = {0};
+    auto clusters_of = [&](int cs) {
+        if (!clustersFor[cs]) {
+            int nc = (b == 4) ? max_clusters<VT, 4>(cs) : max_clusters<VT, 3>(cs);
+            if (opt.max_clusters > 0) nc = std::min(nc, opt.max_clusters);
+            clustersFor[cs] = std::min(std::max(nc, 0), nInst);
+        }
+        return clustersFor[cs];
+    };
+    if (clusters_of(baseCluster) <= 0) { D.fail(NSFV1_ERR_ARGUMENT, "batched solve: cluster size not launchable"); return D.status; }
+    int clusterSize = baseCluster, nClusters = clusters_of(baseCluster);
     const bool useMG = opt.mg_levels != 0 && BS->levels.size() > 1;
     const bool adaptive = opt.forcing_max > 0.0;
     const bool useGraph = opt.graph != 0;
@@ -763,19 +781,23 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
                 !D.cuda_ok(cudaEventCreateWithFlags(&BS->evOut, cudaEventDisableTiming), "graph event"))
                 return false;
         }
-        if (!BS->graph) {
+        cudaGraphExec_t* ge = BS->graph_for(clusterSize);
+        if (!ge) {
             cudaGraph_t g = nullptr;
+            cudaGraphExec_t exec = nullptr;
             if (!D.cuda_ok(cudaStreamBeginCapture(BS->gs, cudaStreamCaptureModeRelaxed), "graph capture")) return false;
             const bool ok = enqueue_step(BS->gs);
             const cudaError_t ce = cudaStreamEndCapture(BS->gs, &g);
             if (!ok) { if (g) cudaGraphDestroy(g); return false; }
             if (!D.cuda_ok(ce, "graph capture")) return false;
-            const cudaError_t ie = cudaGraphInstantiate(&BS->graph, g, 0);
+            const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
             cudaGraphDestroy(g);
-            if (!D.cuda_ok(ie, "graph instantiate")) { BS->graph = nullptr; return false; }
+            if (!D.cuda_ok(ie, "graph instantiate")) return false;
+            BS->graphs.emplace_back(clusterSize, exec);
+            ge = BS->graph_for(clusterSize);
         }
         return D.cuda_ok(cudaEventRecord(BS->evIn, s), "graph event") && D.cuda_ok(cudaStreamWaitEvent(BS->gs, BS->evIn, 0), "graph event") &&
-               D.cuda_ok(cudaGraphLaunch(BS->graph, BS->gs), "graph launch") && D.cuda_ok(cudaEventRecord(BS->evOut, BS->gs), "graph event") &&
+               D.cuda_ok(cudaGraphLaunch(*ge, BS->gs), "graph launch") && D.cuda_ok(cudaEventRecord(BS->evOut, BS->gs), "graph event") &&
                D.cuda_ok(cudaStreamWaitEvent(s, BS->evOut, 0), "graph event");
     };
 
@@ -833,6 +855,12 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
         for (int i = 0; i < nInst; ++i) if (active[i]) q.push_back(i);
         std::stable_sort(q.begin(), q.end(), [&](int a, int c) { return size[a] > size[c]; });
         const int nq = (int)q.size();
+        // tail: with few active instances grow the clusters (up to 16 CTAs) so
+        // that the instances still being solved keep the SMs busy
+        clusterSize = baseCluster;
+        if (opt.tail_clusters)
+            while (clusterSize < 16 && (int64_t)nq * clusterSize * 2 <= numSMs && clusters_of(clusterSize * 2) > 0) clusterSize *= 2;
+        nClusters = clusters_of(clusterSize);
         D.instSkip = true;
         if (!upload_flags(active, D.d_instActive) ||
             !D.cuda_ok(cudaMemcpyAsync(W.queue, q.data(), q.size() * 4, cudaMemcpyHostToDevice, s), "queue") ||

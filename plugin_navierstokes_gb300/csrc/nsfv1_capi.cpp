@@ -440,6 +440,70 @@ int nsfv1_elem_batch(nsfv1_disc* h, int elem_type, int64_t n, const double* corn
     return D->check_err_word(s) ? NSFV1_OK : D->status;
 }
 
+int nsfv1_set_assembly_threads(nsfv1_disc* h, int threads) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (threads < 32 || threads > 128 || threads % 32) {
+        D->fail(NSFV1_ERR_ARGUMENT, "set_assembly_threads: 32, 64, 96 or 128");
+        return D->status;
+    }
+    D->asmThreads = threads;
+    return NSFV1_OK;
+}
+
+int nsfv1_get_assembly_threads(const nsfv1_disc* h) {
+    const Disc* D = reinterpret_cast<const Disc*>(h);
+    return D ? D->asmThreads : 0;
+}
+
+int nsfv1_assembly_autotune(nsfv1_disc* h, const double* u, int prec, const int* candidates, int n_candidates, double* ms, void* stream) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "assembly_autotune: no mesh"); return D->status; }
+    if (!u || !candidates || n_candidates <= 0 || (prec != NSFV1_F64 && prec != NSFV1_F32)) {
+        D->fail(NSFV1_ERR_ARGUMENT, "assembly_autotune: bad arguments");
+        return D->status;
+    }
+    for (int c = 0; c < n_candidates; ++c)
+        if (candidates[c] < 32 || candidates[c] > 128 || candidates[c] % 32) {
+            D->fail(NSFV1_ERR_ARGUMENT, "assembly_autotune: candidates must be 32, 64, 96 or 128");
+            return D->status;
+        }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int b = D->dim + 1;
+    const size_t vbytes = D->colIdx.size() * b * b * (prec == NSFV1_F64 ? 8 : 4);
+    void* J = nullptr;
+    double* d = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    bool ok = D->cuda_ok(cudaMalloc(&J, vbytes), "autotune scratch") && D->cuda_ok(cudaMalloc(&d, D->nNodes * b * 8), "autotune scratch") &&
+              D->cuda_ok(cudaEventCreate(&e0), "autotune") && D->cuda_ok(cudaEventCreate(&e1), "autotune");
+    const int keep = D->asmThreads;
+    std::vector<double> t(n_candidates, 0.0);
+    for (int pass = 0; ok && pass < 2; ++pass)
+        for (int c = 0; ok && c < n_candidates; ++c) {
+            D->asmThreads = candidates[c];
+            cudaEventRecord(e0, s);
+            ok = D->assemble_defect(u, nullptr, 0.0, d, s) && D->assemble_jacobian(u, nullptr, 0.0, J, prec, s, false);
+            cudaEventRecord(e1, s);
+            float msec = 0.f;
+            if (ok) ok = D->cuda_ok(cudaEventSynchronize(e1), "autotune") && D->cuda_ok(cudaEventElapsedTime(&msec, e0, e1), "autotune");
+            t[c] = msec;
+        }
+    if (J) cudaFree(J);
+    if (d) cudaFree(d);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    D->asmThreads = keep;
+    if (!ok) return D->status;
+    int best = 0;
+    for (int c = 1; c < n_candidates; ++c) if (t[c] < t[best]) best = c;
+    D->asmThreads = candidates[best];
+    if (ms) for (int c = 0; c < n_candidates; ++c) ms[c] = t[c];
+    return NSFV1_OK;
+}
+
 int nsfv1_ref_tables(int elem_type, int* nco, int* nedge, int* edges, int* nside, int* side_nco, int* sides, int* edge_face) {
     auto fill = [&](auto r) {
         using R = Ref<decltype(r)::value>;
@@ -480,7 +544,7 @@ bool Disc::assemble_defect(const double* u, const double* u_old, double dt, doub
     for (int c = 0; c < nColors; ++c) {
         AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, d, nullptr,
                   d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive};
-        if (!cuda_ok(launch_defect(roid, P, a, s), "defect kernel")) return false;
+        if (!cuda_ok(launch_defect(roid, P, a, s, asmThreads), "defect kernel")) return false;
     }
     if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, d, nullptr, 0, s), "dirichlet")) return false;
     return check_err_word(s);
@@ -498,7 +562,7 @@ bool Disc::assemble_jacobian(const double* u, const double* u_old, double dt, vo
     for (int c = 0; c < nColors; ++c) {
         AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, nullptr, vals,
                   d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive};
-        if (!cuda_ok(launch_jacobian(roid, P, a, prec, s), "jacobian kernel")) return false;
+        if (!cuda_ok(launch_jacobian(roid, P, a, prec, s, asmThreads), "jacobian kernel")) return false;
     }
     if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, nullptr, vals, prec, s), "dirichlet")) return false;
     return sync ? check_err_word(s) : true;

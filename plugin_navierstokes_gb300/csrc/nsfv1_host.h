@@ -61,6 +61,7 @@ struct Disc {
     double* d_dirVal = nullptr;
     int64_t nDir = 0;
     int* d_err = nullptr;
+    int asmThreads = 32;            // CTA size of the assembly colour launches
 
     Workspace ws;
     void* batch = nullptr;   // workspace of the batched solver

@@ -204,21 +204,22 @@ class NavierStokesFV1:
                              jacobian_prec: str = "f64", gmres_restart: int = 30, cluster_size: int = 4, max_clusters: int = 0,
                              multigrid: bool = True, smooth_steps: int = 2, coarse_steps: int = 20, smooth_omega: float = 0.7,
                              defect_reference: str = "initial", zero_fallback: bool = False, forcing_max: float = 0.0,
-                             graph: bool = True, stream=None, raise_on_error: bool = True) -> list[dict]:
+                             graph: bool = True, tail_clusters: bool = True, stream=None, raise_on_error: bool = True) -> list[dict]:
         """Newton on every instance (nsfv1_newton_solve_batched). ``defect_reference``
         "initial" measures rtol against each instance's own initial defect, "zero"
         against the defect of the zero iterate; with "zero", ``zero_fallback``
         restarts from the zero iterate every instance whose given iterate has the
         larger defect. ``forcing_max`` > 0 switches on Eisenstat-Walker linear
         tolerances in [lin_rtol, forcing_max]; ``graph`` replays each step's fixed
-        device work as one captured CUDA graph."""
+        device work as one captured CUDA graph (one per cluster size); ``tail_clusters``
+        grows the clusters of the remaining instances once few are active."""
         if defect_reference not in ("initial", "zero"):
             raise NSFV1Error(_capi.ERR_ARGUMENT, f"unknown defect reference '{defect_reference}'")
         p = _capi.NewtonParams(rtol, atol, max_iter, lin_rtol, lin_max_iter, line_search_steps,
                                _capi.F64 if jacobian_prec == "f64" else _capi.F32, _capi.GMRES, gmres_restart)
         o = _capi.BatchOptions(cluster_size, max_clusters, 1 if multigrid else 0, smooth_steps, coarse_steps, smooth_omega,
                                1 if defect_reference == "zero" else 0, 1 if zero_fallback else 0, float(forcing_max),
-                               1 if graph else 0)
+                               1 if graph else 0, 1 if tail_clusters else 0)
         res = (_capi.NewtonResult * self.n_inst)()
         st = self._lib.nsfv1_newton_solve_batched(self._h, _ptr(u), _ptr(u_old), float(dt), ctypes.byref(p), ctypes.byref(o),
                                                   ctypes.addressof(res), _stream_ptr(stream))
@@ -228,14 +229,32 @@ class NavierStokesFV1:
             raise NSFV1Error(st, self._lib.nsfv1_last_error(self._h).decode())
         return out
 
+    def set_assembly_threads(self, threads: int) -> None:
+        """CTA size of the assembly colour launches (32, 64, 96 or 128)."""
+        self._c(self._lib.nsfv1_set_assembly_threads(self._h, int(threads)))
+
+    def assembly_threads(self) -> int:
+        return int(self._lib.nsfv1_get_assembly_threads(self._h))
+
+    def assembly_autotune(self, u, jacobian_prec: str = "f64", candidates=(32, 64, 128), stream=None) -> tuple[int, list[float]]:
+        """Times defect + Jacobian assembly at u per CTA size (nsfv1_assembly_autotune) and
+        keeps the fastest; returns (CTA size, milliseconds per candidate)."""
+        c = np.ascontiguousarray(candidates, dtype=np.int32)
+        ms = np.zeros(c.size)
+        self._c(self._lib.nsfv1_assembly_autotune(self._h, _ptr(u), _capi.F64 if jacobian_prec == "f64" else _capi.F32,
+                                                  c.ctypes.data, c.size, ms.ctypes.data, _stream_ptr(stream)))
+        return self.assembly_threads(), [float(x) for x in ms]
+
     def batch_autotune(self, u, u_old=None, dt: float = 0.0, candidates=(2, 4, 8, 16), jacobian_prec: str = "f32",
                        lin_rtol: float = 1e-3, lin_max_iter: int = 400, gmres_restart: int = 30, multigrid: bool = True,
+                       smooth_steps: int = 2, coarse_steps: int = 20, smooth_omega: float = 0.7,
                        forcing_max: float = 0.0, graph: bool = True, stream=None) -> tuple[int, list[float]]:
         """Times one batched Newton step per candidate cluster size (nsfv1_batch_autotune);
         returns (fastest cluster size, milliseconds per candidate). u is not changed."""
         p = _capi.NewtonParams(1e-8, 0.0, 1, lin_rtol, lin_max_iter, 6, _capi.F64 if jacobian_prec == "f64" else _capi.F32,
                                _capi.GMRES, gmres_restart)
-        o = _capi.BatchOptions(0, 0, 1 if multigrid else 0, 2, 20, 0.7, 0, 0, float(forcing_max), 1 if graph else 0)
+        o = _capi.BatchOptions(0, 0, 1 if multigrid else 0, smooth_steps, coarse_steps, smooth_omega, 0, 0, float(forcing_max),
+                               1 if graph else 0, 0)
         c = np.ascontiguousarray(candidates, dtype=np.int32)
         ms = np.zeros(c.size)
         self._c(self._lib.nsfv1_batch_autotune(self._h, _ptr(u), _ptr(u_old), float(dt), ctypes.byref(p), ctypes.byref(o),

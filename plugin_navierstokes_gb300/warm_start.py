@@ -145,7 +145,7 @@ class CavityBatch:
     the batched workload) set up on one NavierStokesFV1 handle: per-element
     viscosity nu = lid / Re, instance ranges, multigrid hierarchy."""
 
-    def __init__(self, N, Re, lid, upwind: str = "full", stabilization: str = "flow"):
+    def __init__(self, N, Re, lid, upwind: str = "full", stabilization: str = "flow", exact_jacobian: float = 0.0):
         import torch
 
         from . import mesh
@@ -159,6 +159,7 @@ class CavityBatch:
         d.set_kinematic_viscosity(1.0)
         d.set_upwind(upwind)
         d.set_stabilization(stabilization)
+        d.set_exact_jacobian(exact_jacobian)
         d.set_mesh(B["elem_type"], B["coords"], B["conn"])
         d.set_elem_viscosity(B["nu_elem"])
         d.set_instances(B["node_offsets"])
@@ -169,17 +170,22 @@ class CavityBatch:
         self.n_nodes = int(B["coords"].shape[0])
         self.xy = torch.from_numpy(B["coords"].astype(np.float32)).cuda()
         self.cond = np.stack([condition(r, l) for r, l in zip(self.Re, self.lid)])
-        self.cluster_size = 8
+        self.exact_jacobian = float(exact_jacobian)
+        self.cluster_size, self.smooth_steps, self.coarse_steps = 8, 2, 20
 
-    def autotune(self, jacobian_prec: str = "f32", candidates=(2, 4, 8, 16), cache_file: str | None = None, **kw) -> int:
-        """Picks the cluster size (CTAs per instance) of this batch by timing one
-        Newton step per candidate (nsfv1_batch_autotune); the choice is cached in
-        a JSON file keyed by device, precision and the multiset of mesh sizes
-        (default ~/.cache/nsfv1_gb300/autotune.json, or $NSFV1_AUTOTUNE_CACHE)."""
+    def autotune(self, jacobian_prec: str = "f32", candidates=(4, 8, 16), smoothing=((2, 20), (3, 20), (2, 40), (3, 40)),
+                 forcing_max: float = 0.0, cache_file: str | None = None) -> dict:
+        """Picks the cluster size (CTAs per instance) and the V-cycle smoothing
+        (pre/post sweeps, coarsest-level sweeps) of this batch by timing one
+        Newton step per combination (nsfv1_batch_autotune per smoothing choice);
+        the choice is cached in a JSON file keyed by device, precision, Newton
+        options and the multiset of mesh sizes (default
+        ~/.cache/nsfv1_gb300/autotune.json, or $NSFV1_AUTOTUNE_CACHE)."""
         import torch
 
         path = Path(cache_file or os.environ.get("NSFV1_AUTOTUNE_CACHE", Path.home() / ".cache" / "nsfv1_gb300" / "autotune.json"))
-        key = "|".join([torch.cuda.get_device_name(), jacobian_prec, ",".join(map(str, candidates)),
+        key = "|".join([torch.cuda.get_device_name(), jacobian_prec, f"exact={self.exact_jacobian}", f"forcing={forcing_max}",
+                        ",".join(map(str, candidates)), ",".join(f"{a}/{b}" for a, b in smoothing),
                         ",".join(f"{n}x{c}" for n, c in sorted(Counter(self.N.tolist()).items()))])
         cache = {}
         if path.exists():
@@ -187,18 +193,24 @@ class CavityBatch:
                 cache = json.loads(path.read_text())
             except (OSError, ValueError):
                 cache = {}
-        if key in cache:
-            self.cluster_size = int(cache[key]["cluster_size"])
-            return self.cluster_size
-        best, ms = self.disc.batch_autotune(self.zeros(), candidates=candidates, jacobian_prec=jacobian_prec, **kw)
-        self.cluster_size = best
-        cache[key] = {"cluster_size": best, "ms": dict(zip(map(str, candidates), ms))}
-        try:
-            path.parent.mkdir(parents=True, exist_ok=True)
-            path.write_text(json.dumps(cache, indent=1))
-        except OSError:
-            pass
-        return best
+        if key not in cache:
+            u = self.zeros()
+            trials = []
+            for sm, co in smoothing:
+                # timed with the fixed linear tolerance: a loose first adaptive step would hide the cost of later ones
+                best, ms = self.disc.batch_autotune(u, candidates=candidates, jacobian_prec=jacobian_prec, smooth_steps=sm,
+                                                    coarse_steps=co, forcing_max=0.0)
+                trials.append((min(ms), best, sm, co))
+            t, best, sm, co = min(trials)
+            cache[key] = {"cluster_size": best, "smooth_steps": sm, "coarse_steps": co, "ms": t}
+            try:
+                path.parent.mkdir(parents=True, exist_ok=True)
+                path.write_text(json.dumps(cache, indent=1))
+            except OSError:
+                pass
+        c = cache[key]
+        self.cluster_size, self.smooth_steps, self.coarse_steps = int(c["cluster_size"]), int(c["smooth_steps"]), int(c["coarse_steps"])
+        return dict(c)
 
     @property
     def n_inst(self) -> int:
@@ -218,7 +230,8 @@ class CavityBatch:
     def solve(self, u, jacobian_prec: str = "f32", rtol: float = 1e-8, defect_reference: str = "zero",
               zero_fallback: bool = False, **kw):
         """Batched Newton from u (in place); returns the per-instance results."""
-        opts = dict(lin_rtol=1e-3, lin_max_iter=400, max_iter=80, cluster_size=self.cluster_size, raise_on_error=False)
+        opts = dict(lin_rtol=1e-3, lin_max_iter=400, max_iter=80, cluster_size=self.cluster_size, smooth_steps=self.smooth_steps,
+                    coarse_steps=self.coarse_steps, raise_on_error=False)
         opts.update(kw)
         return self.disc.newton_solve_batched(u, rtol=rtol, jacobian_prec=jacobian_prec, defect_reference=defect_reference,
                                               zero_fallback=zero_fallback, **opts)

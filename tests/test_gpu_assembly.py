@@ -191,3 +191,29 @@ def test_block_jacobi_matches_numpy(cuda, gen):
     diag = np.array([Jh[rp[i] + np.searchsorted(ci[rp[i]:rp[i + 1]], i)] for i in range(X.shape[0])])
     zref = np.einsum("nij,nj->ni", np.linalg.inv(diag), r.cpu().numpy().reshape(-1, b)).ravel()
     assert rel_err(z.cpu().numpy(), zref) <= TOL64
+
+
+def test_assembly_cta_size_is_bitwise_neutral_and_autotuned(cuda):
+    """The colour scatter is order-free, so the assembly CTA size changes no bit;
+    the assembly autotuner keeps one of its candidates."""
+    import torch
+    from plugin_navierstokes_gb300 import NavierStokesFV1, mesh
+    roid, X, C = mesh.structured_hexes(6)
+    U = mesh.solenoidal_state(X, seed=1)
+    d = NavierStokesFV1("u,v,w,p", "Inner")
+    d.set_kinematic_viscosity(0.0025); d.set_upwind("lps"); d.set_stabilization("flow")
+    d.set_mesh(roid, X, C)
+    nnzb = d.pattern_info()["nnz_blocks"]
+    tu = torch.tensor(U.ravel(), dtype=torch.float64, device=cuda)
+    out = []
+    for t in (32, 64, 96, 128):
+        d.set_assembly_threads(t)
+        D = torch.empty_like(tu)
+        J = torch.empty(nnzb * 16, dtype=torch.float64, device=cuda)
+        d.assemble_defect(tu, D)
+        d.assemble_jacobian(tu, J)
+        out.append((D, J))
+    for D, J in out[1:]:
+        assert torch.equal(D, out[0][0]) and torch.equal(J, out[0][1])
+    best, ms = d.assembly_autotune(tu, "f64", (32, 64, 128))
+    assert best in (32, 64, 128) and len(ms) == 3 and ms[(32, 64, 128).index(best)] == min(ms)

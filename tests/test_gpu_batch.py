@@ -170,3 +170,31 @@ def test_autotune_picks_a_candidate(cuda):
     assert best in (2, 4, 8) and len(ms) == 3 and all(t > 0 for t in ms)
     assert ms[(2, 4, 8).index(best)] == min(ms)
     assert torch.count_nonzero(u) == 0   # the iterate is untouched
+
+
+def test_exact_jacobian_with_forcing_meets_the_oracle_target(cuda):
+    """The fast path of the batched workload (exact-Jacobian factor 1, adaptive
+    linear tolerances up to 0.3, FP32 Jacobian): every instance reaches the FP64
+    oracle defect target of the plain discretisation."""
+    import torch
+    sizes = [16, 32, 24, 40]
+    Re, lid = [200.0, 1000.0, 50.0, 700.0], [1.0, 1.5, 2.0, 0.6]
+    B = mesh.cavity_batch(sizes, Re, lid)
+    d = NavierStokesFV1("u,v,p", "Inner")
+    d.set_kinematic_viscosity(1.0); d.set_upwind("full"); d.set_stabilization("flow"); d.set_exact_jacobian(1.0)
+    d.set_mesh(B["elem_type"], B["coords"], B["conn"]); d.set_elem_viscosity(B["nu_elem"])
+    d.set_instances(B["node_offsets"]); d.set_dirichlet(B["dofs"], B["values"]); d.set_instance_grids(sizes)
+    u = torch.zeros(B["coords"].shape[0] * 3, dtype=torch.float64, device=cuda)
+    res = d.newton_solve_batched(u, rtol=1e-8, lin_rtol=1e-3, jacobian_prec="f32", forcing_max=0.3, max_iter=80,
+                                 defect_reference="zero", smooth_steps=3, coarse_steps=40)
+    U = u.cpu().numpy()
+    offs = B["node_offsets"]
+    for i, (N, re, u0) in enumerate(zip(sizes, Re, lid)):
+        assert res[i]["status"] == 0, (i, res[i])
+        roid, X, C = mesh.structured_quads(N)
+        dofs, vals = mesh.cavity_dirichlet(X, u0)
+        o = oracle.Oracle(2); o.set_kinematic_viscosity(u0 / re); o.set_upwind("full"); o.set_stabilization("flow")
+        o.set_mesh(roid, X, C); o.set_dirichlet(dofs, vals)
+        D, _ = o.assemble(U[offs[i] * 3:offs[i + 1] * 3], jacobian=False)
+        D0, _ = o.assemble(_dir(U[offs[i] * 3:offs[i + 1] * 3].size, dofs, vals), jacobian=False)
+        assert np.linalg.norm(D) <= 1.01e-8 * np.linalg.norm(D0), (i, res[i])

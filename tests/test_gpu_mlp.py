@@ -21,7 +21,7 @@ def _bf16_pair(torch, cuda, M, N, K, seed):
 
 
 @pytest.mark.parametrize("M,N,K,splits", [(128, 256, 64, 1), (256, 64, 1024, 4), (384, 128, 192, 1), (256, 256, 4096, 8),
-                                          (512, 512, 256, 1), (128, 64, 640, 3)])
+                                          (512, 512, 256, 1), (128, 64, 640, 3), (65536, 256, 256, 1)])
 def test_gemm_bf16_matches_float64(cuda, M, N, K, splits):
     import torch
 
