@@ -23,6 +23,9 @@ Two more workloads print their own line (not the default run):
                     step one Newton solve to 1e-6 relative (FP32 Jacobian and block inverses,
                     block-Jacobi BiCGStab to 1e-4 with FP64 Krylov vectors, FP64 defect /
                     update / line search); the all-FP64 run beside it.
+--workload cavity   the plain method on one 64^2 lid-driven cavity (nu 0.01, zero initial guess,
+                    Newton to 1e-8); full upwind with FLOW: with FIELDS the 64^2 cavity enters a
+                    period-2 upwind cycle at 9.8e-4 and never reaches 1e-8 (same in the oracle).
 --workload learned  the warm-start MLP trained on 2048 solves of 128^2 cavities (seed 4),
                     then 256 held-out draws (seed 5); one step = the held-out batch solved
                     from the network's iterate (FP32 Jacobian), plain FP64 from zero beside.
@@ -159,7 +162,7 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="assembly", choices=["assembly", "batched", "learned", "transient"])
+    ap.add_argument("--workload", default="assembly", choices=["assembly", "batched", "learned", "transient", "cavity"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cells", type=int, default=64, help="assembly workload: cells per side (64 is the benchmark; smaller for profiling)")
     ap.add_argument("--time-steps", type=int, default=20, help="transient workload: backward-Euler steps (20 is the benchmark)")
@@ -170,6 +173,8 @@ def main():
         args.steps = 10 if args.workload == "assembly" else 3
     if args.workload == "transient":
         return run_transient(args)
+    if args.workload == "cavity":
+        return run_cavity(args)
     if args.workload != "assembly":
         return run_solves(args)
     if args.impl == "reference":
@@ -318,7 +323,10 @@ def main():
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
             "roofline": {"bound": "hbm", "kernel": "FP64 Jacobian assembly (8 colour launches)", "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "algorithmic_bytes": alg_bytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+                         "traffic_gbs": (traffic / (jac_ms * 1e-3) / 1e9) if traffic else None,
+                         "algorithmic_bytes": alg_bytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
+                         "note": "FP64-pipe bound (ncu: FP64 pipe ~70% of active cycles); traffic = ncu DRAM bytes of one "
+                                 "assembly (profiles/traffic.json): each colour re-streams the Jacobian lines it updates"},
             "cpu_baseline": cpu,
             "gpu_launches": 16 * args.steps,
             "clocks": clk.summary(),
@@ -682,6 +690,125 @@ def run_transient(args):
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": hu.numel() * 8 / n_steps,
                     "d2h_bytes_per_step": hout.numel() * 8 / n_steps},
             "roofline": None, "cpu_baseline": None, "gpu_launches": None, "clocks": clk.summary()}
+    print(json.dumps(line))
+    return 0
+
+
+def run_cavity(args):
+    """The plain method on one 64^2 cavity: single-instance FP64 Newton with block-Jacobi
+    BiCGStab (the reference's solver setup restated), and the batched solver on the same
+    single instance (multigrid-preconditioned GMRES); the CPU oracle Newton beside it."""
+    import numpy as np
+    import torch
+
+    from plugin_navierstokes_gb300 import NavierStokesFV1, build, mesh
+
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    n, nu = 64, 0.01
+    wl = f"{n}^2 lid-driven cavity (quads), nu={nu}, lid 1, full upwind + FLOW, zero initial guess, Newton to rel defect 1e-8"
+    roid, X, C = mesh.structured_quads(n)
+    dofs, vals = mesh.cavity_dirichlet(X, 1.0)
+
+    def oracle_solve():
+        import oracle
+
+        o = oracle.Oracle(2)
+        o.set_kinematic_viscosity(nu)
+        o.set_upwind("full")
+        o.set_stabilization("flow")
+        o.set_mesh(roid, X, C)
+        o.set_dirichlet(dofs, vals)
+        t0 = time.perf_counter()
+        U, st = o.newton(np.zeros(X.shape[0] * 3), rtol=1e-8, maxit=100, lin_rtol=1e-3, lin_maxit=20000)
+        return time.perf_counter() - t0, st
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        el, st = oracle_solve()
+        line = {"impl": "reference", "metric": "solves/s to rel defect 1e-8", "value": 1.0 / el, "unit": "solves/s", "n_gpus": args.gpus,
+                "steps": 1, "warmup": 0, "ms_per_step": 1e3 * el, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": {"workload": wl, "newton_its": st["iterations"]},
+                "cpu_baseline": {"value": 1.0 / el, "unit": "solves/s", "cores": 1, "kind": "port", "sample": "one full solve, serial oracle"},
+                "e2e": {"value": 1.0 / el, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    build.build()
+    d = NavierStokesFV1("u,v,p", "Inner")
+    d.set_kinematic_viscosity(nu)
+    d.set_upwind("full")
+    d.set_stabilization("flow")
+    d.set_mesh(roid, X, C)
+    d.set_dirichlet(dofs, vals)
+    nn = X.shape[0] * 3
+
+    def single():
+        u = torch.zeros(nn, dtype=torch.float64, device=dev)
+        return d.newton_solve(u, rtol=1e-8, lin_rtol=1e-3, lin_max_iter=5000, jacobian_prec="f64", linear_solver="bicgstab")
+
+    def timed(fn, k):
+        ts, r = [], None
+        for _ in range(k):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = fn()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return sum(ts) / len(ts), r
+
+    for _ in range(args.warmup):
+        single()
+    with ClockSampler(local) as clk:
+        sec, r = timed(single, args.steps)
+    # the batched solver on the single instance (multigrid GMRES, one persistent launch per step)
+    from plugin_navierstokes_gb300.warm_start import CavityBatch
+
+    cb = CavityBatch([n], [1.0 / nu], [1.0])
+    cb.cluster_size = 16
+
+    def batched(prec):
+        u = cb.zeros()
+        return cb.solve(u, prec, defect_reference="initial")
+
+    batched("f64")
+    sec_b64, rb64 = timed(lambda: batched("f64"), args.steps)
+    batched("f32")
+    sec_b32, rb32 = timed(lambda: batched("f32"), args.steps)
+    # e2e: host zero iterate in, solution out, through the public API
+    hu = torch.zeros(nn, dtype=torch.float64).pin_memory()
+    ho = torch.empty_like(hu).pin_memory()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    u = hu.to(dev, non_blocking=True)
+    ub = cb.zeros()
+    ub.copy_(u)
+    cb.solve(ub, "f64", defect_reference="initial")
+    ho.copy_(ub, non_blocking=True)
+    e1.record()
+    e1.synchronize()
+    e2e = 1.0 / (e0.elapsed_time(e1) * 1e-3)
+    cpu = None
+    if not args.no_cpu_baseline:
+        el, st = oracle_solve()
+        cpu = {"value": 1.0 / el, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"one full solve, serial oracle Newton ({st['iterations']} steps, {el:.1f} s)"}
+    # value: the plain method (FP64 Jacobian) through the multigrid-preconditioned solver; the
+    # block-Jacobi BiCGStab Newton and the FP32-Jacobian variant beside it
+    line = {"metric": "solves/s to rel defect 1e-8", "value": 1.0 / sec_b64, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sec_b64, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": {"workload": wl, "solver": "Newton + GMRES(30) with the geometric V-cycle",
+                                                           "newton_its": rb64[0]["iterations"], "linear_its": rb64[0]["linear_iterations"],
+                                                           "bicgstab_block_jacobi_f64": {"solves_per_s": 1.0 / sec, "newton_its": r["iterations"],
+                                                                                         "linear_its": r["linear_iterations"]},
+                                                           "fp32_jacobian": {"solves_per_s": 1.0 / sec_b32, "newton_its": rb32[0]["iterations"]}},
+            "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": hu.numel() * 8, "d2h_bytes_per_step": ho.numel() * 8},
+            "roofline": None, "cpu_baseline": cpu, "gpu_launches": None, "clocks": clk.summary()}
     print(json.dumps(line))
     return 0
 

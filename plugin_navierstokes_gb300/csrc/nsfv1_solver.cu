@@ -279,19 +279,20 @@ __global__ void k_bicg_beta(const double* partials, int nb, double* S) {
     if (threadIdx.x == 0) {
         S[S_RHO1] = v[0];
         double beta = (v[0] / S[S_RHO]) * (S[S_ALPHA] / S[S_OMEGA]);
-        // (near) breakdown: rho1 negligible against ||r0|| ||r||, or a non-finite beta
-        if (!(fabs(v[0]) > 1e-14 * sqrt(S[S_NR02] * S[S_NR2])) || !(fabs(beta) < 1e10)) { S[S_FLAG] = 1.0; beta = 0.0; }
+        // breakdown: rho1 = 0 or a non-finite beta (relative thresholds restart far too often
+        // on the convection-dominated systems, where a large beta is ordinary)
+        if (v[0] == 0.0 || !isfinite(beta)) { S[S_FLAG] = 1.0; beta = 0.0; }
         S[S_BETA] = beta;
     }
 }
-// alpha = rho1 / (r0, v); near breakdown when (r0, v) is negligible against ||r0|| ||v||
+// alpha = rho1 / (r0, v); breakdown when (r0, v) = 0 or alpha is not finite
 __global__ void k_bicg_alpha(const double* partials, int nb, double* S) {
-    double v[2];
-    block_sum_partials<2>(partials, nb, v);
+    double v[1];
+    block_sum_partials<1>(partials, nb, v);
     if (threadIdx.x == 0) {
         S[S_R0V] = v[0];
         double alpha = (v[0] != 0.0) ? S[S_RHO1] / v[0] : 0.0;
-        if (!(fabs(v[0]) > 1e-12 * sqrt(S[S_NR02] * v[1])) || !isfinite(alpha)) { S[S_FLAG] = 1.0; alpha = 0.0; }
+        if (v[0] == 0.0 || !isfinite(alpha)) { S[S_FLAG] = 1.0; alpha = 0.0; }
         S[S_ALPHA] = alpha;
     }
 }
@@ -544,7 +545,7 @@ static int bicgstab(Disc& D, const MT* J, const MT* Dinv, const double* rhs, dou
         k_bicg_p<VT><<<g, 256, 0, s>>>(n, S, r, v, p);
         prec_apply<MT, VT>(D, Dinv, p, ph, s);
         spmv<MT, VT>(D, J, ph, v, s);
-        { const VT* a[2] = {r0, v}; const VT* c[2] = {v, v}; dots<VT, 2>(n, a, c, W.red, s); }
+        { const VT* a[1] = {r0}; const VT* c[1] = {v}; dots<VT, 1>(n, a, c, W.red, s); }
         k_bicg_alpha<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
         k_bicg_s<VT><<<g, 256, 0, s>>>(n, S, r, v, sv);
         prec_apply<MT, VT>(D, Dinv, sv, shv, s);
@@ -560,9 +561,9 @@ static int bicgstab(Disc& D, const MT* J, const MT* Dinv, const double* rhs, dou
         *relres = nr / nr0;
         if (!std::isfinite(nr)) return -1;   // hard failure: x is not usable
         if (*relres < rtol) return it;
-        // (near) breakdown (rho1 or (r0, v) negligible, omega = 0): restart with
-        // the current residual as the shadow vector; after too many restarts
-        // stop with the last finite iterate and let the Newton line search judge it
+        // breakdown (rho1 = 0, (r0, v) = 0, a non-finite coefficient, omega = 0): restart
+        // with the current residual as the shadow vector; after too many restarts stop
+        // with the last finite iterate and let the Newton line search judge it
         if (W.hscal[S_FLAG] != 0.0 || W.hscal[S_OMEGA] == 0.0) {
             if (++restarts > kMaxBicgRestarts) return it;
             cudaMemcpyAsync(r0, r, n * sizeof(VT), cudaMemcpyDeviceToDevice, s);
