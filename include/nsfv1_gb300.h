@@ -311,6 +311,11 @@ int nsfv1_get_assembly_threads(const nsfv1_disc* h);
  * ms[n_candidates] (host, may be NULL) receives the second pass's times. */
 int nsfv1_assembly_autotune(nsfv1_disc* h, const double* u, int prec, const int* candidates, int n_candidates, double* ms, void* stream);
 
+/* Timing of the last batched solve: out[0] Newton steps, out[1] device ms of the
+ * steps' fixed work (Jacobians, block inverses, GMRES), out[2] device ms of the
+ * line searches, out[3] wall ms of the whole call; further entries 0. */
+int nsfv1_batch_stats(const nsfv1_disc* h, double* out, int n);
+
 /* Autotuner of the batched solve: times one Newton step from u (u is not
  * changed) for every candidate cluster size (CTAs per instance) and writes the
  * fastest into opt->cluster_size; ms[n_candidates] (host, may be NULL)

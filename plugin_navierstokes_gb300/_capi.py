@@ -122,6 +122,7 @@ _SIGS = {
     "nsfv1_set_assembly_threads": (c_int, [c_void_p, c_int]),
     "nsfv1_get_assembly_threads": (c_int, [c_void_p]),
     "nsfv1_assembly_autotune": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
+    "nsfv1_batch_stats": (c_int, [c_void_p, c_void_p, c_int]),
     "nsfv1_batch_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(BatchOptions), c_void_p,
                                      c_int, c_void_p, c_void_p]),
     "nsfv1_ref_tables": (c_int, [c_int, POINTER(c_int), POINTER(c_int), c_void_p, POINTER(c_int), c_void_p, c_void_p, c_void_p]),

@@ -10,6 +10,7 @@
 // fixed order. Cluster barriers are hardware barriers; the kernel has no
 // spin-wait. Results do not depend on which cluster runs an instance.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -24,11 +25,12 @@ namespace cg = cooperative_groups;
 
 namespace nsfv1 {
 
-static constexpr int kGT = 256;      // threads per CTA of the GMRES kernel
+static constexpr int kGT = 512;      // threads per CTA of the GMRES kernel (16 warps per SM hide the latency of the instance-local loops)
 static constexpr int kMaxM = 32;     // largest restart length
 static constexpr int kWarps = kGT / 32;
 
 static constexpr int kMaxLevels = 8;
+static constexpr int64_t kLocalRows = 289;   // multigrid levels up to 16 x 16 cells run on one CTA
 
 // one level of the geometric multigrid hierarchy (level 0 = the fine mesh)
 template <typename VT>
@@ -108,6 +110,64 @@ __device__ __forceinline__ void block_row_acc(const VT* __restrict__ vals, const
     }
 }
 
+// rows [0, nn) of a block-CSR slice (global row = row0 + local row), U rows per
+// lane group and trip: the row pointers, column indices, blocks and x entries of
+// U rows (two blocks per lane unrolled, predicated) are all requested before the
+// first is used, so each trip pays one memory latency instead of U; longer rows
+// finish in a remainder loop. epi(local row, acc) receives the row sums on lane 0.
+template <typename VT, int b, int G, int U, typename Epi>
+__device__ __forceinline__ void rows_spmv(const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx,
+                                          const VT* __restrict__ vals, int64_t row0, int64_t nn, const VT* __restrict__ xin,
+                                          int64_t xoff, int ctid, int cth, Epi&& epi) {
+    constexpr int KB = 2;
+    const int lane = ctid % G;
+    const int64_t groups = cth / G;
+    const int64_t per = groups * U;
+    const int64_t trips = (nn + per - 1) / per;
+    for (int64_t it = 0; it < trips; ++it) {
+        int64_t q0[U], q1[U];
+        VT acc[U][b];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t lr = ctid / G + (it * U + u) * groups;
+            const bool valid = lr < nn;
+            q0[u] = valid ? rowPtr[row0 + lr] : 0;
+            q1[u] = valid ? rowPtr[row0 + lr + 1] : 0;
+#pragma unroll
+            for (int i = 0; i < b; ++i) acc[u][i] = VT(0);
+        }
+#pragma unroll
+        for (int k = 0; k < KB; ++k)
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int64_t q = q0[u] + lane + k * G;
+                if (q < q1[u]) {
+                    const VT* blk = vals + q * (b * b);
+                    const VT* xc = xin + (int64_t)colIdx[q] * b - xoff;
+                    VT xv[b];
+#pragma unroll
+                    for (int j = 0; j < b; ++j) xv[j] = xc[j];
+#pragma unroll
+                    for (int i = 0; i < b; ++i)
+#pragma unroll
+                        for (int j = 0; j < b; ++j) acc[u][i] = fma(blk[i * b + j], xv[j], acc[u][i]);
+                }
+            }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (q1[u] - q0[u] > KB * G) block_row_acc<VT, b, G>(vals, colIdx, q0[u] + KB * G, q1[u], lane, xin, xoff, acc[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+#pragma unroll
+            for (int off = G / 2; off > 0; off >>= 1)
+#pragma unroll
+                for (int r = 0; r < b; ++r) acc[u][r] += __shfl_down_sync(0xffffffffu, acc[u][r], off, G);
+            const int64_t lr = ctid / G + (it * U + u) * groups;
+            if (lr < nn && lane == 0) epi(lr, acc[u]);
+        }
+    }
+}
+
 template <typename VT, int b, int G>
 __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A) {
     cg::cluster_group cl = cg::this_cluster();
@@ -159,34 +219,28 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
         auto Vk = [&](int k) { return A.V + (int64_t)k * A.nTot + o; };
         VT* __restrict__ t = A.t + o;
         const VT* __restrict__ Dinv = A.Dinv + node0 * b * b;
-        const int64_t nGroups = cth / G;
-        const int64_t spmvTrips = (nNode + nGroups - 1) / nGroups;
 
         // y = M t  (rows of this instance; G lanes per block row, uniform trip count)
         auto spmv = [&](const VT* __restrict__ xin, VT* __restrict__ yout) {
-            const int lane = ctid % G;
-            for (int64_t it = 0; it < spmvTrips; ++it) {
-                const int64_t lr = ctid / G + it * nGroups;
-                const bool valid = lr < nNode;
-                const int64_t row = node0 + lr;
-                const int64_t q0 = valid ? A.rowPtr[row] : 0, q1 = valid ? A.rowPtr[row + 1] : 0;
-                VT acc[b];
+            rows_spmv<VT, b, G, 4>(A.rowPtr, A.colIdx, A.vals, node0, nNode, xin, o, ctid, cth, [&](int64_t lr, const VT (&acc)[b]) {
 #pragma unroll
-                for (int i = 0; i < b; ++i) acc[i] = VT(0);
-                block_row_acc<VT, b, G>(A.vals, A.colIdx, q0, q1, lane, xin, o, acc);
-#pragma unroll
-                for (int off = G / 2; off > 0; off >>= 1)
-#pragma unroll
-                    for (int r = 0; r < b; ++r) acc[r] += __shfl_down_sync(0xffffffffu, acc[r], off, G);
-                if (valid && lane == 0) {
-#pragma unroll
-                    for (int r = 0; r < b; ++r) yout[lr * b + r] = acc[r];
-                }
-            }
+                for (int r = 0; r < b; ++r) yout[lr * b + r] = acc[r];
+            });
         };
         // point-block Jacobi: out = Dm (in) (per node, optionally damped / accumulated)
+        // coarse multigrid levels run on CTA 0 alone with block barriers ("local"
+        // mode); everything else on the whole cluster with cluster barriers
+        bool loc = false;
+        auto me = [&]() { return loc ? tid : ctid; };
+        auto nth = [&]() { return loc ? kGT : cth; };
+        auto bar = [&]() {
+            if (loc) __syncthreads();
+            else cl.sync();
+        };
         auto jacobi = [&](const VT* __restrict__ Dm, int64_t nn, const VT* __restrict__ in, VT* __restrict__ out, VT w, bool accumulate) {
-            for (int64_t nd = ctid; nd < nn; nd += cth) {
+            const int64_t t0 = me(), tn = nth();
+#pragma unroll 2
+            for (int64_t nd = t0; nd < nn; nd += tn) {
                 VT xi[b];
 #pragma unroll
                 for (int j = 0; j < b; ++j) xi[j] = in[nd * b + j];
@@ -202,27 +256,10 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
         // level SpMV with residual epilogue: res = rhs - M_l x  (rhs == nullptr: res = M_l x)
         auto lspmv = [&](const MgLevel<VT>& L, int64_t n0, int64_t nn, const VT* __restrict__ xin, const VT* __restrict__ rhsl,
                          VT* __restrict__ res) {
-            const int lane = ctid % G;
-            const int64_t trips = (nn + nGroups - 1) / nGroups;
-            const int64_t ol = n0 * b;
-            for (int64_t it = 0; it < trips; ++it) {
-                const int64_t lr = ctid / G + it * nGroups;
-                const bool valid = lr < nn;
-                const int64_t row = n0 + lr;
-                const int64_t q0 = valid ? L.rowPtr[row] : 0, q1 = valid ? L.rowPtr[row + 1] : 0;
-                VT acc[b];
+            rows_spmv<VT, b, G, 4>(L.rowPtr, L.colIdx, L.vals, n0, nn, xin, n0 * b, me(), nth(), [&](int64_t lr, const VT (&acc)[b]) {
 #pragma unroll
-                for (int i = 0; i < b; ++i) acc[i] = VT(0);
-                block_row_acc<VT, b, G>(L.vals, L.colIdx, q0, q1, lane, xin, ol, acc);
-#pragma unroll
-                for (int off = G / 2; off > 0; off >>= 1)
-#pragma unroll
-                    for (int r = 0; r < b; ++r) acc[r] += __shfl_down_sync(0xffffffffu, acc[r], off, G);
-                if (valid && lane == 0) {
-#pragma unroll
-                    for (int r = 0; r < b; ++r) res[lr * b + r] = rhsl ? rhsl[lr * b + r] - acc[r] : acc[r];
-                }
-            }
+                for (int r = 0; r < b; ++r) res[lr * b + r] = rhsl ? rhsl[lr * b + r] - acc[r] : acc[r];
+            });
         };
         // instance levels: cells per side, first node on each level
         const int nLev = A.mg.nLevels;
@@ -246,21 +283,22 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
             auto ls = [&](int l) { return A.mg.lv[l].s + ln0[l] * b; };
             auto lD = [&](int l) { return A.mg.lv[l].Dinv + ln0[l] * b * b; };
             auto lnn = [&](int l) { return (int64_t)(lcell[l] + 1) * (lcell[l] + 1); };
-            for (int l = 0; l < myLev; ++l) {
+            // pre-smoothing on level l, then (above the coarsest) residual and restriction into l + 1
+            auto down = [&](int l) {
                 const MgLevel<VT>& L = A.mg.lv[l];
                 const int64_t nn = lnn(l);
                 const int sweeps = (l == myLev - 1) ? A.mg.nuCoarse : A.mg.nu;
                 jacobi(lD(l), nn, lr(l), lx(l), om, false);
-                cl.sync();
+                bar();
                 for (int k = 1; k < sweeps; ++k) {
                     lspmv(L, ln0[l], nn, lx(l), lr(l), ls(l));
-                    cl.sync();
+                    bar();
                     jacobi(lD(l), nn, ls(l), lx(l), om, true);
-                    cl.sync();
+                    bar();
                 }
-                if (l == myLev - 1) break;
+                if (l == myLev - 1) return;
                 lspmv(L, ln0[l], nn, lx(l), lr(l), ls(l));
-                cl.sync();
+                bar();
                 // restriction (transpose of bilinear interpolation), masked on both levels
                 const int nf = lcell[l], nc = lcell[l + 1];
                 const int64_t mf = nf + 1, mc = nc + 1;
@@ -268,7 +306,7 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                 const uint8_t* mkc = A.mg.lv[l + 1].mask + ln0[l + 1] * b;
                 VT* rc = A.mg.lv[l + 1].r + ln0[l + 1] * b;
                 const VT* sf = ls(l);
-                for (int64_t c = ctid; c < mc * mc; c += cth) {
+                for (int64_t c = me(); c < mc * mc; c += nth()) {
                     const int64_t I = c % mc, J = c / mc;
                     VT acc[b];
 #pragma unroll
@@ -288,18 +326,18 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
 #pragma unroll
                     for (int f = 0; f < b; ++f) rc[c * b + f] = mkc[c * b + f] ? acc[f] : VT(0);
                 }
-                cl.sync();
-            }
-            for (int l = myLev - 2; l >= 0; --l) {
+                bar();
+            };
+            // prolongation of the correction of level l + 1 into level l, then post-smoothing on l
+            auto up = [&](int l) {
                 const MgLevel<VT>& L = A.mg.lv[l];
                 const int64_t nn = lnn(l);
-                // prolongation (bilinear) of the coarse correction, masked
                 const int nf = lcell[l];
                 const int64_t mf = nf + 1, mc = lcell[l + 1] + 1;
                 const uint8_t* mkf = L.mask + ln0[l] * b;
                 const VT* xc = lx(l + 1);
                 VT* xf = lx(l);
-                for (int64_t fnode = ctid; fnode < mf * mf; fnode += cth) {
+                for (int64_t fnode = me(); fnode < mf * mf; fnode += nth()) {
                     const int64_t I = fnode % mf, J = fnode / mf;
                     const int64_t i0 = I / 2, j0 = J / 2;
                     const int64_t i1 = (I & 1) ? i0 + 1 : i0, j1 = (J & 1) ? j0 + 1 : j0;
@@ -313,14 +351,30 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                         if (mkf[fnode * b + f]) xf[fnode * b + f] += v;
                     }
                 }
-                cl.sync();
+                bar();
                 for (int k = 0; k < A.mg.nu; ++k) {
                     lspmv(L, ln0[l], nn, lx(l), lr(l), ls(l));
-                    cl.sync();
+                    bar();
                     jacobi(lD(l), nn, ls(l), lx(l), om, true);
-                    cl.sync();
+                    bar();
                 }
+            };
+            // the first level (below the instance's own) with at most kLocalRows nodes starts the
+            // part of the cycle that CTA 0 runs alone
+            int lsm = myLev;
+            for (int l = 1; l < myLev; ++l)
+                if (lnn(l) <= kLocalRows) { lsm = l; break; }
+            for (int l = 0; l < lsm; ++l) down(l);
+            if (lsm < myLev) {
+                if (crank == 0) {
+                    loc = true;
+                    for (int l = lsm; l < myLev; ++l) down(l);
+                    for (int l = myLev - 2; l >= lsm; --l) up(l);
+                    loc = false;
+                }
+                cl.sync();
             }
+            for (int l = min(lsm, myLev - 1) - 1; l >= 0; --l) up(l);
         };
         // ||v||^2 over the cluster
         auto norm2 = [&](const VT* __restrict__ v) {
@@ -358,14 +412,31 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                     if (tid <= j) hcol[tid] = 0.0;
                     // classical Gram-Schmidt, two passes
                     for (int pass = 0; pass < 2; ++pass) {
-                        for (int k = 0; k <= j; ++k) {
-                            const VT* vk = Vk(k);
-                            VT acc = VT(0);
-                            for (int64_t e = ctid; e < n; e += cth) acc += vk[e] * w[e];
-                            ClusterRed::block_part((double)acc, k, wred);
+                        // four basis vectors per pass over w (each dot keeps its own
+                        // summation order, so the results do not change)
+                        for (int k0 = 0; k0 <= j; k0 += 4) {
+                            const int nk = min(4, j + 1 - k0);
+                            const VT* v0k = Vk(k0);
+                            const VT* v1k = Vk(min(k0 + 1, j));
+                            const VT* v2k = Vk(min(k0 + 2, j));
+                            const VT* v3k = Vk(min(k0 + 3, j));
+                            VT a0 = VT(0), a1 = VT(0), a2 = VT(0), a3 = VT(0);
+#pragma unroll 2
+                            for (int64_t e = ctid; e < n; e += cth) {
+                                const VT we = w[e];
+                                a0 += v0k[e] * we;
+                                if (nk > 1) a1 += v1k[e] * we;
+                                if (nk > 2) a2 += v2k[e] * we;
+                                if (nk > 3) a3 += v3k[e] * we;
+                            }
+                            ClusterRed::block_part((double)a0, k0, wred);
+                            if (nk > 1) ClusterRed::block_part((double)a1, k0 + 1, wred);
+                            if (nk > 2) ClusterRed::block_part((double)a2, k0 + 2, wred);
+                            if (nk > 3) ClusterRed::block_part((double)a3, k0 + 3, wred);
                         }
                         cluster_sum(j + 1);
                         if (tid <= j) hcol[tid] += sum[tid];
+#pragma unroll 2
                         for (int64_t e = ctid; e < n; e += cth) {
                             VT a = w[e];
                             for (int k = 0; k <= j; ++k) a -= (VT)sum[k] * Vk(k)[e];
@@ -601,6 +672,8 @@ struct BatchState {
     cudaStream_t gs = nullptr;
     cudaEvent_t evIn = nullptr, evOut = nullptr;
     std::vector<std::pair<int, cudaGraphExec_t>> graphs;   // one per cluster size in use
+    // timing of the last solve (ms): [steps, step work (Jacobians + GMRES), line search, wall]
+    double stats[8] = {0};
     ~BatchState() {
         clear_levels();
         drop_graph();
@@ -656,6 +729,14 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
     BatchState* BS = batch_state(D);
     BatchWs& W = BS->ws;
     BS->drop_graph();
+    for (double& x : BS->stats) x = 0.0;
+    const auto wall0 = std::chrono::steady_clock::now();
+    struct Ev {
+        cudaEvent_t e = nullptr;
+        Ev() { cudaEventCreate(&e); }
+        ~Ev() { if (e) cudaEventDestroy(e); }
+    } eA, eB, eC;
+    cudaEvent_t evA = eA.e, evB = eB.e, evC = eC.e;
     if (W.prec != prec || W.n != n || W.m != m) {
         W.release();
         const size_t vt = sizeof(VT);
@@ -867,7 +948,9 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
             !D.cuda_ok(cudaMemcpyAsync(W.nQueue, &nq, 4, cudaMemcpyHostToDevice, s), "queue") ||
             !D.cuda_ok(cudaMemcpyAsync(W.rtolInst, eta.data(), nInst * 8, cudaMemcpyHostToDevice, s), "tolerances"))
             return D.status;
+        cudaEventRecord(evA, s);
         if (!run_step()) return D.status;
+        cudaEventRecord(evB, s);
         int herr = 0;
         cudaMemcpyAsync(&herr, D.d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(iters.data(), W.iters, nInst * 4, cudaMemcpyDeviceToHost, s);
@@ -910,6 +993,14 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
             k_batch_copy<<<g, 256, 0, s>>>(n, b, D.d_nodeInst, W.accepted, W.Dt, W.D);
             if (!any) break;
         }
+        cudaEventRecord(evC, s);
+        {
+            float a = 0.f, c = 0.f;
+            cudaEventSynchronize(evC);
+            cudaEventElapsedTime(&a, evA, evB);
+            cudaEventElapsedTime(&c, evB, evC);
+            BS->stats[0] += 1.0; BS->stats[1] += a; BS->stats[2] += c;
+        }
         // u <- Ut on the active instances
         if (!upload_flags(active, W.accepted)) return D.status;
         k_batch_copy<<<g, 256, 0, s>>>(n, b, D.d_nodeInst, W.accepted, W.Ut, u);
@@ -927,6 +1018,7 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
     std::vector<int32_t> all(nInst, 1);
     upload_flags(all, D.d_instActive);
     if (!D.cuda_ok(cudaStreamSynchronize(s), "batched newton")) return D.status;
+    BS->stats[3] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
     int worst = NSFV1_OK;
     for (int i = 0; i < nInst; ++i) if (res[i].status != NSFV1_OK) worst = res[i].status;
     if (worst != NSFV1_OK) D.fail(worst, "batched Newton: some instances did not converge (see the per-instance results)");
@@ -1164,6 +1256,14 @@ int nsfv1_batch_autotune(nsfv1_disc* h, const double* u, const double* u_old, do
     if (ms) for (int c = 0; c < n_candidates; ++c) ms[c] = t[c];
     D->status = NSFV1_OK;
     D->lastError.clear();
+    return NSFV1_OK;
+}
+
+int nsfv1_batch_stats(const nsfv1_disc* h, double* out, int n) {
+    const Disc* D = reinterpret_cast<const Disc*>(h);
+    if (!D || !out || n <= 0) return NSFV1_ERR_ARGUMENT;
+    const BatchState* BS = static_cast<const BatchState*>(D->batch);
+    for (int i = 0; i < n; ++i) out[i] = (BS && i < 8) ? BS->stats[i] : 0.0;
     return NSFV1_OK;
 }
 

@@ -229,6 +229,12 @@ class NavierStokesFV1:
             raise NSFV1Error(st, self._lib.nsfv1_last_error(self._h).decode())
         return out
 
+    def batch_stats(self) -> dict:
+        """Timing of the last batched solve (nsfv1_batch_stats)."""
+        out = np.zeros(8)
+        self._c(self._lib.nsfv1_batch_stats(self._h, out.ctypes.data, 8))
+        return {"steps": int(out[0]), "step_work_ms": out[1], "line_search_ms": out[2], "wall_ms": out[3]}
+
     def set_assembly_threads(self, threads: int) -> None:
         """CTA size of the assembly colour launches (32, 64, 96 or 128)."""
         self._c(self._lib.nsfv1_set_assembly_threads(self._h, int(threads)))

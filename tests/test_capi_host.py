@@ -91,3 +91,35 @@ def test_cavity_dirichlet_rows():
     assert (0 * b + 2) in dofs.tolist()
     lid = [(n, v) for d, n, v in zip(dofs, nodes, vals) if d % b == 0 and v != 0]
     assert all(abs(X[n, 1] - 1) < 1e-12 and 0 < X[n, 0] < 1 for n, _ in lid) and len(lid) == 3
+
+
+def test_empty_and_oversized_meshes_are_rejected_before_any_device_work():
+    lib = _capi.load()
+    d = NavierStokesFV1("u,v,w,p")
+    coords = np.zeros((8, 3))
+    conn = np.arange(8, dtype=np.int32)
+    # no elements / no nodes
+    assert lib.nsfv1_set_mesh(d._h, _capi.HEXAHEDRON, 8, coords.ctypes.data, 0, conn.ctypes.data) == _capi.ERR_ARGUMENT
+    assert lib.nsfv1_set_mesh(d._h, _capi.HEXAHEDRON, 0, coords.ctypes.data, 1, conn.ctypes.data) == _capi.ERR_ARGUMENT
+    # 32-bit index limits (checked from the sizes alone, the arrays are not read)
+    assert lib.nsfv1_set_mesh(d._h, _capi.HEXAHEDRON, 8, coords.ctypes.data, 1 << 26, conn.ctypes.data) == _capi.ERR_ARGUMENT
+    assert "32-bit" in d.last_error()
+    # unknown element type
+    assert lib.nsfv1_set_mesh(d._h, 7, 8, coords.ctypes.data, 1, conn.ctypes.data) == _capi.ERR_ARGUMENT
+
+
+def test_single_element_pattern_and_ragged_coloring():
+    # one hexahedron: a dense 8 x 8 block pattern, one colour
+    rp, ci, col, nc = mesh_pattern(_capi.HEXAHEDRON, 8, np.arange(8, dtype=np.int32)[None, :])
+    assert np.array_equal(rp, np.arange(9) * 8) and nc == 1 and col.tolist() == [0]
+    # a ragged strip of triangles sharing one node (a fan): every element needs its own colour
+    fan = np.array([[0, k, k + 1] for k in range(1, 7)], np.int32)
+    rp, ci, col, nc = mesh_pattern(_capi.TRIANGLE, 8, fan)
+    assert nc == 6 and sorted(col.tolist()) == list(range(6))
+    o = oracle.Oracle(2)
+    X = np.zeros((8, 2))
+    X[1:, 0] = np.cos(np.linspace(0, 3, 7))
+    X[1:, 1] = np.sin(np.linspace(0, 3, 7))
+    o.set_mesh(_capi.TRIANGLE, X, fan)
+    orp, oci = o.pattern()
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
