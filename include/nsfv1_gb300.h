@@ -126,7 +126,8 @@ int nsfv1_set_dirichlet(nsfv1_disc* h, int64_t n, const int32_t* dofs, const dou
  * add_rhs_elem (navier_stokes_fv1.cpp:208-248, 597-869) and the scatter. */
 int nsfv1_assemble_defect(nsfv1_disc* h, const double* u, const double* u_old, double dt, double* d, void* stream);
 /* Global Jacobian values J = dA/du (or M + dt dA/du) in the handle's block CSR,
- * vals[nnz_blocks * b * b] of double (NSFV1_F64) or float (NSFV1_F32).
+ * vals[nnz_blocks * b * b] of double (NSFV1_F64) or float (NSFV1_F32; for 3D
+ * meshes 16-byte aligned: each 4-float block row is one vector reduction).
  * Replaces the element loop over add_jac_A_elem + add_jac_M_elem
  * (navier_stokes_fv1.cpp:250-595, 781-808) and the matrix insertion. */
 int nsfv1_assemble_jacobian(nsfv1_disc* h, const double* u, const double* u_old, double dt, void* vals, int prec, void* stream);

@@ -64,13 +64,24 @@ struct GlobalJacSink {
         // colour no other thread touches this block and one thread's updates to an
         // address apply in program order, so the sums stay deterministic
         VT* p = vals + (int64_t)__ldg(blk + i * nsh + k) * (b * b);
+        if constexpr (std::is_same<VT, float>::value && b == 4) {
+            // one 16-byte vector reduction per block row (the value array is 16-byte aligned)
 #pragma unroll
-        for (int r = 0; r < b; ++r)
-#pragma unroll
-            for (int c = 0; c < b; ++c) {
-                const VT v = (VT)B[r][c];
-                atomicAdd(p + r * b + c, plus ? v : -v);
+            for (int r = 0; r < 4; ++r) {
+                const float s = plus ? 1.f : -1.f;
+                asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p + r * 4), "f"(s * (float)B[r][0]),
+                             "f"(s * (float)B[r][1]), "f"(s * (float)B[r][2]), "f"(s * (float)B[r][3])
+                             : "memory");
             }
+        } else {
+#pragma unroll
+            for (int r = 0; r < b; ++r)
+#pragma unroll
+                for (int c = 0; c < b; ++c) {
+                    const VT v = (VT)B[r][c];
+                    atomicAdd(p + r * b + c, plus ? v : -v);
+                }
+        }
     }
 };
 

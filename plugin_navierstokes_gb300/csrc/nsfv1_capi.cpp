@@ -554,6 +554,8 @@ bool Disc::assemble_jacobian(const double* u, const double* u_old, double dt, vo
     if (!hasMesh) return fail(NSFV1_ERR_STATE, "assemble_jacobian: no mesh set");
     if (!u || !vals) return fail(NSFV1_ERR_ARGUMENT, "assemble_jacobian: null pointer");
     if (prec != NSFV1_F64 && prec != NSFV1_F32) return fail(NSFV1_ERR_ARGUMENT, "assemble_jacobian: precision must be NSFV1_F64 or NSFV1_F32");
+    if (prec == NSFV1_F32 && dim == 3 && (reinterpret_cast<uintptr_t>(vals) & 15))
+        return fail(NSFV1_ERR_ARGUMENT, "assemble_jacobian: FP32 values of a 3D mesh must be 16-byte aligned");
     DiscParams P;
     if (!params(P, u_old != nullptr, dt)) return false;
     const int b = dim + 1;

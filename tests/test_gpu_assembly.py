@@ -217,3 +217,18 @@ def test_assembly_cta_size_is_bitwise_neutral_and_autotuned(cuda):
         assert torch.equal(D, out[0][0]) and torch.equal(J, out[0][1])
     best, ms = d.assembly_autotune(tu, "f64", (32, 64, 128))
     assert best in (32, 64, 128) and len(ms) == 3 and ms[(32, 64, 128).index(best)] == min(ms)
+
+
+def test_fp32_3d_jacobian_needs_16_byte_alignment(cuda):
+    import torch
+    from plugin_navierstokes_gb300 import NSFV1Error, NavierStokesFV1, mesh
+    roid, X, C = mesh.structured_hexes(2)
+    d = NavierStokesFV1("u,v,w,p", "Inner")
+    d.set_kinematic_viscosity(0.0025); d.set_upwind("lps"); d.set_stabilization("flow")
+    d.set_mesh(roid, X, C)
+    nnzb = d.pattern_info()["nnz_blocks"]
+    tu = torch.zeros(X.shape[0] * 4, dtype=torch.float64, device=cuda)
+    J = torch.zeros(nnzb * 16 + 4, dtype=torch.float32, device=cuda)
+    with pytest.raises(NSFV1Error):
+        d.assemble_jacobian(tu, J[1:])
+    d.assemble_jacobian(tu, J[4:])   # 16-byte offset: fine
