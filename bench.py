@@ -166,6 +166,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cells", type=int, default=64, help="assembly workload: cells per side (64 is the benchmark; smaller for profiling)")
     ap.add_argument("--time-steps", type=int, default=20, help="transient workload: backward-Euler steps (20 is the benchmark)")
+    ap.add_argument("--instances", type=int, default=256, help="batched workload: first K of the 256 draws (256 is the benchmark)")
     args = ap.parse_args()
     global N_CELLS
     N_CELLS = args.cells
@@ -393,6 +394,7 @@ def run_solves(args):
 
     if args.workload == "batched":
         N, Re, lid = mesh.draw_cavity_params(256, seed=3)
+        N, Re, lid = N[:args.instances], Re[:args.instances], lid[:args.instances]
         wl = "256 lid-driven cavities, N ~ U{32,48,64,96,128,192,256}, Re ~ logU[10,1000], lid ~ U[0.5,2] (seed 3), full upwind + FLOW"
     else:
         Re, lid = cavity_draws(256, 5)

@@ -44,6 +44,7 @@ struct MgLevel {
     VT* x;                  // level correction
     VT* r;                  // level right-hand side
     VT* s;                  // residual scratch
+    VT* x2;                 // second correction buffer (smoother sweeps alternate between x and x2)
 };
 
 template <typename VT>
@@ -278,11 +279,42 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
         auto precond = [&](const VT* __restrict__ in, VT* __restrict__ out) {
             if (myLev <= 1) { jacobi(Dinv, nNode, in, out, VT(1), false); return; }
             const VT om = (VT)A.mg.omega;
-            auto lx = [&](int l) { return l == 0 ? out : A.mg.lv[l].x + ln0[l] * b; };
+            // the correction of each level lives in one of two buffers; a smoother sweep
+            // reads the current one and writes the other
+            auto prim = [&](int l) { return l == 0 ? out : A.mg.lv[l].x + ln0[l] * b; };
+            auto sec = [&](int l) { return A.mg.lv[l].x2 + ln0[l] * b; };
+            bool inSec[kMaxLevels];
+#pragma unroll 1
+            for (int l = 0; l < kMaxLevels; ++l) inSec[l] = false;
+            auto lx = [&](int l) { return inSec[l] ? sec(l) : prim(l); };
             auto lr = [&](int l) { return l == 0 ? in : (const VT*)(A.mg.lv[l].r + ln0[l] * b); };
             auto ls = [&](int l) { return A.mg.lv[l].s + ln0[l] * b; };
             auto lD = [&](int l) { return A.mg.lv[l].Dinv + ln0[l] * b * b; };
             auto lnn = [&](int l) { return (int64_t)(lcell[l] + 1) * (lcell[l] + 1); };
+            // one damped point-block Jacobi sweep in a single pass:
+            //   x_new = x + omega Dinv (r - M x)    (row-local; neighbours read from x)
+            auto fsweep = [&](int l) {
+                const MgLevel<VT>& L = A.mg.lv[l];
+                const VT* xc = lx(l);
+                VT* xn = inSec[l] ? prim(l) : sec(l);
+                const VT* rl = lr(l);
+                const VT* Dm = lD(l);
+                rows_spmv<VT, b, G, 4>(L.rowPtr, L.colIdx, L.vals, ln0[l], lnn(l), xc, ln0[l] * b, me(), nth(),
+                                       [&](int64_t r0, const VT (&acc)[b]) {
+                                           VT sv[b];
+#pragma unroll
+                                           for (int j = 0; j < b; ++j) sv[j] = rl[r0 * b + j] - acc[j];
+#pragma unroll
+                                           for (int i = 0; i < b; ++i) {
+                                               VT a = VT(0);
+#pragma unroll
+                                               for (int j = 0; j < b; ++j) a += Dm[r0 * b * b + i * b + j] * sv[j];
+                                               xn[r0 * b + i] = xc[r0 * b + i] + om * a;
+                                           }
+                                       });
+                inSec[l] = !inSec[l];
+                bar();
+            };
             // pre-smoothing on level l, then (above the coarsest) residual and restriction into l + 1
             auto down = [&](int l) {
                 const MgLevel<VT>& L = A.mg.lv[l];
@@ -290,12 +322,7 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                 const int sweeps = (l == myLev - 1) ? A.mg.nuCoarse : A.mg.nu;
                 jacobi(lD(l), nn, lr(l), lx(l), om, false);
                 bar();
-                for (int k = 1; k < sweeps; ++k) {
-                    lspmv(L, ln0[l], nn, lx(l), lr(l), ls(l));
-                    bar();
-                    jacobi(lD(l), nn, ls(l), lx(l), om, true);
-                    bar();
-                }
+                for (int k = 1; k < sweeps; ++k) fsweep(l);
                 if (l == myLev - 1) return;
                 lspmv(L, ln0[l], nn, lx(l), lr(l), ls(l));
                 bar();
@@ -352,12 +379,8 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                     }
                 }
                 bar();
-                for (int k = 0; k < A.mg.nu; ++k) {
-                    lspmv(L, ln0[l], nn, lx(l), lr(l), ls(l));
-                    bar();
-                    jacobi(lD(l), nn, ls(l), lx(l), om, true);
-                    bar();
-                }
+                for (int k = 0; k < A.mg.nu; ++k) fsweep(l);
+                (void)nn;
             };
             // the first level (below the instance's own) with at most kLocalRows nodes starts the
             // part of the cycle that CTA 0 runs alone
@@ -373,8 +396,17 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                     loc = false;
                 }
                 cl.sync();
+                // which buffer holds level lsm's correction now (every CTA agrees; CTA 0 got
+                // there by running the sweeps: sweeps - 1 fused ones down, nu up)
+                const int sw = (lsm == myLev - 1) ? A.mg.nuCoarse : A.mg.nu;
+                inSec[lsm] = (((sw - 1) + (lsm < myLev - 1 ? A.mg.nu : 0)) & 1) != 0;
             }
             for (int l = min(lsm, myLev - 1) - 1; l >= 0; --l) up(l);
+            if (inSec[0]) {
+                const VT* src = sec(0);
+#pragma unroll 4
+                for (int64_t e = ctid; e < n; e += cth) out[e] = src[e];
+            }
         };
         // ||v||^2 over the cluster
         auto norm2 = [&](const VT* __restrict__ v) {
@@ -619,13 +651,13 @@ struct BatchWs {
     int prec = -1, m = 0;
     int64_t n = 0;
     double *D = nullptr, *Dt = nullptr, *Ut = nullptr, *nrm = nullptr, *lambda = nullptr, *relres = nullptr;
-    void *J = nullptr, *Dinv = nullptr, *V = nullptr, *t = nullptr, *x = nullptr, *q = nullptr, *s = nullptr;
+    void *J = nullptr, *Dinv = nullptr, *V = nullptr, *t = nullptr, *x = nullptr, *q = nullptr, *s = nullptr, *x2 = nullptr;
     int32_t *queue = nullptr, *head = nullptr, *pending = nullptr, *accepted = nullptr, *iters = nullptr, *nQueue = nullptr;
     double* rtolInst = nullptr;
     ~BatchWs() { release(); }
     void release() {
         auto f = [](auto*& p) { if (p) cudaFree((void*)p); p = nullptr; };
-        f(D); f(Dt); f(Ut); f(nrm); f(lambda); f(relres); f(J); f(Dinv); f(V); f(t); f(x); f(q); f(s);
+        f(D); f(Dt); f(Ut); f(nrm); f(lambda); f(relres); f(J); f(Dinv); f(V); f(t); f(x); f(q); f(s); f(x2);
         f(queue); f(head); f(pending); f(accepted); f(iters); f(nQueue); f(rtolInst);
         prec = -1;
     }
@@ -653,11 +685,11 @@ struct Level {
     int32_t* d_inj = nullptr;      // [level nodes] node of the next finer level at the same point
     uint8_t* d_mask = nullptr;     // [level dofs] 1 = free row
     double* d_u = nullptr;         // injected state
-    void *J = nullptr, *Dinv = nullptr, *x = nullptr, *r = nullptr, *s = nullptr;
+    void *J = nullptr, *Dinv = nullptr, *x = nullptr, *r = nullptr, *s = nullptr, *x2 = nullptr;
     int prec = -1;
     void release() {
         auto f = [](auto*& p) { if (p) cudaFree((void*)p); p = nullptr; };
-        f(d_node0); f(d_inj); f(d_mask); f(d_u); f(J); f(Dinv); f(x); f(r); f(s);
+        f(d_node0); f(d_inj); f(d_mask); f(d_u); f(J); f(Dinv); f(x); f(r); f(s); f(x2);
         delete disc; disc = nullptr;
         prec = -1;
     }
@@ -744,6 +776,7 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
         if (!al(W.D, n * 8) || !al(W.Dt, n * 8) || !al(W.Ut, n * 8) || !al(W.nrm, nInst * 8) || !al(W.lambda, nInst * 8) ||
             !al(W.relres, nInst * 8) || !al(W.J, D.colIdx.size() * b * b * vt) || !al(W.Dinv, (size_t)D.nNodes * b * b * vt) ||
             !al(W.V, (size_t)(m + 1) * n * vt) || !al(W.t, n * vt) || !al(W.x, n * vt) || !al(W.q, n * vt) || !al(W.s, n * vt) ||
+            !al(W.x2, n * vt) ||
             !al(W.queue, nInst * 4) || !al(W.head, 4) || !al(W.nQueue, 4) || !al(W.rtolInst, nInst * 8) ||
             !al(W.pending, nInst * 4) || !al(W.accepted, nInst * 4) || !al(W.iters, nInst * 4))
             return D.status;
@@ -780,13 +813,14 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
             Disc& C = *L.disc;
             const int64_t nc = C.nNodes;
             auto f = [](auto*& q) { if (q) cudaFree((void*)q); q = nullptr; };
-            f(L.J); f(L.Dinv); f(L.x); f(L.r); f(L.s);
+            f(L.J); f(L.Dinv); f(L.x); f(L.r); f(L.s); f(L.x2);
             const size_t vt = sizeof(VT);
             if (!D.cuda_ok(cudaMalloc(&L.J, C.colIdx.size() * b * b * vt), "level J") ||
                 !D.cuda_ok(cudaMalloc(&L.Dinv, (size_t)nc * b * b * vt), "level Dinv") ||
                 !D.cuda_ok(cudaMalloc(&L.x, (size_t)nc * b * vt), "level x") ||
                 !D.cuda_ok(cudaMalloc(&L.r, (size_t)nc * b * vt), "level r") ||
-                !D.cuda_ok(cudaMalloc(&L.s, (size_t)nc * b * vt), "level s"))
+                !D.cuda_ok(cudaMalloc(&L.s, (size_t)nc * b * vt), "level s") ||
+                !D.cuda_ok(cudaMalloc(&L.x2, (size_t)nc * b * vt), "level x2"))
                 return D.status;
             L.prec = prec;
         }
@@ -822,11 +856,11 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
         ga.mg.nuCoarse = opt.coarse_steps > 0 ? opt.coarse_steps : 20;
         ga.mg.omega = opt.smooth_omega > 0.0 ? opt.smooth_omega : 0.7;
         ga.mg.lv[0] = MgLevel<VT>{D.d_rowPtr, D.d_colIdx, (const VT*)W.J, (const VT*)W.Dinv, D.d_instNode0, BS->d_mask0,
-                                  (VT*)W.t, nullptr, (VT*)W.s};
+                                  (VT*)W.t, nullptr, (VT*)W.s, (VT*)W.x2};
         for (size_t l = 1; l < BS->levels.size(); ++l) {
             Level& L = BS->levels[l];
             ga.mg.lv[l] = MgLevel<VT>{L.disc->d_rowPtr, L.disc->d_colIdx, (const VT*)L.J, (const VT*)L.Dinv, L.d_node0, L.d_mask,
-                                      (VT*)L.x, (VT*)L.r, (VT*)L.s};
+                                      (VT*)L.x, (VT*)L.r, (VT*)L.s, (VT*)L.x2};
         }
     }
 

@@ -411,12 +411,9 @@ template <int BN, int STAGES>
 cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, float* C, int M, int N, int K, int splits, int kChunk, int* err,
                         cudaStream_t s) {
     using S = nsfv1::tc::GemmSmem<BN, STAGES>;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(nsfv1::tc::k_gemm_bf16_tn<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kBytes);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    // per launch: the attribute belongs to the current device
+    cudaError_t e = cudaFuncSetAttribute(nsfv1::tc::k_gemm_bf16_tn<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kBytes);
+    if (e != cudaSuccess) return e;
     dim3 grid(M / nsfv1::tc::BM, N / BN, splits);
     nsfv1::tc::k_gemm_bf16_tn<BN, STAGES><<<grid, 128, S::kBytes, s>>>(a, b, C, M, N, K, kChunk, err);
     return cudaGetLastError();
@@ -446,14 +443,10 @@ int gemm_bf16(const bf16* A, const bf16* B, float* C, int M, int N, int K, int s
 }
 
 int g_num_sms() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 148;
-    }
-    return n;
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 152;
 }
 
 }  // namespace
@@ -766,9 +759,14 @@ int nsfv1_mlp_predict(nsfv1_mlp* m, int64_t n_points, const float* xy, int n_slo
 }
 
 int nsfv1_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* C, int splits, void* stream) {
-    static int* err = nullptr;
+    // status word of the bounded waits, one per device
+    static int* errs[64] = {nullptr};
     static std::mutex mu;
     std::lock_guard<std::mutex> g(mu);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return NSFV1_ERR_ARGUMENT;
+    int*& err = errs[dev];
     if (!err && cudaMalloc(&err, 4) != cudaSuccess) return NSFV1_ERR_CUDA;
     cudaStream_t s = (cudaStream_t)stream;
     cudaMemsetAsync(err, 0, 4, s);

@@ -38,25 +38,26 @@ struct DFloat {
     float hi, lo;
 };
 
-// x = xh + xl (+ |x| 2^-47): both floats from the bits of x, no FP64 instruction
+// x = xh + xl (+ |x| 2^-47): both floats from the bits of x by integer operations
+// only (GB300 has little FP64 throughput, and a conversion would use it).
+// |x| < 2^-126 flushes to 0; |x| >= 2^128 becomes +-inf; nan stays nan.
 __device__ __forceinline__ void split_double(double x, float& xh, float& xl) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
-    const unsigned e = (unsigned)(u >> 52) & 0x7FFu;
-    const unsigned sgn = (unsigned)(u >> 63) << 31;
-    if (e < 897u || e > 1150u) {   // 0, subnormal, tiny, huge, inf or nan: one conversion
-        xh = (float)x;
-        xl = 0.f;
-        return;
-    }
-    const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
-    xh = __uint_as_float(sgn | ((e - 896u) << 23) | (unsigned)(m >> 29));
-    const unsigned r = (unsigned)(m & 0x1FFFFFFFull);   // the 29 mantissa bits below xh
-    if (e < 949u || r == 0u) {
-        xl = 0.f;   // |x| < 2^-74: the remainder is below float range
-        return;
-    }
-    const float scale = __uint_as_float((e - 1075u + 127u) << 23);   // 2^(e - 1075)
-    xl = __uint_as_float(__float_as_uint((float)r * scale) | sgn);
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned e = (hi >> 20) & 0x7FFu;
+    const unsigned sgn = hi & 0x80000000u;
+    const unsigned mh = hi & 0xFFFFFu;                    // top 20 mantissa bits
+    // leading 23 mantissa bits: mh (20) and the top 3 bits of lo
+    const unsigned m23 = (mh << 3) | (lo >> 29);
+    const unsigned r = lo & 0x1FFFFFFFu;                  // the 29 mantissa bits below them
+    unsigned hbits;
+    if (e >= 897u && e <= 1150u) hbits = sgn | ((e - 896u) << 23) | m23;
+    else if (e > 1150u) hbits = sgn | 0x7F800000u | ((e == 0x7FFu && (mh | lo)) ? 0x400000u : 0u);
+    else hbits = sgn;
+    xh = __uint_as_float(hbits);
+    // xl = +-r 2^(e - 1075) when that is a normal float (e >= 949), else 0
+    const bool has_lo = (e >= 949u) && (e <= 1150u) && (r != 0u);
+    const float scale = __uint_as_float(((has_lo ? e : 1075u) - 1075u + 127u) << 23);
+    xl = has_lo ? __uint_as_float(__float_as_uint(__uint2float_rn(r) * scale) | sgn) : 0.f;
 }
 
 // a + b exactly as s + err (Knuth's TwoSum; _rn intrinsics keep the compiler
@@ -170,10 +171,11 @@ __global__ void __launch_bounds__(256) k_bsr_mv(int64_t nRows, const int32_t* __
     const int lane = threadIdx.x % G;
     // rows past the end run the (empty) loop so every lane reaches the shuffles
     const bool valid = row < nRows;
-    const int64_t q0 = valid ? rowPtr[row] : 0, q1 = valid ? rowPtr[row + 1] : 0;
+    // block indices fit in 32 bits (the pattern is built with int32 row pointers)
+    const int q0 = valid ? rowPtr[row] : 0, q1 = valid ? rowPtr[row + 1] : 0;
     RowAcc<VT, XT, b> acc;
     acc.zero();
-    for (int64_t q = q0 + lane; q < q1; q += G) acc.block(vals + q * (b * b), x + (int64_t)__ldg(colIdx + q) * b);
+    for (int q = q0 + lane; q < q1; q += G) acc.block(vals + (size_t)q * (b * b), x + (size_t)__ldg(colIdx + q) * b);
     acc.template reduce<G>();
     if (valid && lane == 0) {
 #pragma unroll
