@@ -115,7 +115,8 @@ __device__ __forceinline__ void block_row_acc(const VT* __restrict__ vals, const
 // lane group and trip: the row pointers, column indices, blocks and x entries of
 // U rows (two blocks per lane unrolled, predicated) are all requested before the
 // first is used, so each trip pays one memory latency instead of U; longer rows
-// finish in a remainder loop. epi(local row, acc) receives the row sums on lane 0.
+// finish in a remainder loop. epi(local row, component c, acc) runs on lane c < b
+// of the group with the row sums (spreading the epilogue over b lanes).
 template <typename VT, int b, int G, int U, typename Epi>
 __device__ __forceinline__ void rows_spmv(const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx,
                                           const VT* __restrict__ vals, int64_t row0, int64_t nn, const VT* __restrict__ xin,
@@ -159,12 +160,13 @@ __device__ __forceinline__ void rows_spmv(const int32_t* __restrict__ rowPtr, co
             if (q1[u] - q0[u] > KB * G) block_row_acc<VT, b, G>(vals, colIdx, q0[u] + KB * G, q1[u], lane, xin, xoff, acc[u]);
 #pragma unroll
         for (int u = 0; u < U; ++u) {
+            // butterfly: every lane of the group gets the row sums; lane c < b handles component c
 #pragma unroll
             for (int off = G / 2; off > 0; off >>= 1)
 #pragma unroll
-                for (int r = 0; r < b; ++r) acc[u][r] += __shfl_down_sync(0xffffffffu, acc[u][r], off, G);
+                for (int r = 0; r < b; ++r) acc[u][r] += __shfl_xor_sync(0xffffffffu, acc[u][r], off, G);
             const int64_t lr = ctid / G + (it * U + u) * groups;
-            if (lr < nn && lane == 0) epi(lr, acc[u]);
+            if (lr < nn && lane < b) epi(lr, lane, acc[u]);
         }
     }
 }
@@ -223,9 +225,11 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
 
         // y = M t  (rows of this instance; G lanes per block row, uniform trip count)
         auto spmv = [&](const VT* __restrict__ xin, VT* __restrict__ yout) {
-            rows_spmv<VT, b, G, 4>(A.rowPtr, A.colIdx, A.vals, node0, nNode, xin, o, ctid, cth, [&](int64_t lr, const VT (&acc)[b]) {
+            rows_spmv<VT, b, G, 4>(A.rowPtr, A.colIdx, A.vals, node0, nNode, xin, o, ctid, cth, [&](int64_t lr, int c, const VT (&acc)[b]) {
+                VT v = acc[0];
 #pragma unroll
-                for (int r = 0; r < b; ++r) yout[lr * b + r] = acc[r];
+                for (int r = 1; r < b; ++r) v = (c == r) ? acc[r] : v;
+                yout[lr * b + c] = v;
             });
         };
         // point-block Jacobi: out = Dm (in) (per node, optionally damped / accumulated)
@@ -257,9 +261,11 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
         // level SpMV with residual epilogue: res = rhs - M_l x  (rhs == nullptr: res = M_l x)
         auto lspmv = [&](const MgLevel<VT>& L, int64_t n0, int64_t nn, const VT* __restrict__ xin, const VT* __restrict__ rhsl,
                          VT* __restrict__ res) {
-            rows_spmv<VT, b, G, 4>(L.rowPtr, L.colIdx, L.vals, n0, nn, xin, n0 * b, me(), nth(), [&](int64_t lr, const VT (&acc)[b]) {
+            rows_spmv<VT, b, G, 4>(L.rowPtr, L.colIdx, L.vals, n0, nn, xin, n0 * b, me(), nth(), [&](int64_t lr, int c, const VT (&acc)[b]) {
+                VT v = acc[0];
 #pragma unroll
-                for (int r = 0; r < b; ++r) res[lr * b + r] = rhsl ? rhsl[lr * b + r] - acc[r] : acc[r];
+                for (int r = 1; r < b; ++r) v = (c == r) ? acc[r] : v;
+                res[lr * b + c] = rhsl ? rhsl[lr * b + c] - v : v;
             });
         };
         // instance levels: cells per side, first node on each level
@@ -300,17 +306,14 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                 const VT* rl = lr(l);
                 const VT* Dm = lD(l);
                 rows_spmv<VT, b, G, 4>(L.rowPtr, L.colIdx, L.vals, ln0[l], lnn(l), xc, ln0[l] * b, me(), nth(),
-                                       [&](int64_t r0, const VT (&acc)[b]) {
+                                       [&](int64_t r0, int c, const VT (&acc)[b]) {
                                            VT sv[b];
 #pragma unroll
                                            for (int j = 0; j < b; ++j) sv[j] = rl[r0 * b + j] - acc[j];
+                                           VT a = VT(0);
 #pragma unroll
-                                           for (int i = 0; i < b; ++i) {
-                                               VT a = VT(0);
-#pragma unroll
-                                               for (int j = 0; j < b; ++j) a += Dm[r0 * b * b + i * b + j] * sv[j];
-                                               xn[r0 * b + i] = xc[r0 * b + i] + om * a;
-                                           }
+                                           for (int j = 0; j < b; ++j) a += Dm[r0 * b * b + c * b + j] * sv[j];
+                                           xn[r0 * b + c] = xc[r0 * b + c] + om * a;
                                        });
                 inSec[l] = !inSec[l];
                 bar();

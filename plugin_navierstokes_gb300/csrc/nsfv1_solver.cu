@@ -24,7 +24,9 @@ static constexpr int kRedThreads = 256;
 // blocks l, l+G, ... of the row (consecutive lanes read consecutive blocks)
 // and applies each whole b x b block to the b entries of x it multiplies, so
 // every matrix entry costs one fused multiply-add; the group then reduces its
-// b row sums with shuffles in a fixed order.
+// b row sums with butterfly shuffles in a fixed order, and lane r stores component r
+// (a warp-wide FP64 instruction costs its full issue time however few lanes are
+// active, so the conversions are spread over the lanes).
 //
 // GB300 issues only two FP64 instructions per clock per SM, so the FP32-matrix
 // variant keeps its arithmetic off the FP64 pipe: x (FP64) is split into two
@@ -88,14 +90,20 @@ struct RowAcc<double, XT, b> {
 #pragma unroll
             for (int j = 0; j < b; ++j) v[i] = fma(__ldg(blk + i * b + j), x[j], v[i]);
     }
+    // butterfly: every lane of the group ends with the sums
     template <int G>
     __device__ __forceinline__ void reduce() {
 #pragma unroll
         for (int off = G / 2; off > 0; off >>= 1)
 #pragma unroll
-            for (int i = 0; i < b; ++i) v[i] += __shfl_down_sync(0xffffffffu, v[i], off, G);
+            for (int i = 0; i < b; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], off, G);
     }
-    __device__ __forceinline__ double value(int i) const { return v[i]; }
+    __device__ __forceinline__ double value(int i) const {
+        double r = v[0];
+#pragma unroll
+        for (int k = 1; k < b; ++k) r = (i == k) ? v[k] : r;
+        return r;
+    }
 };
 
 template <int b>
@@ -127,14 +135,23 @@ struct RowAcc<float, double, b> {
         for (int off = G / 2; off > 0; off >>= 1)
 #pragma unroll
             for (int i = 0; i < b; ++i) {
-                const float oh = __shfl_down_sync(0xffffffffu, v[i].hi, off, G);
-                const float ol = __shfl_down_sync(0xffffffffu, v[i].lo, off, G);
+                const float oh = __shfl_xor_sync(0xffffffffu, v[i].hi, off, G);
+                const float ol = __shfl_xor_sync(0xffffffffu, v[i].lo, off, G);
                 float e;
                 v[i].hi = two_sum(v[i].hi, oh, e);
                 v[i].lo += e + ol;
             }
     }
-    __device__ __forceinline__ double value(int i) const { return (double)v[i].hi + (double)v[i].lo; }
+    // component i in FP64: the float pair is selected first, so a lane converts one value
+    __device__ __forceinline__ double value(int i) const {
+        float h = v[0].hi, l = v[0].lo;
+#pragma unroll
+        for (int k = 1; k < b; ++k) {
+            h = (i == k) ? v[k].hi : h;
+            l = (i == k) ? v[k].lo : l;
+        }
+        return (double)h + (double)l;
+    }
 };
 
 template <int b>
@@ -158,14 +175,20 @@ struct RowAcc<float, float, b> {
 #pragma unroll
         for (int off = G / 2; off > 0; off >>= 1)
 #pragma unroll
-            for (int i = 0; i < b; ++i) v[i] += __shfl_down_sync(0xffffffffu, v[i], off, G);
+            for (int i = 0; i < b; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], off, G);
     }
-    __device__ __forceinline__ float value(int i) const { return v[i]; }
+    __device__ __forceinline__ float value(int i) const {
+        float r = v[0];
+#pragma unroll
+        for (int k = 1; k < b; ++k) r = (i == k) ? v[k] : r;
+        return r;
+    }
 };
 
 template <typename VT, typename XT, int b, int G>
 __global__ void __launch_bounds__(256) k_bsr_mv(int64_t nRows, const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx,
                                                 const VT* __restrict__ vals, const XT* __restrict__ x, XT* __restrict__ y) {
+    static_assert(G >= b, "a lane per row component");
     const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t row = gid / G;
     const int lane = threadIdx.x % G;
@@ -177,10 +200,8 @@ __global__ void __launch_bounds__(256) k_bsr_mv(int64_t nRows, const int32_t* __
     acc.zero();
     for (int q = q0 + lane; q < q1; q += G) acc.block(vals + (size_t)q * (b * b), x + (size_t)__ldg(colIdx + q) * b);
     acc.template reduce<G>();
-    if (valid && lane == 0) {
-#pragma unroll
-        for (int r = 0; r < b; ++r) y[row * b + r] = (XT)acc.value(r);
-    }
+    // lanes 0..b-1 of the group each store one component (G >= b)
+    if (valid && lane < b) y[row * b + lane] = (XT)acc.value(lane);
 }
 
 template <typename VT, typename OT, int b>
