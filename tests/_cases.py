@@ -17,7 +17,7 @@ REF = {
 }
 
 # (upwind, stabilisation, diff length, transient, exact jacobian, peclet, laplace, stokes, source)
-CONFIGS = [
+DISC_CASES = [
     ("full", "fields", "raw", False, 0.0, False, False, False, False),
     ("lps", "flow", "raw", False, 0.0, False, False, False, False),
     ("no", "fields", "fivepoint", True, 1.0, False, False, False, True),
@@ -56,7 +56,7 @@ def random_local_u(roid: int, n: int, seed: int, zero_frac: float = 0.0) -> np.n
 
 
 def configure(disc, dim: int, cfg) -> None:
-    """Apply a CONFIGS entry to a disc (oracle or product: same method names)."""
+    """Apply a DISC_CASES entry to a disc (oracle or product: same method names)."""
     up, stab, dl, transient, exact, peclet, laplace, stokes, source = cfg
     disc.set_kinematic_viscosity(0.01 if dim == 2 else 0.0025)
     disc.set_density(1.0 if not source else 1.3)

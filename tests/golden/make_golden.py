@@ -16,7 +16,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 import oracle  # noqa: E402
-from _cases import CONFIGS, DIM, ROIDS, configure, random_elements, random_local_u  # noqa: E402
+from _cases import DISC_CASES, DIM, ROIDS, configure, random_elements, random_local_u  # noqa: E402
 from plugin_navierstokes_gb300 import mesh  # noqa: E402
 
 N_ELEM = 4
@@ -27,7 +27,7 @@ def element_fixtures():
     out = {}
     for tname, roid in ROIDS.items():
         dim = DIM[roid]
-        for ci, cfg in enumerate(CONFIGS):
+        for ci, cfg in enumerate(DISC_CASES):
             seed = 1000 * roid + ci
             corners = random_elements(roid, N_ELEM, seed)
             u = random_local_u(roid, N_ELEM, seed + 1, zero_frac=0.25)
@@ -50,7 +50,7 @@ def mesh_fixtures():
     # 8 x 8 cavity, full upwind + FIELDS, nu = 0.01, at a seeded state
     roid, X, C = mesh.structured_quads(8)
     o = oracle.Oracle(2)
-    configure(o, 2, CONFIGS[0])
+    configure(o, 2, DISC_CASES[0])
     o.set_mesh(roid, X, C)
     dofs, vals = mesh.cavity_dirichlet(X, 1.0)
     o.set_dirichlet(dofs, vals)
@@ -64,7 +64,7 @@ def mesh_fixtures():
     # 3 x 3 x 3 hexes, LPS + FLOW, nu = 0.0025, solenoidal state
     roid, X, C = mesh.structured_hexes(3)
     o = oracle.Oracle(3)
-    configure(o, 3, CONFIGS[1])
+    configure(o, 3, DISC_CASES[1])
     o.set_mesh(roid, X, C)
     U = mesh.solenoidal_state(X, seed=1)
     D, J = o.assemble(U)
@@ -74,7 +74,7 @@ def mesh_fixtures():
     # jittered triangles 6 x 6, transient full + FIELDS
     roid, X, C = mesh.jittered_triangles(6, seed=2)
     o = oracle.Oracle(2)
-    configure(o, 2, CONFIGS[0])
+    configure(o, 2, DISC_CASES[0])
     o.set_mesh(roid, X, C)
     dofs, vals = mesh.cavity_dirichlet(X, 1.0)
     o.set_dirichlet(dofs, vals)

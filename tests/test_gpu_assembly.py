@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
-from _cases import CONFIGS, DIM, NSH, ROIDS, cfg_name, configure, random_elements, random_local_u, rel_err
+from _cases import DISC_CASES, DIM, NSH, ROIDS, cfg_name, configure, random_elements, random_local_u, rel_err
 from plugin_navierstokes_gb300 import NavierStokesFV1, NSFV1Error, mesh
 
 pytestmark = pytest.mark.gpu
@@ -35,23 +35,23 @@ def _gpu_elem(cuda, roid, cfg, corners, u, uo, dt=0.01):
 
 
 @pytest.mark.parametrize("tname", list(ROIDS))
-@pytest.mark.parametrize("ci", range(len(CONFIGS)))
+@pytest.mark.parametrize("ci", range(len(DISC_CASES)))
 def test_element_callbacks_match_golden(cuda, tname, ci):
     g = np.load(os.path.join(GOLDEN, "elements.npz"))
     roid = ROIDS[tname]
     key = f"{tname}_{ci}"
     uo = g[key + "_uold"] if (key + "_uold") in g else None
-    r = _gpu_elem(cuda, roid, CONFIGS[ci], g[key + "_corners"], g[key + "_u"], uo)
+    r = _gpu_elem(cuda, roid, DISC_CASES[ci], g[key + "_corners"], g[key + "_u"], uo)
     for k in ("defA", "jacA", "defM", "jacM", "rhs"):
-        assert rel_err(r[k], g[key + "_" + k]) <= TOL64, (key, cfg_name(CONFIGS[ci]), k, rel_err(r[k], g[key + "_" + k]))
+        assert rel_err(r[k], g[key + "_" + k]) <= TOL64, (key, cfg_name(DISC_CASES[ci]), k, rel_err(r[k], g[key + "_" + k]))
 
 
 @pytest.mark.parametrize("tname", list(ROIDS))
-@pytest.mark.parametrize("ci", range(len(CONFIGS)))
+@pytest.mark.parametrize("ci", range(len(DISC_CASES)))
 def test_element_callbacks_match_oracle_random(cuda, tname, ci):
     roid = ROIDS[tname]
     dim = DIM[roid]
-    cfg = CONFIGS[ci]
+    cfg = DISC_CASES[ci]
     n = 257
     corners = random_elements(roid, n, 9000 + 17 * ci + roid)
     u = random_local_u(roid, n, 9100 + ci, zero_frac=0.1)
@@ -66,11 +66,11 @@ def test_element_callbacks_match_oracle_random(cuda, tname, ci):
 
 def _setup_mesh_pair(name, g):
     if name == "quad":
-        roid, dim, cfg, U, Uo, dt = 3, 2, CONFIGS[0], g["quad_U"], None, 0.0
+        roid, dim, cfg, U, Uo, dt = 3, 2, DISC_CASES[0], g["quad_U"], None, 0.0
     elif name == "hex":
-        roid, dim, cfg, U, Uo, dt = 8, 3, CONFIGS[1], g["hex_U"], None, 0.0
+        roid, dim, cfg, U, Uo, dt = 8, 3, DISC_CASES[1], g["hex_U"], None, 0.0
     else:
-        roid, dim, cfg, U, Uo, dt = 2, 2, CONFIGS[0], g["tri_U"], g["tri_Uold"], 0.01
+        roid, dim, cfg, U, Uo, dt = 2, 2, DISC_CASES[0], g["tri_U"], g["tri_Uold"], 0.01
     return roid, dim, cfg, U, Uo, dt
 
 
@@ -117,7 +117,7 @@ def test_global_assembly_matches_oracle(cuda, gen, cfgi):
     roid, X, C = {"quads": lambda: mesh.structured_quads(24), "hexes": lambda: mesh.structured_hexes(6),
                   "tris": lambda: mesh.jittered_triangles(16, seed=4)}[gen]()
     dim = DIM[roid]
-    cfg = CONFIGS[cfgi]
+    cfg = DISC_CASES[cfgi]
     b = dim + 1
     U = mesh.solenoidal_state(X, seed=7) if dim == 3 else (mesh.uniform(8, X.shape[0] * 3) * 2 - 1).reshape(-1, 3)
     Uo = (U * 0.9) if cfg[3] else None
@@ -142,8 +142,8 @@ def test_global_assembly_matches_oracle(cuda, gen, cfgi):
 def test_bsr_spmv_matches_oracle(cuda):
     import torch
     g = np.load(os.path.join(GOLDEN, "meshes.npz"))
-    o = oracle.Oracle(3); configure(o, 3, CONFIGS[1]); o.set_mesh(8, g["hex_coords"], g["hex_conn"])
-    d = NavierStokesFV1(dim=3); configure(d, 3, CONFIGS[1]); d.set_mesh(8, g["hex_coords"], g["hex_conn"])
+    o = oracle.Oracle(3); configure(o, 3, DISC_CASES[1]); o.set_mesh(8, g["hex_coords"], g["hex_conn"])
+    d = NavierStokesFV1(dim=3); configure(d, 3, DISC_CASES[1]); d.set_mesh(8, g["hex_coords"], g["hex_conn"])
     x = mesh.uniform(5, g["hex_U"].size) - 0.5
     y_ref = o.bsr_mv(g["hex_J"], x)
     for dt_ in (torch.float64, torch.float32):
@@ -177,7 +177,7 @@ def test_block_jacobi_matches_numpy(cuda, gen):
     roid, X, C = {"quads": lambda: mesh.structured_quads(12), "hexes": lambda: mesh.structured_hexes(4)}[gen]()
     dim = DIM[roid]
     b = dim + 1
-    d = NavierStokesFV1(dim=dim); configure(d, dim, CONFIGS[0] if dim == 2 else CONFIGS[1]); d.set_mesh(roid, X, C)
+    d = NavierStokesFV1(dim=dim); configure(d, dim, DISC_CASES[0] if dim == 2 else DISC_CASES[1]); d.set_mesh(roid, X, C)
     U = mesh.solenoidal_state(X, seed=3) if dim == 3 else (mesh.uniform(8, X.shape[0] * 3) * 2 - 1).reshape(-1, 3)
     rp, ci = d.pattern()
     tu = torch.tensor(U.ravel(), dtype=torch.float64, device=cuda)

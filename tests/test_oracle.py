@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle
-from _cases import CONFIGS, DIM, NSH, ROIDS, configure, random_elements, random_local_u, rel_err
+from _cases import DISC_CASES, DIM, NSH, ROIDS, configure, random_elements, random_local_u, rel_err
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -79,7 +79,7 @@ def test_global_assembly_is_sum_of_element_callbacks():
     from plugin_navierstokes_gb300 import mesh
     roid, X, C = mesh.jittered_triangles(4, seed=5)
     o = oracle.Oracle(2)
-    configure(o, 2, CONFIGS[0])
+    configure(o, 2, DISC_CASES[0])
     o.set_mesh(roid, X, C)
     U = (mesh.uniform(3, X.shape[0] * 3) * 2 - 1).reshape(-1, 3)
     D, J = o.assemble(U)
@@ -131,7 +131,7 @@ def test_pattern_and_coloring_properties(gen):
 def test_oracle_matches_golden_elements():
     g = np.load(os.path.join(GOLDEN, "elements.npz"))
     for tname, roid in ROIDS.items():
-        for ci, cfg in enumerate(CONFIGS):
+        for ci, cfg in enumerate(DISC_CASES):
             key = f"{tname}_{ci}"
             o = oracle.Oracle(DIM[roid])
             configure(o, DIM[roid], cfg)
@@ -145,7 +145,7 @@ def test_oracle_matches_golden_meshes():
     from plugin_navierstokes_gb300 import mesh
     g = np.load(os.path.join(GOLDEN, "meshes.npz"))
     o = oracle.Oracle(2)
-    configure(o, 2, CONFIGS[0])
+    configure(o, 2, DISC_CASES[0])
     o.set_mesh(3, g["quad_coords"], g["quad_conn"])
     o.set_dirichlet(g["quad_dofs"], g["quad_dvals"])
     D, J = o.assemble(g["quad_U"])
@@ -153,7 +153,7 @@ def test_oracle_matches_golden_meshes():
     rp, ci = o.pattern()
     assert np.array_equal(rp, g["quad_rowptr"]) and np.array_equal(ci, g["quad_colidx"])
     o3 = oracle.Oracle(3)
-    configure(o3, 3, CONFIGS[1])
+    configure(o3, 3, DISC_CASES[1])
     o3.set_mesh(8, g["hex_coords"], g["hex_conn"])
     D, J = o3.assemble(g["hex_U"])
     assert rel_err(D, g["hex_D"]) < 1e-13 and rel_err(J, g["hex_J"]) < 1e-13

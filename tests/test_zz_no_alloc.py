@@ -12,7 +12,7 @@ failure has run every other test.
 import numpy as np
 import pytest
 
-from _cases import CONFIGS, DIM, configure, rel_err
+from _cases import DISC_CASES, DIM, configure, rel_err
 from plugin_navierstokes_gb300 import NavierStokesFV1, _capi, mesh
 
 pytestmark = pytest.mark.gpu
@@ -35,7 +35,7 @@ def test_noalloc_matches_allocating_entry_point(cuda, gen, jdtype):
     dim = DIM[roid]
     b = dim + 1
     d = NavierStokesFV1(dim=dim)
-    configure(d, dim, CONFIGS[0] if dim == 2 else CONFIGS[1])
+    configure(d, dim, DISC_CASES[0] if dim == 2 else DISC_CASES[1])
     d.set_mesh(roid, X, C)
     U = mesh.solenoidal_state(X, seed=3) if dim == 3 else (mesh.uniform(8, X.shape[0] * 3) * 2 - 1).reshape(-1, 3)
     nnzb = d.pattern_info()["nnz_blocks"]
@@ -59,7 +59,7 @@ def test_noalloc_rejects_meshes_above_the_limit(cuda):
     roid, X, C = mesh.structured_quads(n)
     assert X.shape[0] > _capi.NOALLOC_MAX_NODES
     d = NavierStokesFV1(dim=2)
-    configure(d, 2, CONFIGS[0])
+    configure(d, 2, DISC_CASES[0])
     d.set_mesh(roid, X, C)
     nnzb = d.pattern_info()["nnz_blocks"]
     J = torch.zeros(nnzb * 9, dtype=torch.float64, device=cuda)
