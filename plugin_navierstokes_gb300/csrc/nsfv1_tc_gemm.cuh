@@ -191,7 +191,8 @@ __global__ void __launch_bounds__(128, 1)
     }
     __syncwarp();
     // epilogue
-    const bool done = mbar_wait(doneBar, 0);
+    // warp-uniform: tcgen05.ld below is a .sync.aligned instruction
+    const bool done = __all_sync(0xffffffffu, mbar_wait(doneBar, 0));
     fence_after();
     if (!done) ok = false;
     if (done && nk > 0) {
