@@ -185,3 +185,52 @@ def test_full_upwind_limit_cycle_64():
         U = U - spl.spsolve(A, D)
     rel = np.array(hist) / hist[0]
     assert rel[-1] > 1e-4 and abs(rel[-1] - rel[-3]) < 1e-6 * rel[-1] * 1e3
+
+
+@pytest.mark.parametrize("roid", [2, 3, 4, 8])
+def test_full_newton_jacobian_is_exact_without_upwind_and_stabilisation(roid):
+    """Navier-Stokes with no upwind (flux through ip interpolation), no
+    stabilisation and the full-Newton factor 1: the convective flux is
+    rho (u_ip . n) u_ip and the reference's fixpoint + full-Newton parts of
+    add_jac_A_elem (navier_stokes_fv1.cpp:377-550) form its exact derivative."""
+    dim = DIM[roid]
+    o = oracle.Oracle(dim)
+    o.set_kinematic_viscosity(0.01)
+    o.set_density(1.1)
+    o.set_upwind("no")
+    o.set_stabilization("without")
+    o.set_exact_jacobian(1.0)
+    corners = random_elements(roid, 2, 500 + roid)
+    u = random_local_u(roid, 2, 501 + roid)
+    r = o.elem_batch(roid, corners, u, None, 0.0, want=("defA", "jacA"))
+    n = u.shape[1]
+    for e in range(2):
+        J = r["jacA"][e].reshape(n, n)
+        Jfd = np.zeros((n, n))
+        h = 1e-6
+        for j in range(n):
+            up = u.copy(); um = u.copy()
+            up[e, j] += h; um[e, j] -= h
+            dp = o.elem_batch(roid, corners, up, None, 0.0, want=("defA",))["defA"][e]
+            dm = o.elem_batch(roid, corners, um, None, 0.0, want=("defA",))["defA"][e]
+            Jfd[:, j] = (dp - dm) / (2 * h)
+        assert rel_err(J, Jfd) < 1e-7
+
+
+@pytest.mark.parametrize("roid", [2, 3, 4, 8])
+@pytest.mark.parametrize("up,stab", [("lps", "flow"), ("full", "fields"), ("skewed", "fields")])
+def test_assembly_is_translation_invariant(roid, up, stab):
+    """Moving every corner by the same vector changes no geometric quantity the
+    discretisation uses, so the element defect and Jacobian agree to rounding."""
+    dim = DIM[roid]
+    o = oracle.Oracle(dim)
+    o.set_kinematic_viscosity(0.01)
+    o.set_upwind(up)
+    o.set_stabilization(stab)
+    corners = random_elements(roid, 3, 600 + roid)
+    u = random_local_u(roid, 3, 601 + roid)
+    shift = np.array([0.37, -1.25, 2.5][:dim])
+    r0 = o.elem_batch(roid, corners, u, None, 0.0, want=("defA", "jacA"))
+    r1 = o.elem_batch(roid, corners + shift, u, None, 0.0, want=("defA", "jacA"))
+    for k in ("defA", "jacA"):
+        assert rel_err(r1[k], r0[k]) < 1e-11, (k, rel_err(r1[k], r0[k]))
