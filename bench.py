@@ -114,8 +114,10 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def cpu_baseline_run(roid, X, C, U, nthreads, steps=1):
-    """The oracle (scalar C++ restatement of the reference path) on the host cores."""
+def cpu_baseline_run(roid, X, C, U, nthreads):
+    """The oracle (scalar C++ restatement of the reference path) on the host cores: one
+    defect + Jacobian assembly of the full mesh, timed; returns (elements/s, oracle, D, J)
+    so that the same outputs check the GPU's."""
     import oracle
 
     o = oracle.Oracle(3)
@@ -124,10 +126,70 @@ def cpu_baseline_run(roid, X, C, U, nthreads, steps=1):
     o.set_stabilization(STAB)
     o.set_mesh(roid, X, C)
     t0 = time.perf_counter()
-    for _ in range(steps):
-        o.assemble(U, defect=True, jacobian=True, nthreads=nthreads)
-    dt = (time.perf_counter() - t0) / steps
-    return C.shape[0] / dt
+    Dref, Jref = o.assemble(U, defect=True, jacobian=True, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return C.shape[0] / dt, o, Dref, Jref
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b| over whole arrays (the parity tests' measure), in chunks."""
+    import numpy as np
+
+    num, den = 0.0, 0.0
+    step = 1 << 24
+    for i in range(0, b.size, step):
+        x, y = a[i:i + step].astype(np.float64), b[i:i + step]
+        num = max(num, float(np.abs(x - y).max()))
+        den = max(den, float(np.abs(y).max()))
+    return num / den if den > 0 else num
+
+
+def oracle_check(o, d, Dref, Jref, D, J64, J32):
+    """The FP64 oracle's full-size outputs against the GPU's: sparsity pattern and element
+    colouring bit-exact, defect and FP64 Jacobian within 1e-12, FP32 Jacobian within 2e-5
+    (max |gpu - oracle| / max |oracle| per array)."""
+    import numpy as np
+
+    rp, ci = d.pattern()
+    orp, oci = o.pattern()
+    col = d.coloring()
+    ocol, _ = o.coloring()
+    out = {"pattern_bit_exact": bool(np.array_equal(rp, orp) and np.array_equal(ci, oci)),
+           "coloring_bit_exact": bool(np.array_equal(col, ocol)),
+           "oracle_err_defect": rel_err(D, Dref), "oracle_err_jacobian_f64": rel_err(J64, Jref),
+           "oracle_err_jacobian_f32": rel_err(J32, Jref), "tolerance_f64": 1e-12, "tolerance_f32": 2e-5}
+    out["pass"] = bool(out["pattern_bit_exact"] and out["coloring_bit_exact"] and out["oracle_err_defect"] <= 1e-12
+                       and out["oracle_err_jacobian_f64"] <= 1e-12 and out["oracle_err_jacobian_f32"] <= 2e-5)
+    return out
+
+
+def count_launches(fn):
+    """Kernel launches of one call of fn, counted by the CUDA profiler interface
+    (torch.profiler / CUPTI): {kernel name: launches} of this library's kernels (namespace
+    nsfv1), plus the total of all kernels. None if the profiler is unavailable."""
+    import torch
+
+    try:
+        from torch.profiler import ProfilerActivity, profile
+
+        torch.cuda.synchronize()
+        with profile(activities=[ProfilerActivity.CUDA]) as prof:
+            fn()
+            torch.cuda.synchronize()
+        names = {}
+        total = 0
+        for e in prof.events():
+            if getattr(e, "device_type", None) != torch.autograd.DeviceType.CUDA:
+                continue
+            if "memset" in e.name.lower() or "memcpy" in e.name.lower():
+                continue
+            total += 1
+            if "nsfv1" in e.name:
+                key = e.name.split("(")[0].replace("void ", "")
+                names[key] = names.get(key, 0) + 1
+        return {"ours": sum(names.values()), "all_kernels": total, "by_kernel": names}
+    except Exception as ex:  # noqa: BLE001 - the count is evidence, not a requirement of the run
+        return {"ours": None, "error": str(ex)[:200]}
 
 
 def run_reference(args):
@@ -220,9 +282,12 @@ def main():
     J32 = torch.empty(nnzb * b * b, dtype=torch.float32, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    def step(J):
+    def step64():
+        d.assemble_defect_jacobian(tu, D, J64, stream=stream)
+
+    def step32():
         d.assemble_defect(tu, D, stream=stream)
-        d.assemble_jacobian(tu, J, stream=stream)
+        d.assemble_jacobian(tu, J32, stream=stream)
 
     # CTA size of the colour launches from the assembly autotuner
     asm_threads, asm_ms = d.assembly_autotune(tu, "f64", (32, 64, 128), stream=stream)
@@ -230,41 +295,44 @@ def main():
     ev = lambda: torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
-            step(J64)
-            step(J32)
+            step64()
+            step32()
     torch.cuda.synchronize()
 
-    def timed(J, k):
-        """per-step device times (ms) of defect, jacobian, total; L2 flushed before each step"""
-        tdef, tjac = [], []
+    def timed(calls, k):
+        """per-step device times (ms) of each call in calls; L2 flushed before each step"""
+        out = [[] for _ in calls]
         for _ in range(k):
             with torch.cuda.stream(stream):
                 flush.fill_(1.0)
-                e0, e1, e2 = ev(), ev(), ev()
-                e0.record(stream)
-                d.assemble_defect(tu, D, stream=stream)
-                e1.record(stream)
-                d.assemble_jacobian(tu, J, stream=stream)
-                e2.record(stream)
-            e2.synchronize()
-            tdef.append(e0.elapsed_time(e1))
-            tjac.append(e1.elapsed_time(e2))
-        return tdef, tjac
+                evs = [ev() for _ in range(len(calls) + 1)]
+                evs[0].record(stream)
+                for i, c in enumerate(calls):
+                    c()
+                    evs[i + 1].record(stream)
+            evs[-1].synchronize()
+            for i in range(len(calls)):
+                out[i].append(evs[i].elapsed_time(evs[i + 1]))
+        return out
 
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        tdef64, tjac64 = timed(J64, args.steps)
-        tdef32, tjac32 = timed(J32, args.steps)
+        (t64,) = timed([step64], args.steps)
+        tdef32, tjac32 = timed([lambda: d.assemble_defect(tu, D, stream=stream),
+                                lambda: d.assemble_jacobian(tu, J32, stream=stream)], args.steps)
     torch.cuda.synchronize()
-    ms64 = (sum(tdef64) + sum(tjac64)) / args.steps
+    ms64 = sum(t64) / args.steps
     ms32 = (sum(tdef32) + sum(tjac32)) / args.steps
     if world > 1:
         t = torch.tensor([ms64, ms32], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms64, ms32 = t.tolist()
     value = world * n_el / (ms64 * 1e-3)
+    # the separate FP64 defect and Jacobian calls, for comparison with the fused pass
+    tdef64, tjac64 = timed([lambda: d.assemble_defect(tu, D, stream=stream),
+                            lambda: d.assemble_jacobian(tu, J64, stream=stream)], max(2, args.steps // 2))
 
     # e2e through the C ABI with host buffers (pinned): u in, defect + Jacobian out
     hu = torch.tensor(U.ravel(), dtype=torch.float64).pin_memory()
@@ -278,8 +346,7 @@ def main():
             e0, e1 = ev(), ev()
             e0.record(stream)
             du.copy_(hu, non_blocking=True)
-            d.assemble_defect(du, D, stream=stream)
-            d.assemble_jacobian(du, J64, stream=stream)
+            d.assemble_defect_jacobian(du, D, J64, stream=stream)
             hD.copy_(D, non_blocking=True)
             hJ.copy_(J64, non_blocking=True)
             e1.record(stream)
@@ -290,11 +357,18 @@ def main():
     h2d = hu.numel() * 8
     d2h = (hD.numel() + hJ.numel()) * 8
 
-    # roofline of the dominant kernel (the FP64 Jacobian assembly): algorithmic bytes =
-    # Jacobian values written once + u, coordinates, connectivity, block map read once
-    jac_ms = sum(tjac64) / args.steps
-    alg_bytes = nnzb * b * b * 8 + tu.numel() * 8 + X.size * 8 + C.size * 4 + n_el * 64 * 4
-    achieved = alg_bytes / (jac_ms * 1e-3) / 1e9
+    # kernel launches of one step of each mode (counted by the profiler interface, after the timed region)
+    with torch.cuda.stream(stream):
+        launches64 = count_launches(step64)
+        launches32 = count_launches(step32)
+
+    # roofline of the dominant kernel (the fused FP64 defect + Jacobian pass): algorithmic bytes =
+    # Jacobian values and defect written once + u, coordinates, connectivity, block map read once
+    in_bytes = tu.numel() * 8 + X.size * 8 + C.size * 4 + n_el * 64 * 4
+    alg_bytes = nnzb * b * b * 8 + tu.numel() * 8 + in_bytes
+    achieved = alg_bytes / (ms64 * 1e-3) / 1e9
+    jac32_ms = sum(tjac32) / args.steps
+    alg32 = nnzb * b * b * 4 + in_bytes
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -302,41 +376,55 @@ def main():
     except OSError:
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
-    traffic = None
+    prof = {}
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get("jacobian_f64_bytes_per_assembly")
+            prof = json.load(f)
     except OSError:
         pass
+    traffic = prof.get("defect_jacobian_f64_bytes_per_assembly")
+    traffic32 = prof.get("jacobian_f32_bytes_per_assembly")
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    cpu, check = None, None
+    if rank == 0:
+        # the oracle's full-size assembly: the CPU baseline (timed) and the parity check of this run
         nthreads = os.cpu_count() or 1
-        v = cpu_baseline_run(roid, X, C, U, nthreads, steps=1)
-        cpu = {"value": v, "unit": "elems/s", "cores": nthreads, "kind": "port",
-               "sample": f"full {N_CELLS}^3 mesh, one defect + Jacobian assembly (oracle, OpenMP over colours)"}
+        v, o, Dref, Jref = cpu_baseline_run(roid, X, C, U, nthreads)
+        if world == 1 and not args.no_cpu_baseline:
+            cpu = {"value": v, "unit": "elems/s", "cores": nthreads, "kind": "port",
+                   "sample": f"full {N_CELLS}^3 mesh, one defect + Jacobian assembly (oracle, OpenMP over colours)"}
+        check = oracle_check(o, d, Dref, Jref, hD.numpy(), hJ.numpy(), J32.cpu().numpy())
+        del o, Dref, Jref
 
     if rank == 0:
         line = {
             "metric": "assembly elems/s", "value": value, "unit": "elems/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded solenoidal state)",
-            "config": config_dict({"defect_ms": sum(tdef64) / args.steps, "jacobian_ms": jac_ms,
+            "config": config_dict({"step": "one FP64 defect + Jacobian assembly (nsfv1_assemble_defect_jacobian, one pass)",
+                                   "separate_calls_ms": {"defect": sum(tdef64) / len(tdef64), "jacobian": sum(tjac64) / len(tjac64)},
                                    "assembly_cta_threads": asm_threads,
                                    "autotune_ms": dict(zip(("32", "64", "128"), [round(x, 3) for x in asm_ms])),
+                                   "oracle_check": check,
                                    "fp32_jacobian_mode": {"value": world * n_el / (ms32 * 1e-3), "ms_per_step": ms32,
-                                                          "defect_ms": sum(tdef32) / args.steps,
-                                                          "jacobian_ms": sum(tjac32) / args.steps}}),
+                                                          "defect_ms": sum(tdef32) / args.steps, "jacobian_ms": jac32_ms,
+                                                          "roofline": {"bound": "hbm", "kernel": "FP32 Jacobian assembly",
+                                                                       "achieved": alg32 / (jac32_ms * 1e-3) / 1e9, "peak": peak,
+                                                                       "unit": "GB/s", "frac": alg32 / (jac32_ms * 1e-3) / 1e9 / peak,
+                                                                       "algorithmic_bytes": alg32,
+                                                                       "traffic": traffic32,
+                                                                       "traffic_source": prof.get("source_f32")}}}),
             "e2e": {"value": world * n_el / (e2e_ms * 1e-3), "unit": "elems/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-            "roofline": {"bound": "hbm", "kernel": "FP64 Jacobian assembly (8 colour launches)", "achieved": achieved,
-                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "traffic_gbs": (traffic / (jac_ms * 1e-3) / 1e9) if traffic else None,
+            "roofline": {"bound": "hbm", "kernel": "fused FP64 defect + Jacobian assembly (one launch per colour)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "traffic_source": prof.get("source_f64"),
                          "algorithmic_bytes": alg_bytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
-                         "note": "FP64-pipe bound (ncu: FP64 pipe ~70% of active cycles); traffic = ncu DRAM bytes of one "
-                                 "assembly (profiles/traffic.json): each colour re-streams the Jacobian lines it updates"},
+                         "fp64_pipe_active_frac": prof.get("fp64_pipe_active_frac"),
+                         "note": "FP64-pipe bound (GB300: 2 FP64 lanes per clock per SM)"},
             "cpu_baseline": cpu,
-            "gpu_launches": 16 * args.steps,
+            "gpu_launches": (launches64["ours"] * args.steps) if launches64.get("ours") is not None else None,
+            "gpu_launches_per_step": {"f64": launches64, "f32_mode": launches32},
             "clocks": clk.summary(),
         }
         print(json.dumps(line))

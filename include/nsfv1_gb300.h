@@ -131,6 +131,14 @@ int nsfv1_assemble_defect(nsfv1_disc* h, const double* u, const double* u_old, d
  * Replaces the element loop over add_jac_A_elem + add_jac_M_elem
  * (navier_stokes_fv1.cpp:250-595, 781-808) and the matrix insertion. */
 int nsfv1_assemble_jacobian(nsfv1_disc* h, const double* u, const double* u_old, double dt, void* vals, int prec, void* stream);
+/* Defect and Jacobian at the same state (both outputs of the two calls above) in
+ * one pass over the elements: the per-SCVF geometry, upwind shapes and
+ * stabilisation feed both, where the reference evaluates them in each of
+ * add_def_A_elem and add_jac_A_elem (navier_stokes_fv1.cpp:296-309, 645-659).
+ * Same results as nsfv1_assemble_defect + nsfv1_assemble_jacobian; with
+ * NSFV1_F32 values it runs those two. */
+int nsfv1_assemble_defect_jacobian(nsfv1_disc* h, const double* u, const double* u_old, double dt, double* d, void* vals, int prec,
+                                   void* stream);
 /* The reference's per-element callbacks, batched over n independent elements
  * (device arrays): corners[n][nsh][dim], u/u_old[n][b*nsh] (local layout);
  * outputs (each may be NULL) defA, defM, rhs [n][b*nsh] and jacA, jacM
@@ -157,13 +165,15 @@ int nsfv1_block_jacobi(nsfv1_disc* h, const void* vals, int prec, const double* 
 #define NSFV1_NOALLOC_MAX_NODES 32768
 
 /* The same preconditioner as nsfv1_block_jacobi, allocating nothing: for
- * callers whose device memory belongs to their own pool allocator, or whose
- * solver loop cannot absorb cudaMalloc's implicit synchronisation. No
- * counterpart in the reference (its CPU preconditioner allocates freely).
+ * callers whose device memory is all handed out by their own pool allocator,
+ * so that a cudaMalloc from inside a library would fail or fragment that pool.
+ * No counterpart in the reference (its CPU preconditioner allocates freely).
  * The scratch is a fixed 4 MiB device array inside the library, shared by all
  * calls; meshes above NSFV1_NOALLOC_MAX_NODES nodes are rejected with
  * NSFV1_ERR_ARGUMENT. The first call on a device looks the array up with
- * cudaGetSymbolAddress and should come before any stream capture. Calls that
+ * cudaGetSymbolAddress and should come before any stream capture. Like
+ * nsfv1_block_jacobi, every call waits for its stream to finish: it reads the
+ * singular-block flag back to the host (NSFV1_ERR_BREAKDOWN). Calls that
  * overlap on the GPU race on the shared array and must be serialised. */
 int nsfv1_block_jacobi_noalloc(nsfv1_disc* h, const void* vals, int prec, const double* r, double* z, void* stream);
 
@@ -308,7 +318,8 @@ int nsfv1_gemm_bf16_splits(int K, int splits);
 int nsfv1_set_assembly_threads(nsfv1_disc* h, int threads);
 int nsfv1_get_assembly_threads(const nsfv1_disc* h);
 /* Assembly autotuner: times one defect + Jacobian assembly at u (device) for
- * every candidate CTA size, in precision prec, and keeps the fastest;
+ * every candidate CTA size, in precision prec (nsfv1_assemble_defect_jacobian),
+ * and keeps the fastest;
  * ms[n_candidates] (host, may be NULL) receives the second pass's times. */
 int nsfv1_assembly_autotune(nsfv1_disc* h, const double* u, int prec, const int* candidates, int n_candidates, double* ms, void* stream);
 

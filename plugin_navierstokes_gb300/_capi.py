@@ -108,6 +108,7 @@ _SIGS = {
     "nsfv1_set_dirichlet": (c_int, [c_void_p, c_int64, c_void_p, c_void_p]),
     "nsfv1_assemble_defect": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p]),
     "nsfv1_assemble_jacobian": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_int, c_void_p]),
+    "nsfv1_assemble_defect_jacobian": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p, c_int, c_void_p]),
     "nsfv1_elem_batch": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p]),
     "nsfv1_bsr_mv": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),

@@ -1,7 +1,8 @@
 // FV1 assembly kernels for sm_103a: one thread per element, elements of one
-// colour per launch (no two share a node), so the scatter into the global
-// defect / block-CSR Jacobian is a plain read-modify-write and the summation
-// order per entry is fixed (colour order, then SCVF order): runs are bitwise
+// colour per launch (no two share a node). The scatter into the global defect /
+// block-CSR Jacobian uses fire-and-forget L2 reductions (red.global.add); within
+// a colour every address is updated by one thread only, so the summation order
+// per entry is fixed (colour order, then SCVF order): runs are bitwise
 // reproducible.
 #include <type_traits>
 #include "nsfv1_internal.h"
@@ -214,6 +215,70 @@ __global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const
     }
 }
 
+// Defect and FP64 Jacobian at the same state in one pass over the elements of a
+// colour (one launch per colour instead of two): the per-SCVF geometry, upwinds
+// and stabilisation are evaluated once for both outputs.
+template <int ROID, bool TRANSIENT>
+__global__ void __launch_bounds__(kThreads) k_defect_jacobian(const DiscParams P, const AsmArgs A) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh, b = R::b;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.count) return;
+    const int32_t e = __ldg(A.elems + t);
+    if (A.elemInst && !__ldg(A.instActive + __ldg(A.elemInst + e))) return;
+    const double nuEl = A.nuElem ? __ldg(A.nuElem + e) : P.nu;
+    GlobalDefSink<nsh, b> sink;
+    sink.D = A.D;
+#pragma unroll
+    for (int k = 0; k < nsh; ++k) sink.nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
+    Elem<ROID, double> E;
+    load_corners<ROID, double>(A.coords, sink.nodes, E);
+    elem_setup<ROID, double>(E);
+    double u[b][nsh];
+    load_u<ROID, double>(A.U, sink.nodes, u);
+    double uo[TRANSIENT ? dim : 1][nsh];
+    if constexpr (TRANSIENT) {
+        double t4[b][nsh];
+        load_u<ROID, double>(A.Uold, sink.nodes, t4);
+#pragma unroll
+        for (int d = 0; d < dim; ++d)
+#pragma unroll
+            for (int k = 0; k < nsh; ++k) uo[d][k] = t4[d][k];
+    }
+    GlobalJacSink<double, nsh> jsink{reinterpret_cast<double*>(A.vals), A.elemBlk + (int64_t)e * nsh * nsh};
+    DiscParams Q = P;
+    Q.transient = TRANSIENT ? 1 : 0;
+    bool ok;
+    if constexpr (TRANSIENT) {
+        struct Scaled {
+            GlobalDefSink<nsh, b>& s; double dt;
+            __device__ __forceinline__ void add(int i, int f, double v) { s.add(i, f, v * dt); }
+        } ss{sink, P.dt};
+        ok = elem_def_jac_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(uo), ss, P.dt, jsink, nuEl);
+    } else {
+        ok = elem_def_jac_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(u), sink, 1.0, jsink, nuEl);
+    }
+    if (!ok) atomicOr(A.err, 1);
+    // mass (implicit Euler) and source parts, per SCV: defect as in k_defect, Jacobian as in k_jacobian
+    const double rho = P.rho;
+#pragma unroll
+    for (int k = 0; k < nsh; ++k) {
+#pragma unroll
+        for (int f = 0; f < dim; ++f) {
+            double v = 0.0;
+            bool any = false;
+            if (P.hasSource) { v -= P.src[f] * E.vol[k] * rho; any = true; }
+            if constexpr (TRANSIENT) { v = (u[f][k] * E.vol[k] * rho - uo[f][k] * E.vol[k] * rho) + v * P.dt; any = true; }
+            if (any) atomicAdd(A.D + (int64_t)sink.nodes[k] * b + f, v);
+        }
+        if constexpr (TRANSIENT) {
+            double* p = jsink.vals + (int64_t)__ldg(jsink.blk + k * nsh + k) * (b * b);
+#pragma unroll
+            for (int d = 0; d < dim; ++d) atomicAdd(p + d * b + d, E.vol[k] * rho);
+        }
+    }
+}
+
 // ---- batched element-local callbacks ----------------------------------------
 
 template <int ROID>
@@ -340,6 +405,16 @@ cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int
         constexpr int RO = decltype(r)::value;
         if (prec == 0) k_jacobian<RO, double, double><<<grid, t, 0, s>>>(P, a);
         else k_jacobian<RO, float, float><<<grid, t, 0, s>>>(P, a);
+    });
+}
+
+cudaError_t launch_defect_jacobian(int roid, const DiscParams& P, const AsmArgs& a, cudaStream_t s, int threads) {
+    if (a.count <= 0) return cudaSuccess;
+    const int t = clamp_threads(threads);
+    const int grid = (a.count + t - 1) / t;
+    return dispatch_roid(roid, [&](auto r) {
+        if (P.transient) k_defect_jacobian<decltype(r)::value, true><<<grid, t, 0, s>>>(P, a);
+        else k_defect_jacobian<decltype(r)::value, false><<<grid, t, 0, s>>>(P, a);
     });
 }
 

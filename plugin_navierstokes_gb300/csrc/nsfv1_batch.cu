@@ -651,8 +651,8 @@ static int max_clusters(int clusterSize) {
 // ---- the batched Newton driver -----------------------------------------------------
 
 struct BatchWs {
-    int prec = -1, m = 0;
-    int64_t n = 0;
+    int prec = -1, m = 0, nInst = 0;
+    int64_t n = 0, nnzb = 0;   // every buffer is sized by (prec, n, m, nInst, nnzb)
     double *D = nullptr, *Dt = nullptr, *Ut = nullptr, *nrm = nullptr, *lambda = nullptr, *relres = nullptr;
     void *J = nullptr, *Dinv = nullptr, *V = nullptr, *t = nullptr, *x = nullptr, *q = nullptr, *s = nullptr, *x2 = nullptr;
     int32_t *queue = nullptr, *head = nullptr, *pending = nullptr, *accepted = nullptr, *iters = nullptr, *nQueue = nullptr;
@@ -772,7 +772,8 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
         ~Ev() { if (e) cudaEventDestroy(e); }
     } eA, eB, eC;
     cudaEvent_t evA = eA.e, evB = eB.e, evC = eC.e;
-    if (W.prec != prec || W.n != n || W.m != m) {
+    const int64_t nnzb = (int64_t)D.colIdx.size();
+    if (W.prec != prec || W.n != n || W.m != m || W.nInst != nInst || W.nnzb != nnzb) {
         W.release();
         const size_t vt = sizeof(VT);
         auto al = [&](auto*& ptr, size_t bytes) { return D.cuda_ok(cudaMalloc((void**)&ptr, bytes), "batch workspace"); };
@@ -783,7 +784,7 @@ int batched_newton(Disc& D, double* u, const double* u_old, double dt, const nsf
             !al(W.queue, nInst * 4) || !al(W.head, 4) || !al(W.nQueue, 4) || !al(W.rtolInst, nInst * 8) ||
             !al(W.pending, nInst * 4) || !al(W.accepted, nInst * 4) || !al(W.iters, nInst * 4))
             return D.status;
-        W.prec = prec; W.n = n; W.m = m;
+        W.prec = prec; W.n = n; W.m = m; W.nInst = nInst; W.nnzb = nnzb;
     }
     const int baseCluster = opt.cluster_size > 0 ? opt.cluster_size : 4;
     int numSMs = 0;
@@ -1122,6 +1123,9 @@ int nsfv1_set_instances(nsfv1_disc* h, int n_inst, const int32_t* node_offsets) 
     if (!up(D->d_instNode0, node_offsets, n_inst + 1) || !up(D->d_nodeInst, nodeInst.data(), nodeInst.size()) ||
         !up(D->d_elemInst, elemInst.data(), elemInst.size()) || !up(D->d_instActive, ones.data(), n_inst))
         return D->status;
+    // multigrid levels, graphs and solver buffers of the previous partition no longer apply
+    if (D->batch) { batch_free(D->batch); D->batch = nullptr; }
+    D->instCells.clear();
     D->nInst = n_inst;
     D->instNode0.assign(node_offsets, node_offsets + n_inst + 1);
     D->instSkip = false;

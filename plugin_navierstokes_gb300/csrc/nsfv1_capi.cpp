@@ -79,6 +79,8 @@ void Disc::free_mesh() {
     dfree(d_dirRow); dfree(d_dirVal); dfree(d_diagPos); dfree(d_bjDinv); dfree(d_nuElem);
     dfree(d_instNode0); dfree(d_elemInst); dfree(d_nodeInst); dfree(d_instActive);
     nInst = 0; instNode0.clear(); instSkip = false;
+    // the batched solver's levels, graphs and buffers belong to this mesh
+    if (batch) { batch_free(batch); batch = nullptr; }
 }
 
 Disc::~Disc() {
@@ -164,6 +166,20 @@ static void build_pattern(int nsh, int64_t nNodes, int64_t nElems, const int32_t
             for (int j = 0; j < nsh; ++j)
                 elemBlk[(e * nsh + i) * nsh + j] = (int32_t)(std::lower_bound(b0, b1, conn[e * nsh + j]) - colIdx.data());
         }
+}
+
+// Connectivity check of a mesh: every index in range and every node referenced
+// by at least one element (an unreferenced node would get an empty block row
+// without a diagonal block). Returns the error text, or nullptr.
+static const char* check_connectivity(int nsh, int64_t nNodes, int64_t nElems, const int32_t* conn) {
+    std::vector<uint8_t> used(nNodes, 0);
+    for (int64_t k = 0; k < nElems * nsh; ++k) {
+        if (conn[k] < 0 || conn[k] >= nNodes) return "connectivity out of range";
+        used[conn[k]] = 1;
+    }
+    for (int64_t r = 0; r < nNodes; ++r)
+        if (!used[r]) return "a node belongs to no element (its matrix row would have no diagonal block)";
+    return nullptr;
 }
 
 // greedy colouring in element order: the smallest colour not used by an
@@ -296,8 +312,7 @@ int nsfv1_set_mesh(nsfv1_disc* h, int elem_type, int64_t n_nodes, const double* 
         if (dim != D->dim) { D->fail(NSFV1_ERR_ARGUMENT, "element dimension does not match the disc"); return D->status; }
         if (n_nodes <= 0 || n_elems <= 0 || !coords || !conn) { D->fail(NSFV1_ERR_ARGUMENT, "empty mesh"); return D->status; }
         if (n_nodes >= (int64_t(1) << 31) / 4 || n_elems * nsh * nsh >= (int64_t(1) << 31)) { D->fail(NSFV1_ERR_ARGUMENT, "mesh too large for 32-bit indices"); return D->status; }
-        for (int64_t k = 0; k < n_elems * nsh; ++k)
-            if (conn[k] < 0 || conn[k] >= n_nodes) { D->fail(NSFV1_ERR_ARGUMENT, "connectivity out of range"); return D->status; }
+        if (const char* bad = check_connectivity(nsh, n_nodes, n_elems, conn)) { D->fail(NSFV1_ERR_ARGUMENT, bad); return D->status; }
         D->free_mesh();
         D->hasMesh = false;
         D->roid = elem_type; D->nsh = nsh; D->nNodes = n_nodes; D->nElems = n_elems;
@@ -326,7 +341,8 @@ int nsfv1_set_mesh(nsfv1_disc* h, int elem_type, int64_t n_nodes, const double* 
             std::vector<int32_t> dp(n_nodes);
             for (int64_t r = 0; r < n_nodes; ++r) {
                 int32_t q = D->rowPtr[r];
-                while (D->colIdx[q] != r) ++q;
+                while (q < D->rowPtr[r + 1] && D->colIdx[q] != r) ++q;
+                if (q == D->rowPtr[r + 1]) { D->fail(NSFV1_ERR_ARGUMENT, "a matrix row has no diagonal block"); return D->status; }
                 dp[r] = q;
             }
             if (!D->cuda_ok(dupload(D->d_diagPos, dp.data(), dp.size()), "upload diagPos")) return D->status;
@@ -359,9 +375,8 @@ int nsfv1_mesh_pattern(int elem_type, int64_t n_nodes, int64_t n_elems, const in
                        int* n_colors, int32_t* row_ptr, int32_t* col_idx, int32_t* elem_color) {
     const int nsh = ref_nsh(elem_type);
     if (nsh == 0 || n_nodes <= 0 || n_elems <= 0 || !conn) return NSFV1_ERR_ARGUMENT;
-    for (int64_t k = 0; k < n_elems * nsh; ++k)
-        if (conn[k] < 0 || conn[k] >= n_nodes) return NSFV1_ERR_ARGUMENT;
     try {
+        if (check_connectivity(nsh, n_nodes, n_elems, conn)) return NSFV1_ERR_ARGUMENT;
         std::vector<int32_t> rp, ci, eb, col;
         build_pattern(nsh, n_nodes, n_elems, conn, rp, ci, eb);
         const int nc = build_coloring(nsh, n_nodes, n_elems, conn, col);
@@ -421,6 +436,12 @@ int nsfv1_assemble_defect(nsfv1_disc* h, const double* u, const double* u_old, d
 int nsfv1_assemble_jacobian(nsfv1_disc* h, const double* u, const double* u_old, double dt, void* vals, int prec, void* stream) {
     NSFV1_H;
     return D->assemble_jacobian(u, u_old, dt, vals, prec, (cudaStream_t)stream) ? NSFV1_OK : D->status;
+}
+
+int nsfv1_assemble_defect_jacobian(nsfv1_disc* h, const double* u, const double* u_old, double dt, double* d, void* vals, int prec,
+                                   void* stream) {
+    NSFV1_H;
+    return D->assemble_defect_jacobian(u, u_old, dt, d, vals, prec, (cudaStream_t)stream) ? NSFV1_OK : D->status;
 }
 
 int nsfv1_elem_batch(nsfv1_disc* h, int elem_type, int64_t n, const double* corners, const double* u, const double* u_old,
@@ -485,7 +506,7 @@ int nsfv1_assembly_autotune(nsfv1_disc* h, const double* u, int prec, const int*
         for (int c = 0; ok && c < n_candidates; ++c) {
             D->asmThreads = candidates[c];
             cudaEventRecord(e0, s);
-            ok = D->assemble_defect(u, nullptr, 0.0, d, s) && D->assemble_jacobian(u, nullptr, 0.0, J, prec, s, false);
+            ok = D->assemble_defect_jacobian(u, nullptr, 0.0, d, J, prec, s);
             cudaEventRecord(e1, s);
             float msec = 0.f;
             if (ok) ok = D->cuda_ok(cudaEventSynchronize(e1), "autotune") && D->cuda_ok(cudaEventElapsedTime(&msec, e0, e1), "autotune");
@@ -547,6 +568,27 @@ bool Disc::assemble_defect(const double* u, const double* u_old, double dt, doub
         if (!cuda_ok(launch_defect(roid, P, a, s, asmThreads), "defect kernel")) return false;
     }
     if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, d, nullptr, 0, s), "dirichlet")) return false;
+    return check_err_word(s);
+}
+
+bool Disc::assemble_defect_jacobian(const double* u, const double* u_old, double dt, double* d, void* vals, int prec, cudaStream_t s) {
+    if (!hasMesh) return fail(NSFV1_ERR_STATE, "assemble_defect_jacobian: no mesh set");
+    if (!u || !d || !vals) return fail(NSFV1_ERR_ARGUMENT, "assemble_defect_jacobian: null pointer");
+    if (prec != NSFV1_F64 && prec != NSFV1_F32) return fail(NSFV1_ERR_ARGUMENT, "assemble_defect_jacobian: precision must be NSFV1_F64 or NSFV1_F32");
+    // FP32 values: the FP64 defect and the FP32-arithmetic Jacobian kernel (cheaper than
+    // deriving FP32 blocks from the FP64 element state)
+    if (prec == NSFV1_F32) return assemble_defect(u, u_old, dt, d, s) && assemble_jacobian(u, u_old, dt, vals, prec, s);
+    DiscParams P;
+    if (!params(P, u_old != nullptr, dt)) return false;
+    const int b = dim + 1;
+    if (!cuda_ok(cudaMemsetAsync(d, 0, sizeof(double) * nNodes * b, s), "memset defect")) return false;
+    if (!cuda_ok(cudaMemsetAsync(vals, 0, colIdx.size() * b * b * sizeof(double), s), "memset jacobian")) return false;
+    for (int c = 0; c < nColors; ++c) {
+        AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, d, vals,
+                  d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive};
+        if (!cuda_ok(launch_defect_jacobian(roid, P, a, s, asmThreads), "defect+jacobian kernel")) return false;
+    }
+    if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, d, vals, NSFV1_F64, s), "dirichlet")) return false;
     return check_err_word(s);
 }
 

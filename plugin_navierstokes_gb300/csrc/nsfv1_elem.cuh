@@ -762,21 +762,13 @@ __device__ __forceinline__ T peclet_blend(const IpGeo<T>& G, const T* StdVel, T 
 // Returns false if an upwind ray found no side.
 // ---------------------------------------------------------------------------
 template <int ROID, typename T, class DSink>
-__device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
+__device__ __forceinline__ void scvf_def_A(const DiscParams& P, const Elem<ROID, T>& E, const IpGeo<T>& G, const IpState<ROID, T>& S,
+                                           const int ip, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
                                            const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], DSink& sink, const T nu) {
     using R = Ref<ROID>;
-    constexpr int dim = R::dim, nsh = R::nsh, Pc = dim, nip = R::nip;
-    T corMinN = T(0), corMinD = T(0), corAvgN = T(1);
-    if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, T>(E, corMinN, corMinD, corAvgN);
+    constexpr int dim = R::dim, nsh = R::nsh, Pc = dim;
     const T rho = T(P.rho);
-    bool ok = true;
-#pragma unroll 1
-    for (int ip = 0; ip < nip; ++ip) {
-        IpGeo<T> G;
-        ip_geom<ROID, T>(E, ip, G);
-        IpState<ROID, T> S;
-        ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
-        ok &= S.ok;
+    {
         // velocity and pressure gradients: local gradients first, then one J^-T
         // (grad_k = J^-T lgrad_k, so sum_k u_k grad_k = J^-T sum_k u_k lgrad_k)
         T gradVel[3][3], gradP[3];
@@ -894,6 +886,24 @@ __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID,
         sink.add(G.from, Pc, contFlux);
         sink.add(G.to, Pc, -contFlux);
     }
+}
+
+template <int ROID, typename T, class DSink>
+__device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
+                                           const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], DSink& sink, const T nu) {
+    using R = Ref<ROID>;
+    T corMinN = T(0), corMinD = T(0), corAvgN = T(1);
+    if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, T>(E, corMinN, corMinD, corAvgN);
+    bool ok = true;
+#pragma unroll 1
+    for (int ip = 0; ip < R::nip; ++ip) {
+        IpGeo<T> G;
+        ip_geom<ROID, T>(E, ip, G);
+        IpState<ROID, T> S;
+        ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
+        ok &= S.ok;
+        scvf_def_A<ROID, T>(P, E, G, S, ip, u, uo, sink, nu);
+    }
     return ok;
 }
 
@@ -904,22 +914,14 @@ __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID,
 // implicit-Euler Jacobian M + dt dA/du).
 // ---------------------------------------------------------------------------
 template <int ROID, typename T, class Sink>
-__device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
-                                           const T scale, Sink& sink, const T nu) {
+__device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const Elem<ROID, T>& E, const IpGeo<T>& G, const IpState<ROID, T>& S,
+                                           const int ip, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh], const T scale, Sink& sink,
+                                           const T nu) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, b = R::b, Pc = dim;
-    T corMinN = T(0), corMinD = T(0), corAvgN = T(1);
-    if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, T>(E, corMinN, corMinD, corAvgN);
     const T rho = T(P.rho);
     const T mnr = T(-1.0) * nu * rho;
-    bool ok = true;
-#pragma unroll 1
-    for (int ip = 0; ip < R::nip; ++ip) {
-        IpGeo<T> G;
-        ip_geom<ROID, T>(E, ip, G);
-        IpState<ROID, T> S;
-        ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
-        ok &= S.ok;
+    {
         T UpwindVel[3] = {T(0), T(0), T(0)};
         T w = T(1), prod = T(0), Vn = T(0);
 #pragma unroll
@@ -1008,6 +1010,51 @@ __device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID,
             sink.add(G.from, k, B, true);
             sink.add(G.to, k, B, false);
         }
+    }
+}
+
+template <int ROID, typename T, class Sink>
+__device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
+                                           const T scale, Sink& sink, const T nu) {
+    using R = Ref<ROID>;
+    T corMinN = T(0), corMinD = T(0), corAvgN = T(1);
+    if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, T>(E, corMinN, corMinD, corAvgN);
+    bool ok = true;
+#pragma unroll 1
+    for (int ip = 0; ip < R::nip; ++ip) {
+        IpGeo<T> G;
+        ip_geom<ROID, T>(E, ip, G);
+        IpState<ROID, T> S;
+        ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
+        ok &= S.ok;
+        scvf_jac_A<ROID, T>(P, E, G, S, ip, u, scale, sink, nu);
+    }
+    return ok;
+}
+
+// Defect and Jacobian of one element at the same state in one pass: the
+// geometry, upwind shapes and stabilisation of every SCVF are computed once and
+// feed both (the reference evaluates them separately in add_def_A_elem and
+// add_jac_A_elem, navier_stokes_fv1.cpp:296-309, 645-659). 'jscale' multiplies
+// the Jacobian blocks (dt for the implicit-Euler Jacobian); the defect sink
+// applies its own scaling.
+template <int ROID, typename T, class DSink, class JSink>
+__device__ __forceinline__ bool elem_def_jac_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
+                                               const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], DSink& dsink, const T jscale,
+                                               JSink& jsink, const T nu) {
+    using R = Ref<ROID>;
+    T corMinN = T(0), corMinD = T(0), corAvgN = T(1);
+    if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, T>(E, corMinN, corMinD, corAvgN);
+    bool ok = true;
+#pragma unroll 1
+    for (int ip = 0; ip < R::nip; ++ip) {
+        IpGeo<T> G;
+        ip_geom<ROID, T>(E, ip, G);
+        IpState<ROID, T> S;
+        ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
+        ok &= S.ok;
+        scvf_def_A<ROID, T>(P, E, G, S, ip, u, uo, dsink, nu);
+        scvf_jac_A<ROID, T>(P, E, G, S, ip, u, jscale, jsink, nu);
     }
     return ok;
 }

@@ -78,6 +78,7 @@ struct Disc {
     bool params(DiscParams& P, bool transient, double dt);
     bool assemble_defect(const double* u, const double* u_old, double dt, double* d, cudaStream_t s);
     bool assemble_jacobian(const double* u, const double* u_old, double dt, void* vals, int prec, cudaStream_t s, bool sync = true);
+    bool assemble_defect_jacobian(const double* u, const double* u_old, double dt, double* d, void* vals, int prec, cudaStream_t s);
     bool ensure_workspace(int prec, int gmresM);
     bool set_dirichlet_values(double* u, cudaStream_t s);   // u[dof] = g for every Dirichlet row
 };

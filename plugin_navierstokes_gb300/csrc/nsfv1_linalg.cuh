@@ -5,7 +5,7 @@
 namespace nsfv1 {
 
 // Inverse of one b x b block (Gauss-Jordan with partial pivoting, FP64);
-// returns false on a zero pivot (O untouched).
+// returns false on a zero pivot (O is then set to zero).
 template <int b, typename VT, typename OT>
 __device__ __forceinline__ bool block_inverse(const VT* __restrict__ A, OT* __restrict__ O) {
     double M[b][2 * b];
@@ -18,7 +18,13 @@ __device__ __forceinline__ bool block_inverse(const VT* __restrict__ A, OT* __re
         int p = c;
 #pragma unroll
         for (int q = c + 1; q < b; ++q) if (fabs(M[q][c]) > fabs(M[p][c])) p = q;
-        if (M[p][c] == 0.0) return false;
+        if (M[p][c] == 0.0) {
+            // singular: a zero block (the caller reports the breakdown; later
+            // kernels that still read this block see finite values)
+#pragma unroll
+            for (int i = 0; i < b * b; ++i) O[i] = (OT)0;
+            return false;
+        }
         if (p != c) {
 #pragma unroll
             for (int j = 0; j < 2 * b; ++j) { const double t = M[p][j]; M[p][j] = M[c][j]; M[c][j] = t; }

@@ -3,10 +3,9 @@
 //
 // Who needs it: applications whose device memory is entirely handed out by
 // their own pool allocator (a cudaMalloc from a library would fail or fragment
-// that pool), and latency-bound solver loops where cudaMalloc's implicit
-// device synchronisation is not acceptable. nsfv1_block_jacobi allocates its
-// scratch (the inverted diagonal blocks) on first use; this variant keeps that
-// scratch in a fixed device array of this file instead and allocates nothing.
+// that pool). nsfv1_block_jacobi allocates its scratch (the inverted diagonal
+// blocks) on first use; this variant keeps that scratch in a fixed device
+// array of this file instead and allocates nothing.
 //
 // Limits and behaviour:
 //  - The scratch holds NSFV1_NOALLOC_MAX_NODES (32768) nodes of 4 x 4 FP64
@@ -15,6 +14,8 @@
 //  - The first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current) and caches it; make that
 //    first call before any stream capture.
+//  - Each call waits for its stream to finish, as nsfv1_block_jacobi does: the
+//    singular-block flag is read back to the host (NSFV1_ERR_BREAKDOWN).
 //  - All calls in the process share the one array and it keeps the contents
 //    of the last call: calls that overlap on the GPU (two streams, two
 //    threads, two handles) race and must be serialised by the caller. Every

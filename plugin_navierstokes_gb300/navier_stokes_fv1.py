@@ -147,6 +147,14 @@ class NavierStokesFV1:
         prec = _capi.F64 if vals.dtype == torch.float64 else _capi.F32
         self._c(self._lib.nsfv1_assemble_jacobian(self._h, _ptr(u), _ptr(u_old), float(dt), _ptr(vals), prec, _stream_ptr(stream)))
 
+    def assemble_defect_jacobian(self, u, d, vals, u_old=None, dt: float = 0.0, stream=None) -> None:
+        """Defect into d and Jacobian into vals at the same u, in one pass over the elements."""
+        import torch
+
+        prec = _capi.F64 if vals.dtype == torch.float64 else _capi.F32
+        self._c(self._lib.nsfv1_assemble_defect_jacobian(self._h, _ptr(u), _ptr(u_old), float(dt), _ptr(d), _ptr(vals), prec,
+                                                         _stream_ptr(stream)))
+
     def elem_batch(self, elem_type: int, corners, u, u_old=None, dt: float = 0.0, defA=None, jacA=None, defM=None,
                    jacM=None, rhs=None, stream=None) -> None:
         n = corners.shape[0]

@@ -123,3 +123,31 @@ def test_single_element_pattern_and_ragged_coloring():
     o.set_mesh(_capi.TRIANGLE, X, fan)
     orp, oci = o.pattern()
     assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+
+
+def test_meshes_with_unreferenced_nodes_are_rejected():
+    """A node that no element references would get a matrix row without a diagonal
+    block: nsfv1_set_mesh and nsfv1_mesh_pattern refuse such meshes (before any
+    device work)."""
+    lib = _capi.load()
+    roid, X, C = mesh.structured_quads(3)
+    Xo = np.vstack([X, [[2.0, 2.0]]])   # one orphan node after the grid
+    d = NavierStokesFV1("u,v,p")
+    st = lib.nsfv1_set_mesh(d._h, roid, Xo.shape[0], np.ascontiguousarray(Xo).ctypes.data, C.shape[0],
+                            np.ascontiguousarray(C, dtype=np.int32).ctypes.data)
+    assert st == _capi.ERR_ARGUMENT and "belongs to no element" in d.last_error()
+    with pytest.raises(NSFV1Error):
+        mesh_pattern(roid, Xo.shape[0], C)
+
+
+def test_pattern_and_coloring_bit_exact_at_benchmark_size_host():
+    """The 64^3 hexahedral benchmark mesh through the host-only pattern build:
+    7,189,057 blocks and the element colouring, bit-exact with the oracle."""
+    roid, X, C = mesh.structured_hexes(64)
+    rp, ci, col, nc = mesh_pattern(roid, X.shape[0], C)
+    o = oracle.Oracle(3)
+    o.set_mesh(roid, X, C)
+    orp, oci = o.pattern()
+    ocol, onc = o.coloring()
+    assert ci.size == 193 ** 3 and nc == onc == 8
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci) and np.array_equal(col, ocol)

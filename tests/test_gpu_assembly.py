@@ -232,3 +232,60 @@ def test_fp32_3d_jacobian_needs_16_byte_alignment(cuda):
     with pytest.raises(NSFV1Error):
         d.assemble_jacobian(tu, J[1:])
     d.assemble_jacobian(tu, J[4:])   # 16-byte offset: fine
+
+
+@pytest.mark.parametrize("gen", ["quads", "hexes", "tris"])
+@pytest.mark.parametrize("cfgi", range(len(DISC_CASES)))
+def test_fused_defect_jacobian_matches_oracle(cuda, gen, cfgi):
+    """nsfv1_assemble_defect_jacobian (one pass for both outputs) against the oracle,
+    for every discretisation case, stationary or implicit Euler as the case says."""
+    import torch
+    roid, X, C = {"quads": lambda: mesh.structured_quads(16), "hexes": lambda: mesh.structured_hexes(5),
+                  "tris": lambda: mesh.jittered_triangles(12, seed=5)}[gen]()
+    dim = DIM[roid]
+    cfg = DISC_CASES[cfgi]
+    b = dim + 1
+    U = mesh.solenoidal_state(X, seed=9) if dim == 3 else (mesh.uniform(11, X.shape[0] * 3) * 2 - 1).reshape(-1, 3)
+    Uo = (U * 0.8) if cfg[3] else None
+    dt = 0.02 if cfg[3] else 0.0
+    o = oracle.Oracle(dim); configure(o, dim, cfg); o.set_mesh(roid, X, C)
+    d = NavierStokesFV1(dim=dim); configure(d, dim, cfg); d.set_mesh(roid, X, C)
+    if dim == 2:
+        dofs, vals = mesh.cavity_dirichlet(X, 1.0)
+        o.set_dirichlet(dofs, vals); d.set_dirichlet(dofs, vals)
+    Dref, Jref = o.assemble(U, Uo, dt)
+    tu = torch.tensor(U.ravel(), dtype=torch.float64, device=cuda)
+    tuo = None if Uo is None else torch.tensor(Uo.ravel(), dtype=torch.float64, device=cuda)
+    D = torch.full_like(tu, float("nan"))
+    J = torch.full((o.nnzb * b * b,), float("nan"), dtype=torch.float64, device=cuda)
+    d.assemble_defect_jacobian(tu, D, J, tuo, dt)
+    torch.cuda.synchronize()
+    assert rel_err(D.cpu().numpy(), Dref) <= TOL64, (gen, cfg_name(cfg))
+    assert rel_err(J.cpu().numpy(), Jref) <= TOL64, (gen, cfg_name(cfg))
+    # FP32 values through the same entry point (FP64 defect + FP32 Jacobian)
+    D32 = torch.full_like(tu, float("nan"))
+    J32 = torch.full((o.nnzb * b * b,), float("nan"), dtype=torch.float32, device=cuda)
+    d.assemble_defect_jacobian(tu, D32, J32, tuo, dt)
+    torch.cuda.synchronize()
+    assert rel_err(D32.cpu().numpy(), Dref) <= TOL64
+    assert rel_err(J32.double().cpu().numpy(), Jref) <= TOL32
+    # determinism of the fused pass
+    D2, J2 = torch.empty_like(D), torch.empty_like(J)
+    d.assemble_defect_jacobian(tu, D2, J2, tuo, dt)
+    torch.cuda.synchronize()
+    assert torch.equal(D, D2) and torch.equal(J, J2)
+
+
+def test_pattern_and_coloring_bit_exact_at_benchmark_size(cuda):
+    """The 64^3 hexahedral benchmark mesh: block-CSR pattern (7,189,057 blocks) and
+    element colouring of the handle, bit-exact with the oracle's."""
+    roid, X, C = mesh.structured_hexes(64)
+    d = NavierStokesFV1(dim=3); configure(d, 3, DISC_CASES[1]); d.set_mesh(roid, X, C)
+    o = oracle.Oracle(3); configure(o, 3, DISC_CASES[1]); o.set_mesh(roid, X, C)
+    rp, ci = d.pattern()
+    orp, oci = o.pattern()
+    assert ci.size == 193 ** 3
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    col = d.coloring()
+    ocol, onc = o.coloring()
+    assert np.array_equal(col, ocol) and d.pattern_info()["n_colors"] == onc

@@ -198,3 +198,34 @@ def test_exact_jacobian_with_forcing_meets_the_oracle_target(cuda):
         D, _ = o.assemble(U[offs[i] * 3:offs[i + 1] * 3], jacobian=False)
         D0, _ = o.assemble(_dir(U[offs[i] * 3:offs[i + 1] * 3].size, dofs, vals), jacobian=False)
         assert np.linalg.norm(D) <= 1.01e-8 * np.linalg.norm(D0), (i, res[i])
+
+
+def test_repartition_one_mesh_into_more_instances(cuda):
+    """The same mesh of four cavities solved first as two instances (two cavities
+    each), then as four: the batched solver's per-instance buffers follow the new
+    partition, and every cavity meets its FP64 oracle defect target."""
+    import torch
+    sizes = [8, 8, 12, 12]
+    Re = [100.0, 300.0, 50.0, 200.0]
+    lid = [1.0, 1.5, 0.5, 2.0]
+    d, B = _batch(sizes, Re, lid)
+    offs = np.asarray(B["node_offsets"])
+    d.set_instances([offs[0], offs[2], offs[4]])
+    d.set_dirichlet(B["dofs"], B["values"])
+    u2 = torch.zeros(B["coords"].shape[0] * 3, dtype=torch.float64, device=cuda)
+    r2 = d.newton_solve_batched(u2, rtol=1e-8, lin_rtol=1e-3, jacobian_prec="f32")
+    assert len(r2) == 2 and all(r["status"] == 0 for r in r2)
+    d.set_instances(offs)
+    d.set_dirichlet(B["dofs"], B["values"])
+    u4 = torch.zeros_like(u2)
+    r4 = d.newton_solve_batched(u4, rtol=1e-8, lin_rtol=1e-3, jacobian_prec="f32")
+    assert len(r4) == 4
+    U = u4.cpu().numpy()
+    for i, (N, re, u0) in enumerate(zip(sizes, Re, lid)):
+        assert r4[i]["status"] == 0, (i, r4[i])
+        roid, X, C = mesh.structured_quads(N)
+        dofs, vals = mesh.cavity_dirichlet(X, u0)
+        o = oracle.Oracle(2); o.set_kinematic_viscosity(u0 / re); o.set_upwind("full"); o.set_stabilization("flow")
+        o.set_mesh(roid, X, C); o.set_dirichlet(dofs, vals)
+        D, _ = o.assemble(U[offs[i] * 3:offs[i + 1] * 3], jacobian=False)
+        assert np.linalg.norm(D) <= 1.01e-8 * r4[i]["initial_defect"], (i, np.linalg.norm(D), r4[i])

@@ -1,8 +1,9 @@
 """The allocation-free block-Jacobi entry point (nsfv1_block_jacobi_noalloc).
 
-It serves callers that cannot allocate device memory (their memory belongs to
-their own pool allocator, or their loop cannot take cudaMalloc's implicit
-synchronisation): its scratch is a fixed array inside the library. The test
+It serves callers that cannot allocate device memory (all of their memory is
+handed out by their own pool allocator): its scratch is a fixed array inside
+the library. Like the allocating entry point, each call waits for its stream
+to read the singular-block flag. The test
 calls it through the C ABI twice in a row and checks it against the allocating
 entry point nsfv1_block_jacobi, within the FP64 tolerance of the parity tests
 (max |a - b| / max |b| <= 1e-12), and checks that a mesh above the stated
@@ -67,3 +68,32 @@ def test_noalloc_rejects_meshes_above_the_limit(cuda):
     z = torch.zeros_like(r)
     assert _noalloc(d, J, r, z) == _capi.ERR_ARGUMENT
     assert "at most 32768" in d.last_error()
+
+
+def test_noalloc_reports_a_planted_singular_block_and_recovers(cuda):
+    """A zero diagonal block written into the Jacobian by the test gives
+    NSFV1_ERR_BREAKDOWN from the allocation-free entry point, as from the
+    allocating one; the next call with the valid Jacobian matches again."""
+    import torch
+
+    roid, X, C = mesh.structured_quads(12)
+    d = NavierStokesFV1(dim=2)
+    configure(d, 2, DISC_CASES[0])
+    d.set_mesh(roid, X, C)
+    nnzb = d.pattern_info()["nnz_blocks"]
+    tu = torch.tensor(mesh.uniform(31, X.shape[0] * 3) * 2 - 1, dtype=torch.float64, device=cuda)
+    J = torch.empty(nnzb * 9, dtype=torch.float64, device=cuda)
+    d.assemble_jacobian(tu, J)
+    rp, ci = d.pattern()
+    q = int(rp[20] + np.nonzero(ci[rp[20]:rp[21]] == 20)[0][0])
+    Jbad = J.clone()
+    Jbad[q * 9:(q + 1) * 9] = 0
+    r = torch.tensor(mesh.uniform(32, tu.numel()) - 0.5, dtype=torch.float64, device=cuda)
+    z = torch.empty_like(r)
+    assert _noalloc(d, Jbad, r, z) == _capi.ERR_BREAKDOWN
+    assert "singular" in d.last_error()
+    z_ref = torch.empty_like(r)
+    d.block_jacobi(J, r, z_ref)
+    assert _noalloc(d, J, r, z) == _capi.OK, d.last_error()
+    torch.cuda.synchronize()
+    assert rel_err(z.cpu().numpy(), z_ref.cpu().numpy()) <= TOL64
