@@ -3,7 +3,10 @@
 A scalar FP64 C++ restatement of the reference's algorithm (nsfv1_oracle.cpp),
 used as the checker by tests/, __graft_entry__.smoke() and bench.py's CPU
 baseline leg. The product package never imports this module.
-Parity status: PARITY UNPINNED (see the header of nsfv1_oracle.cpp).
+Parity status: pinned to the reference's own element callbacks, compiled from
+the reference sources against a ugcore stand-in (oracle/ugshim, build_ref(),
+tests/test_reference_pin.py); the ugcore pieces stay restated (see the header
+of nsfv1_oracle.cpp).
 """
 from __future__ import annotations
 
@@ -190,3 +193,97 @@ def ref_tables(roid):
                        sides.ctypes.data, ef.ctypes.data)
     return {"nco": nco.value, "edges": edges[:2 * ne.value].reshape(-1, 2), "sides": sides[:4 * ns.value].reshape(-1, 4),
             "side_nco": snc[:ns.value], "edge_face": ef[:2 * ne.value].reshape(-1, 2)}
+
+
+# ---------------------------------------------------------------------------
+# The reference's own element callbacks (oracle/_ref/libnsfv1_ref.so): the
+# unmodified reference sources compiled against the ugcore stand-in in
+# oracle/ugshim (make -C oracle ref). Only built where the reference checkout
+# exists; used to pin this oracle.
+# ---------------------------------------------------------------------------
+REF_LIB = HERE / "_ref" / "libnsfv1_ref.so"
+_ref_lib = None
+
+
+class RefConfig(ctypes.Structure):
+    _fields_ = [("nu", c_double), ("rho", c_double), ("full_newton", c_double), ("src", c_double * 3),
+                ("has_source", c_int), ("stokes", c_int), ("laplace", c_int), ("peclet", c_int), ("pac", c_int),
+                ("upwind", c_char_p), ("stab", c_char_p), ("diff_length", c_char_p), ("stab_upwind", c_char_p)]
+
+
+def reference_root() -> Path | None:
+    """The reference checkout (NSREF_ROOT, default /root/reference), or None."""
+    root = Path(os.environ.get("NSREF_ROOT", "/root/reference"))
+    return root if (root / "incompressible" / "fv1" / "navier_stokes_fv1.cpp").exists() else None
+
+
+def build_ref(force: bool = False) -> Path | None:
+    """Build oracle/_ref/libnsfv1_ref.so from the reference sources; None if they are absent."""
+    root = reference_root()
+    if root is None:
+        return None
+    subprocess.run(["make", "-C", str(HERE), "ref", f"NSREF_ROOT={root}"] + (["-B"] if force else []), check=True,
+                   capture_output=True)
+    return REF_LIB
+
+
+def load_ref():
+    global _ref_lib
+    if _ref_lib is None:
+        if build_ref() is None:
+            raise RuntimeError("reference sources not available")
+        lib = ctypes.CDLL(str(REF_LIB))
+        lib.ref_elem_batch.restype = c_int
+        lib.ref_elem_batch.argtypes = [c_int, c_int64, ctypes.POINTER(RefConfig), c_void_p, c_void_p, c_void_p, c_double,
+                                       c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+        lib.ref_geometry.restype = c_int
+        lib.ref_geometry.argtypes = [c_int, c_void_p, c_void_p]
+        lib.ref_last_error.restype = c_char_p
+        _ref_lib = lib
+    return _ref_lib
+
+
+def ref_elem_batch(roid, cfg: dict, corners, u, u_old=None, dt=0.0, want=("defA", "jacA", "defM", "jacM", "rhs")):
+    """The reference's add_*_elem outputs for n elements (same layouts as Oracle.elem_batch).
+    cfg keys: nu, rho, full_newton, source (None or list), stokes, laplace, peclet, pac,
+    upwind, stab, diff_length, stab_upwind."""
+    lib = load_ref()
+    corners = np.ascontiguousarray(corners, np.float64)
+    u = np.ascontiguousarray(u, np.float64)
+    ne = corners.shape[0]
+    nloc = (DIM[roid] + 1) * NSH[roid]
+    out = {}
+    for k in ("defA", "defM", "rhs"):
+        out[k] = np.zeros((ne, nloc)) if k in want else None
+    for k in ("jacA", "jacM"):
+        out[k] = np.zeros((ne, nloc * nloc)) if k in want else None
+    uo = None if u_old is None else np.ascontiguousarray(u_old, np.float64)
+    src = cfg.get("source")
+    enc = lambda s: None if s is None else s.encode()
+    c = RefConfig(float(cfg.get("nu", 0.01)), float(cfg.get("rho", 1.0)), float(cfg.get("full_newton", 0.0)),
+                  (c_double * 3)(*(list(src) + [0.0] * (3 - len(src)) if src is not None else [0.0, 0.0, 0.0])),
+                  int(src is not None), int(bool(cfg.get("stokes"))), int(bool(cfg.get("laplace"))), int(bool(cfg.get("peclet"))),
+                  int(bool(cfg.get("pac"))), enc(cfg["upwind"]), enc(cfg["stab"]), enc(cfg.get("diff_length")),
+                  enc(cfg.get("stab_upwind")))
+    st = lib.ref_elem_batch(roid, ne, ctypes.byref(c), corners.ctypes.data, u.ctypes.data, _p(uo), float(dt), _p(out["defA"]),
+                            _p(out["jacA"]), _p(out["defM"]), _p(out["jacM"]), _p(out["rhs"]))
+    if st != 0:
+        raise RuntimeError(f"reference error {st}: {lib.ref_last_error().decode()}")
+    return {k: v for k, v in out.items() if v is not None}
+
+
+def ref_geometry(roid, corners):
+    """The ugcore stand-in's FV1 geometry of one element (same layout as geometry())."""
+    lib = load_ref()
+    nscvf = {2: 3, 3: 4, 4: 6, 8: 12}[roid]
+    nsh = NSH[roid]
+    out = np.zeros(nscvf * 40 + nsh)
+    c = np.ascontiguousarray(corners, np.float64)
+    if lib.ref_geometry(roid, c.ctypes.data, out.ctypes.data) != 0:
+        raise RuntimeError(lib.ref_last_error().decode())
+    scvf = []
+    for i in range(nscvf):
+        o = out[i * 40:(i + 1) * 40]
+        scvf.append({"from": int(o[0]), "to": int(o[1]), "ip": o[2:5], "normal": o[5:8], "shape": o[8:8 + nsh],
+                     "grad": o[16:40].reshape(8, 3)[:nsh]})
+    return scvf, out[nscvf * 40:]

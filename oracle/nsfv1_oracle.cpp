@@ -10,14 +10,20 @@
  * bench.py load it. The product library (plugin_navierstokes_gb300) never
  * links, loads or calls it.
  *
- * Parity status: PARITY UNPINNED against the reference. The reference ships
- * no tests, fixtures or golden vectors for this path, and it cannot be built
- * here as shipped (every file includes ugcore, which is not in the tree).
- * The plugin-level algorithm (navier_stokes_fv1.cpp, stabilization.cpp,
- * diffusion_length.h, upwind.cpp, upwind_interface.h) is restated line by line
- * below, each function citing the lines it follows. The ugcore pieces
- * (FV1Geometry, ElementSideRayIntersection, Newton, Krylov) are restated from
- * the box-method definition and documented where they are defined.
+ * Parity status: PINNED to the reference's own plugin code. The reference
+ * ships no tests, fixtures or golden vectors for this path, and every file
+ * includes ugcore (UG4's core library, not in the reference tree). Its FV1
+ * sources (navier_stokes_fv1.cpp, stabilization.cpp, upwind.cpp,
+ * upwind_interface.cpp, the NavierStokes base classes) are therefore compiled
+ * unmodified against a ugcore stand-in (oracle/ugshim, oracle/ref_driver.cpp,
+ * make -C oracle ref), and this restatement matches their element callbacks
+ * to about 2e-14 relative on every element type and discretisation case
+ * (tests/test_reference_pin.py, fixtures tests/golden/reference_elements.npz).
+ * The plugin-level algorithm is restated line by line below, each function
+ * citing the lines it follows. The ugcore pieces (FV1Geometry,
+ * ElementSideRayIntersection, Newton, Krylov) are restated from the box-method
+ * definition and documented where they are defined; the stand-in restates the
+ * same ugcore pieces independently, so they are cross-checked, not pinned.
  *
  * Layouts (shared with the product's C ABI):
  *   element-local vector  u[fct * nsh + sh]                (fct-major, as

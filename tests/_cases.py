@@ -70,6 +70,15 @@ def configure(disc, dim: int, cfg) -> None:
         disc.set_source([0.3, -0.2, 0.1][:dim])
 
 
+def ref_config(dim: int, cfg) -> dict:
+    """The same DISC_CASES entry as a configuration of the reference library
+    (oracle.ref_elem_batch); values as in configure()."""
+    up, stab, dl, transient, exact, peclet, laplace, stokes, source = cfg
+    return {"nu": 0.01 if dim == 2 else 0.0025, "rho": 1.0 if not source else 1.3, "full_newton": exact,
+            "source": [0.3, -0.2, 0.1][:dim] if source else None, "stokes": stokes, "laplace": laplace, "peclet": peclet,
+            "upwind": up, "stab": stab, "diff_length": dl}
+
+
 def cfg_name(cfg) -> str:
     up, stab, dl, transient, exact, peclet, laplace, stokes, source = cfg
     return f"{up}-{stab}-{dl}" + ("-tr" if transient else "") + ("-ex" if exact else "") + ("-pe" if peclet else "") + \

@@ -48,6 +48,21 @@ def test_element_callbacks_match_golden(cuda, tname, ci):
 
 @pytest.mark.parametrize("tname", list(ROIDS))
 @pytest.mark.parametrize("ci", range(len(DISC_CASES)))
+def test_element_callbacks_match_reference_fixtures(cuda, tname, ci):
+    """The GPU element callbacks against the numbers of the reference's own
+    code (tests/golden/reference_elements.npz, made by make_reference_golden.py
+    from the reference sources compiled against the ugcore stand-in)."""
+    g = np.load(os.path.join(GOLDEN, "reference_elements.npz"))
+    roid = ROIDS[tname]
+    key = f"{tname}_{ci}"
+    uo = g[key + "_uold"] if (key + "_uold") in g else None
+    r = _gpu_elem(cuda, roid, DISC_CASES[ci], g[key + "_corners"], g[key + "_u"], uo)
+    for k in ("defA", "jacA", "defM", "jacM", "rhs"):
+        assert rel_err(r[k], g[key + "_" + k]) <= TOL64, (key, cfg_name(DISC_CASES[ci]), k, rel_err(r[k], g[key + "_" + k]))
+
+
+@pytest.mark.parametrize("tname", list(ROIDS))
+@pytest.mark.parametrize("ci", range(len(DISC_CASES)))
 def test_element_callbacks_match_oracle_random(cuda, tname, ci):
     roid = ROIDS[tname]
     dim = DIM[roid]
