@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const
 // Defect and FP64 Jacobian at the same state in one pass over the elements of a
 // colour (one launch per colour instead of two): the per-SCVF geometry, upwinds
 // and stabilisation are evaluated once for both outputs.
-template <int ROID, bool TRANSIENT>
+template <int ROID, bool TRANSIENT, typename VT>
 __global__ void __launch_bounds__(kThreads) k_defect_jacobian(const DiscParams P, const AsmArgs A) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, b = R::b;
@@ -245,18 +245,22 @@ __global__ void __launch_bounds__(kThreads) k_defect_jacobian(const DiscParams P
 #pragma unroll
             for (int k = 0; k < nsh; ++k) uo[d][k] = t4[d][k];
     }
-    GlobalJacSink<double, nsh> jsink{reinterpret_cast<double*>(A.vals), A.elemBlk + (int64_t)e * nsh * nsh};
+    GlobalJacSink<VT, nsh> jsink{reinterpret_cast<VT*>(A.vals), A.elemBlk + (int64_t)e * nsh * nsh};
     DiscParams Q = P;
     Q.transient = TRANSIENT ? 1 : 0;
     bool ok;
-    if constexpr (TRANSIENT) {
-        struct Scaled {
-            GlobalDefSink<nsh, b>& s; double dt;
-            __device__ __forceinline__ void add(int i, int f, double v) { s.add(i, f, v * dt); }
-        } ss{sink, P.dt};
-        ok = elem_def_jac_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(uo), ss, P.dt, jsink, nuEl);
+    struct Scaled {
+        GlobalDefSink<nsh, b>& s; double dt;
+        __device__ __forceinline__ void add(int i, int f, double v) { s.add(i, f, v * dt); }
+    } ss{sink, P.dt};
+    const double* uoPtr = TRANSIENT ? &uo[0][0] : &u[0][0];
+    const double(&uoRef)[dim][nsh] = *reinterpret_cast<const double(*)[dim][nsh]>(uoPtr);
+    if constexpr (std::is_same<VT, double>::value) {
+        if constexpr (TRANSIENT) ok = elem_def_jac_A<ROID, double>(Q, E, u, uoRef, ss, P.dt, jsink, nuEl);
+        else ok = elem_def_jac_A<ROID, double>(Q, E, u, uoRef, sink, 1.0, jsink, nuEl);
     } else {
-        ok = elem_def_jac_A<ROID, double>(Q, E, u, reinterpret_cast<const double(&)[dim][nsh]>(u), sink, 1.0, jsink, nuEl);
+        if constexpr (TRANSIENT) ok = elem_def_jac_A_mixed<ROID>(Q, E, u, uoRef, ss, (float)P.dt, jsink, nuEl);
+        else ok = elem_def_jac_A_mixed<ROID>(Q, E, u, uoRef, sink, 1.0f, jsink, nuEl);
     }
     if (!ok) atomicOr(A.err, 1);
     // mass (implicit Euler) and source parts, per SCV: defect as in k_defect, Jacobian as in k_jacobian
@@ -272,9 +276,9 @@ __global__ void __launch_bounds__(kThreads) k_defect_jacobian(const DiscParams P
             if (any) atomicAdd(A.D + (int64_t)sink.nodes[k] * b + f, v);
         }
         if constexpr (TRANSIENT) {
-            double* p = jsink.vals + (int64_t)__ldg(jsink.blk + k * nsh + k) * (b * b);
+            VT* p = jsink.vals + (int64_t)__ldg(jsink.blk + k * nsh + k) * (b * b);
 #pragma unroll
-            for (int d = 0; d < dim; ++d) atomicAdd(p + d * b + d, E.vol[k] * rho);
+            for (int d = 0; d < dim; ++d) atomicAdd(p + d * b + d, (VT)(E.vol[k] * rho));
         }
     }
 }
@@ -408,13 +412,19 @@ cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int
     });
 }
 
-cudaError_t launch_defect_jacobian(int roid, const DiscParams& P, const AsmArgs& a, cudaStream_t s, int threads) {
+cudaError_t launch_defect_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s, int threads) {
     if (a.count <= 0) return cudaSuccess;
     const int t = clamp_threads(threads);
     const int grid = (a.count + t - 1) / t;
     return dispatch_roid(roid, [&](auto r) {
-        if (P.transient) k_defect_jacobian<decltype(r)::value, true><<<grid, t, 0, s>>>(P, a);
-        else k_defect_jacobian<decltype(r)::value, false><<<grid, t, 0, s>>>(P, a);
+        constexpr int RO = decltype(r)::value;
+        if (prec == 0) {
+            if (P.transient) k_defect_jacobian<RO, true, double><<<grid, t, 0, s>>>(P, a);
+            else k_defect_jacobian<RO, false, double><<<grid, t, 0, s>>>(P, a);
+        } else {
+            if (P.transient) k_defect_jacobian<RO, true, float><<<grid, t, 0, s>>>(P, a);
+            else k_defect_jacobian<RO, false, float><<<grid, t, 0, s>>>(P, a);
+        }
     });
 }
 

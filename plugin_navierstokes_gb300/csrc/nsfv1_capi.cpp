@@ -575,20 +575,20 @@ bool Disc::assemble_defect_jacobian(const double* u, const double* u_old, double
     if (!hasMesh) return fail(NSFV1_ERR_STATE, "assemble_defect_jacobian: no mesh set");
     if (!u || !d || !vals) return fail(NSFV1_ERR_ARGUMENT, "assemble_defect_jacobian: null pointer");
     if (prec != NSFV1_F64 && prec != NSFV1_F32) return fail(NSFV1_ERR_ARGUMENT, "assemble_defect_jacobian: precision must be NSFV1_F64 or NSFV1_F32");
-    // FP32 values: the FP64 defect and the FP32-arithmetic Jacobian kernel (cheaper than
-    // deriving FP32 blocks from the FP64 element state)
-    if (prec == NSFV1_F32) return assemble_defect(u, u_old, dt, d, s) && assemble_jacobian(u, u_old, dt, vals, prec, s);
+    if (prec == NSFV1_F32 && dim == 3 && (reinterpret_cast<uintptr_t>(vals) & 15))
+        return fail(NSFV1_ERR_ARGUMENT, "assemble_defect_jacobian: FP32 values of a 3D mesh must be 16-byte aligned");
     DiscParams P;
     if (!params(P, u_old != nullptr, dt)) return false;
     const int b = dim + 1;
     if (!cuda_ok(cudaMemsetAsync(d, 0, sizeof(double) * nNodes * b, s), "memset defect")) return false;
-    if (!cuda_ok(cudaMemsetAsync(vals, 0, colIdx.size() * b * b * sizeof(double), s), "memset jacobian")) return false;
+    const size_t vsize = prec == NSFV1_F64 ? sizeof(double) : sizeof(float);
+    if (!cuda_ok(cudaMemsetAsync(vals, 0, colIdx.size() * b * b * vsize, s), "memset jacobian")) return false;
     for (int c = 0; c < nColors; ++c) {
         AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, d, vals,
                   d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive};
-        if (!cuda_ok(launch_defect_jacobian(roid, P, a, s, asmThreads), "defect+jacobian kernel")) return false;
+        if (!cuda_ok(launch_defect_jacobian(roid, P, a, prec, s, asmThreads), "defect+jacobian kernel")) return false;
     }
-    if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, d, vals, NSFV1_F64, s), "dirichlet")) return false;
+    if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, d, vals, prec, s), "dirichlet")) return false;
     return check_err_word(s);
 }
 

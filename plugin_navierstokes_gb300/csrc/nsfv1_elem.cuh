@@ -26,6 +26,7 @@
 // runtime index is selected from registers without local-memory indexing.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 #include "nsfv1_params.h"
 #include "nsfv1_refelem.cuh"
 
@@ -34,32 +35,36 @@ namespace nsfv1 {
 // ---------------------------------------------------------------------------
 // per-element-type tables (generated at compile time from nsfv1_refelem.cuh)
 // ---------------------------------------------------------------------------
-struct ElemTab {
-    double ipLoc[12][3];   // local (reference) coordinates of the SCVF integration points
-    double ipShape[12][8];
-    double ipLGrad[12][8][3];
-    double refCo[8][3];
+// Tables in the arithmetic type F of the kernel (double or float): a float
+// kernel reading double constants would convert every use on the FP64 pipe.
+template <typename F>
+struct ElemTabT {
+    F ipLoc[12][3];   // local (reference) coordinates of the SCVF integration points
+    F ipShape[12][8];
+    F ipLGrad[12][8][3];
+    F refCo[8][3];
     int edge[12][2];
     int edgeFace[12][2];
     int side[6][4];
     int sideNco[6];
     int sideMask[6];   // bit k set: corner k belongs to the side
 };
+typedef ElemTabT<double> ElemTab;
 
-template <int ROID> constexpr ElemTab make_tab() {
+template <int ROID, typename F> constexpr ElemTabT<F> make_tab() {
     using R = Ref<ROID>;
-    ElemTab t{};
+    ElemTabT<F> t{};
     for (int ip = 0; ip < R::nip; ++ip) {
         for (int k = 0; k < R::nsh; ++k) {
-            t.ipShape[ip][k] = ip_shape<ROID>(ip, k);
-            for (int d = 0; d < R::dim; ++d) t.ipLGrad[ip][k][d] = ip_lgrad<ROID>(ip, k, d);
+            t.ipShape[ip][k] = F(ip_shape<ROID>(ip, k));
+            for (int d = 0; d < R::dim; ++d) t.ipLGrad[ip][k][d] = F(ip_lgrad<ROID>(ip, k, d));
         }
-        for (int d = 0; d < 3; ++d) t.ipLoc[ip][d] = d < R::dim ? loc_ip<R>(ip, d) : 0.0;
+        for (int d = 0; d < 3; ++d) t.ipLoc[ip][d] = F(d < R::dim ? loc_ip<R>(ip, d) : 0.0);
         t.edge[ip][0] = R::edge(ip, 0); t.edge[ip][1] = R::edge(ip, 1);
         t.edgeFace[ip][0] = R::edge_face(ip, 0); t.edgeFace[ip][1] = R::edge_face(ip, 1);
     }
     for (int c = 0; c < R::nsh; ++c)
-        for (int d = 0; d < 3; ++d) t.refCo[c][d] = d < R::dim ? R::co(c, d) : 0.0;
+        for (int d = 0; d < 3; ++d) t.refCo[c][d] = F(d < R::dim ? R::co(c, d) : 0.0);
     for (int s = 0; s < R::nside; ++s) {
         t.sideNco[s] = R::side_nco(s);
         int m = 0;
@@ -72,16 +77,27 @@ template <int ROID> constexpr ElemTab make_tab() {
     return t;
 }
 
-static __constant__ ElemTab c_tabTri = make_tab<ROID_TRIANGLE>();
-static __constant__ ElemTab c_tabQuad = make_tab<ROID_QUADRILATERAL>();
-static __constant__ ElemTab c_tabTet = make_tab<ROID_TETRAHEDRON>();
-static __constant__ ElemTab c_tabHex = make_tab<ROID_HEXAHEDRON>();
+static __constant__ ElemTabT<double> c_tabTri = make_tab<ROID_TRIANGLE, double>();
+static __constant__ ElemTabT<double> c_tabQuad = make_tab<ROID_QUADRILATERAL, double>();
+static __constant__ ElemTabT<double> c_tabTet = make_tab<ROID_TETRAHEDRON, double>();
+static __constant__ ElemTabT<double> c_tabHex = make_tab<ROID_HEXAHEDRON, double>();
+static __constant__ ElemTabT<float> c_tabTriF = make_tab<ROID_TRIANGLE, float>();
+static __constant__ ElemTabT<float> c_tabQuadF = make_tab<ROID_QUADRILATERAL, float>();
+static __constant__ ElemTabT<float> c_tabTetF = make_tab<ROID_TETRAHEDRON, float>();
+static __constant__ ElemTabT<float> c_tabHexF = make_tab<ROID_HEXAHEDRON, float>();
 
-template <int ROID> __device__ __forceinline__ const ElemTab& tab() {
-    if constexpr (ROID == ROID_TRIANGLE) return c_tabTri;
-    else if constexpr (ROID == ROID_QUADRILATERAL) return c_tabQuad;
-    else if constexpr (ROID == ROID_TETRAHEDRON) return c_tabTet;
-    else return c_tabHex;
+template <int ROID, typename F = double> __device__ __forceinline__ const ElemTabT<F>& tab() {
+    if constexpr (std::is_same<F, float>::value) {
+        if constexpr (ROID == ROID_TRIANGLE) return c_tabTriF;
+        else if constexpr (ROID == ROID_QUADRILATERAL) return c_tabQuadF;
+        else if constexpr (ROID == ROID_TETRAHEDRON) return c_tabTetF;
+        else return c_tabHexF;
+    } else {
+        if constexpr (ROID == ROID_TRIANGLE) return c_tabTri;
+        else if constexpr (ROID == ROID_QUADRILATERAL) return c_tabQuad;
+        else if constexpr (ROID == ROID_TETRAHEDRON) return c_tabTet;
+        else return c_tabHex;
+    }
 }
 
 template <typename T> struct Num;
@@ -285,7 +301,7 @@ template <int ROID, typename T>
 __device__ __forceinline__ void ip_geom(const Elem<ROID, T>& E, const int ip, IpGeo<T>& G) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh;
-    const ElemTab& tb = tab<ROID>();
+    const auto& tb = tab<ROID, T>();
     G.from = tb.edge[ip][0]; G.to = tb.edge[ip][1];
     pick(E.x, G.from, G.xf);
     pick(E.x, G.to, G.xt);
@@ -335,7 +351,7 @@ __device__ __forceinline__ void ip_geom(const Elem<ROID, T>& E, const int ip, Ip
 template <int ROID, typename T>
 __device__ __forceinline__ void ip_grad(const IpGeo<T>& G, const int ip, const int k, T g[3]) {
     constexpr int dim = Ref<ROID>::dim;
-    const ElemTab& tb = tab<ROID>();
+    const auto& tb = tab<ROID, T>();
 #pragma unroll
     for (int r = 0; r < dim; ++r) {
         T s = T(0);
@@ -346,7 +362,7 @@ __device__ __forceinline__ void ip_grad(const IpGeo<T>& G, const int ip, const i
 }
 
 template <int ROID, typename T>
-__device__ __forceinline__ T ipN(const int ip, const int k) { return T(tab<ROID>().ipShape[ip][k]); }
+__device__ __forceinline__ T ipN(const int ip, const int k) { return T(tab<ROID, T>().ipShape[ip][k]); }
 
 // ---------------------------------------------------------------------------
 // Upwind shapes of one SCVF (INavierStokesUpwind::compute, upwind.cpp)
@@ -369,7 +385,7 @@ __device__ __forceinline__ bool ray_upwind(const Elem<ROID, T>& E, const T* from
                                            T (&up)[Ref<ROID>::nsh], T& convLen) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh;
-    const ElemTab& tb = tab<ROID>();
+    const auto& tb = tab<ROID, T>();
     const T tol = T(1e-12);
     int hitSide = -1;
     T gInt[3] = {T(0), T(0), T(0)}, lInt[3] = {T(0), T(0), T(0)};
@@ -492,7 +508,7 @@ __device__ __forceinline__ bool ray_upwind(const Elem<ROID, T>& E, const T* from
 // s |vel|. The downwind exit (velocity negated, FLOW) uses the same w with the
 // opposite sign. Same point as the side-by-side ray test, in closed form.
 template <int ROID, typename T>
-__device__ __forceinline__ bool lps_affine(const ElemTab& tb, const T (&w)[3], const int ip, const bool down, const T vnorm,
+__device__ __forceinline__ bool lps_affine(const ElemTabT<T>& tb, const T (&w)[3], const int ip, const bool down, const T vnorm,
                                            T (&up)[Ref<ROID>::nsh], T& convLen) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh;
@@ -587,7 +603,7 @@ __device__ __forceinline__ bool upwind_shapes(const int type, const Elem<ROID, T
         convLen = T(1);
         return true;
     }
-    if (type == UPW_LPS && E.affine) return lps_affine<ROID, T>(tab<ROID>(), wref, ip, down, vnorm, up, convLen);
+    if (type == UPW_LPS && E.affine) return lps_affine<ROID, T>(tab<ROID, T>(), wref, ip, down, vnorm, up, convLen);
     return ray_upwind<ROID, T>(E, G.gip, vel, type == UPW_LPS, up, convLen);
 }
 
@@ -662,7 +678,7 @@ struct IpState {
     T dnS[nsh];         // stabilisation downwind shapes (FLOW)
     T nuL;              // nu / L_diff^2
     T nsvcl, nsvdl;     // |v| / L_up ; |v| / (L_down + L_up)
-    T diag;
+    T diag, idiag;      // the stabilisation's diagonal and its inverse (0 without stabilisation)
     bool ok;
 };
 
@@ -727,7 +743,7 @@ __device__ __forceinline__ void ip_state(const DiscParams& P, const Elem<ROID, T
             for (int k = 0; k < nsh; ++k) S.upC[k] = S.upS[k];
         }
     }
-    S.nuL = T(0); S.nsvcl = T(0); S.nsvdl = T(0); S.diag = T(1);
+    S.nuL = T(0); S.nsvcl = T(0); S.nsvdl = T(0); S.diag = T(1); S.idiag = T(0);
     if (P.stab == STAB_WITHOUT) return;
     const T Linv = diff_len_sq_inv<ROID, T>(P.diffLen, E, G, corMinN, corMinD, corAvgN);
     S.nuL = nuEl * Linv;
@@ -738,6 +754,7 @@ __device__ __forceinline__ void ip_state(const DiscParams& P, const Elem<ROID, T
     S.diag = S.nuL;
     if (P.transient) S.diag += T(1) / T(P.dt);
     if (!stokes) S.diag += S.nsvcl;
+    S.idiag = T(1) / S.diag;
 }
 
 // peclet_blend weight (navier_stokes_fv1.cpp:871-892); blends UpwindVel in place
@@ -773,7 +790,7 @@ __device__ __forceinline__ void scvf_def_A(const DiscParams& P, const Elem<ROID,
         // (grad_k = J^-T lgrad_k, so sum_k u_k grad_k = J^-T sum_k u_k lgrad_k)
         T gradVel[3][3], gradP[3];
         {
-            const ElemTab& tb = tab<ROID>();
+            const auto& tb = tab<ROID, T>();
             T gl[4][3];
 #pragma unroll
             for (int f = 0; f <= dim; ++f)
@@ -843,7 +860,7 @@ __device__ __forceinline__ void scvf_def_A(const DiscParams& P, const Elem<ROID,
             T trace = T(0);
 #pragma unroll
             for (int d = 0; d < dim; ++d) trace += gradVel[d][d];
-            const T idiag = T(1) / S.diag;
+            const T idiag = S.idiag, irho = T(1) / rho;
 #pragma unroll
             for (int d = 0; d < dim; ++d) {
                 T rhs = T(0);
@@ -873,7 +890,7 @@ __device__ __forceinline__ void scvf_def_A(const DiscParams& P, const Elem<ROID,
                         if (d2 != d) cross += S.StdVel[d2] * gradVel[d][d2];
                     rhs += S.StdVel[d] * (trace - gradVel[d][d]) - cross;
                 }
-                rhs -= gradP[d] / rho;
+                rhs -= gradP[d] * irho;
                 stabVel[d] = rhs * idiag;
             }
         }
@@ -914,7 +931,7 @@ __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID,
 // implicit-Euler Jacobian M + dt dA/du).
 // ---------------------------------------------------------------------------
 template <int ROID, typename T, class Sink>
-__device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const Elem<ROID, T>& E, const IpGeo<T>& G, const IpState<ROID, T>& S,
+__device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const IpGeo<T>& G, const IpState<ROID, T>& S,
                                            const int ip, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh], const T scale, Sink& sink,
                                            const T nu) {
     using R = Ref<ROID>;
@@ -937,13 +954,13 @@ __device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const Elem<ROID,
             if (P.peclet) w = peclet_blend<ROID, T>(G, S.StdVel, nu, UpwindVel);
             prod = Vn * rho;
         }
-        const T idiag = (P.stab == STAB_WITHOUT) ? T(0) : T(1) / S.diag;
+        const T idiag = S.idiag;
         const T ri = rho * idiag;
         // per-SCVF factors of the column loop
         T mn[3], rin[3], nrho[3];
 #pragma unroll
         for (int d = 0; d < dim; ++d) { mn[d] = mnr * G.n[d]; rin[d] = ri * G.n[d]; nrho[d] = G.n[d] * rho; }
-        const T riVn = ri * Vn, pw = prod * w, ppe = prod * (T(1) - w), ppr = -ri / rho;
+        const T riVn = ri * Vn, pw = prod * w, ppe = prod * (T(1) - w), ppr = -ri * (T(1) / rho);
 #pragma unroll
         for (int k = 0; k < nsh; ++k) {
             T g[3];
@@ -1027,7 +1044,63 @@ __device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID,
         IpState<ROID, T> S;
         ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
         ok &= S.ok;
-        scvf_jac_A<ROID, T>(P, E, G, S, ip, u, scale, sink, nu);
+        scvf_jac_A<ROID, T>(P, G, S, ip, u, scale, sink, nu);
+    }
+    return ok;
+}
+
+// FP32 copies of the per-SCVF geometry and state (the FP32-Jacobian blocks of
+// the fused pass are formed from the FP64 state the defect used)
+__device__ __forceinline__ void narrow(const IpGeo<double>& a, IpGeo<float>& o) {
+    o.from = a.from; o.to = a.to;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        o.n[d] = (float)a.n[d]; o.gip[d] = (float)a.gip[d]; o.em[d] = (float)a.em[d];
+        o.xf[d] = (float)a.xf[d]; o.xt[d] = (float)a.xt[d];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o.JtInv[d][c] = (float)a.JtInv[d][c];
+    }
+}
+template <int ROID>
+__device__ __forceinline__ void narrow(const IpState<ROID, double>& a, IpState<ROID, float>& o) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) o.StdVel[d] = (float)a.StdVel[d];
+#pragma unroll
+    for (int k = 0; k < Ref<ROID>::nsh; ++k) { o.upC[k] = (float)a.upC[k]; o.upS[k] = (float)a.upS[k]; o.dnS[k] = (float)a.dnS[k]; }
+    o.nuL = (float)a.nuL; o.nsvcl = (float)a.nsvcl; o.nsvdl = (float)a.nsvdl;
+    o.diag = (float)a.diag; o.idiag = (float)a.idiag; o.ok = a.ok;
+}
+
+// FP64 defect and FP32 Jacobian of one element in one pass: geometry, upwinds,
+// stabilisation and defect in FP64; the Jacobian blocks in FP32 from that state.
+template <int ROID, class DSink, class JSink>
+__device__ __forceinline__ bool elem_def_jac_A_mixed(const DiscParams& P, const Elem<ROID, double>& E,
+                                                     const double (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
+                                                     const double (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], DSink& dsink, const float jscale,
+                                                     JSink& jsink, const double nu) {
+    using R = Ref<ROID>;
+    constexpr int b = R::b, nsh = R::nsh;
+    double corMinN = 0.0, corMinD = 0.0, corAvgN = 1.0;
+    if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, double>(E, corMinN, corMinD, corAvgN);
+    float uf[b][nsh];
+#pragma unroll
+    for (int f = 0; f < b; ++f)
+#pragma unroll
+        for (int k = 0; k < nsh; ++k) uf[f][k] = (float)u[f][k];
+    bool ok = true;
+#pragma unroll 1
+    for (int ip = 0; ip < R::nip; ++ip) {
+        IpGeo<double> G;
+        ip_geom<ROID, double>(E, ip, G);
+        IpState<ROID, double> S;
+        ip_state<ROID, double>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
+        ok &= S.ok;
+        scvf_def_A<ROID, double>(P, E, G, S, ip, u, uo, dsink, nu);
+        IpGeo<float> Gf;
+        IpState<ROID, float> Sf;
+        narrow(G, Gf);
+        narrow<ROID>(S, Sf);
+        scvf_jac_A<ROID, float>(P, Gf, Sf, ip, uf, jscale, jsink, (float)nu);
     }
     return ok;
 }
@@ -1054,7 +1127,7 @@ __device__ __forceinline__ bool elem_def_jac_A(const DiscParams& P, const Elem<R
         ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
         ok &= S.ok;
         scvf_def_A<ROID, T>(P, E, G, S, ip, u, uo, dsink, nu);
-        scvf_jac_A<ROID, T>(P, E, G, S, ip, u, jscale, jsink, nu);
+        scvf_jac_A<ROID, T>(P, G, S, ip, u, jscale, jsink, nu);
     }
     return ok;
 }

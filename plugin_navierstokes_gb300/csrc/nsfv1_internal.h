@@ -38,8 +38,9 @@ struct ElemBatchArgs {
 // threads: CTA size of the colour launches (32..128, a multiple of 32)
 cudaError_t launch_defect(int roid, const DiscParams& P, const AsmArgs& a, cudaStream_t s, int threads = 128);
 cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s, int threads = 128);
-// defect (a.D) and FP64 Jacobian (a.vals) at the same state, one launch per colour
-cudaError_t launch_defect_jacobian(int roid, const DiscParams& P, const AsmArgs& a, cudaStream_t s, int threads = 128);
+// FP64 defect (a.D) and the Jacobian (a.vals; prec 0: FP64, 1: FP32 blocks from the FP64
+// state) at the same state, one launch per colour
+cudaError_t launch_defect_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s, int threads = 128);
 cudaError_t launch_elem_batch(int roid, const DiscParams& P, const ElemBatchArgs& a, cudaStream_t s);
 cudaError_t launch_dirichlet(int b, int64_t n, const int32_t* rows, const double* vals, const int32_t* rowPtr,
                              const int32_t* colIdx, const double* U, double* D, void* J, int prec, cudaStream_t s);
