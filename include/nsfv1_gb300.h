@@ -148,6 +148,13 @@ int nsfv1_assemble_defect_jacobian(nsfv1_disc* h, const double* u, const double*
 int nsfv1_elem_batch(nsfv1_disc* h, int elem_type, int64_t n, const double* corners, const double* u, const double* u_old,
                      double dt, double* defA, double* jacA, double* defM, double* jacM, double* rhs, void* stream);
 
+/* The same callbacks with HOST arrays (same layouts): the library stages them
+ * through device memory it allocates for the call and returns when the outputs
+ * are on the host. For host-side element loops such as a ugcore IElemDisc
+ * adapter (navier_stokes_fv1.cpp:1553-1579 registers the reference's). */
+int nsfv1_elem_batch_host(nsfv1_disc* h, int elem_type, int64_t n, const double* corners, const double* u, const double* u_old,
+                          double dt, double* defA, double* jacA, double* defM, double* jacM, double* rhs);
+
 /* ---- linear algebra on the handle's pattern (device pointers) ------------ */
 
 /* y = J x with J in the handle's block CSR (prec as above; x, y FP64) */

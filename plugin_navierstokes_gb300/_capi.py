@@ -111,6 +111,8 @@ _SIGS = {
     "nsfv1_assemble_defect_jacobian": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p, c_int, c_void_p]),
     "nsfv1_elem_batch": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p]),
+    "nsfv1_elem_batch_host": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
+                                      c_void_p, c_void_p, c_void_p]),
     "nsfv1_bsr_mv": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "nsfv1_block_jacobi": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "nsfv1_block_jacobi_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),

@@ -461,6 +461,45 @@ int nsfv1_elem_batch(nsfv1_disc* h, int elem_type, int64_t n, const double* corn
     return D->check_err_word(s) ? NSFV1_OK : D->status;
 }
 
+int nsfv1_elem_batch_host(nsfv1_disc* h, int elem_type, int64_t n, const double* corners, const double* u, const double* u_old,
+                          double dt, double* defA, double* jacA, double* defM, double* jacM, double* rhs) {
+    NSFV1_H;
+    const int dim = ref_dim(elem_type), nsh = ref_nsh(elem_type);
+    if (dim != D->dim) { D->fail(NSFV1_ERR_ARGUMENT, "element dimension does not match the disc"); return D->status; }
+    if (n < 0 || (n > 0 && (!corners || !u))) { D->fail(NSFV1_ERR_ARGUMENT, "elem_batch_host: bad arguments"); return D->status; }
+    {
+        DiscParams P;   // the setup checks of prep_elem_loop, also for an empty batch
+        if (!D->params(P, u_old != nullptr, dt)) return D->status;
+    }
+    if (n == 0) return NSFV1_OK;
+    const size_t nloc = (size_t)(dim + 1) * nsh, nc = (size_t)n * nsh * dim, nv = (size_t)n * nloc, nm = (size_t)n * nloc * nloc;
+    // device staging: corners, u, u_old, and every requested output
+    const size_t total = nc + nv * (u_old ? 2 : 1) + (defA ? nv : 0) + (defM ? nv : 0) + (rhs ? nv : 0) + (jacA ? nm : 0) + (jacM ? nm : 0);
+    double* buf = nullptr;
+    if (!D->cuda_ok(cudaMalloc((void**)&buf, total * sizeof(double)), "elem_batch_host: staging")) return D->status;
+    double* p = buf;
+    auto take = [&](size_t cnt) { double* q = p; p += cnt; return q; };
+    double* dC = take(nc);
+    double* dU = take(nv);
+    double* dUo = u_old ? take(nv) : nullptr;
+    double* dDA = defA ? take(nv) : nullptr;
+    double* dDM = defM ? take(nv) : nullptr;
+    double* dR = rhs ? take(nv) : nullptr;
+    double* dJA = jacA ? take(nm) : nullptr;
+    double* dJM = jacM ? take(nm) : nullptr;
+    bool ok = D->cuda_ok(cudaMemcpy(dC, corners, nc * 8, cudaMemcpyHostToDevice), "elem_batch_host: copy") &&
+              D->cuda_ok(cudaMemcpy(dU, u, nv * 8, cudaMemcpyHostToDevice), "elem_batch_host: copy") &&
+              (!u_old || D->cuda_ok(cudaMemcpy(dUo, u_old, nv * 8, cudaMemcpyHostToDevice), "elem_batch_host: copy"));
+    if (ok) ok = nsfv1_elem_batch(h, elem_type, n, dC, dU, dUo, dt, dDA, dJA, dDM, dJM, dR, nullptr) == NSFV1_OK;
+    auto back = [&](double* host, const double* dev, size_t cnt) {
+        return !host || D->cuda_ok(cudaMemcpy(host, dev, cnt * 8, cudaMemcpyDeviceToHost), "elem_batch_host: copy back");
+    };
+    if (ok) ok = back(defA, dDA, nv) && back(defM, dDM, nv) && back(rhs, dR, nv) && back(jacA, dJA, nm) && back(jacM, dJM, nm);
+    const int st = D->status;
+    cudaFree(buf);
+    return ok ? NSFV1_OK : (st ? st : NSFV1_ERR_CUDA);
+}
+
 int nsfv1_set_assembly_threads(nsfv1_disc* h, int threads) {
     Disc* D = reinterpret_cast<Disc*>(h);
     if (!D) return NSFV1_ERR_ARGUMENT;
