@@ -118,6 +118,30 @@ int nsfv1_device_pattern(const nsfv1_disc* h, const int32_t** row_ptr, const int
  * DirichletBoundary semantics, bnd/wall_impl.h:57-69). */
 int nsfv1_set_dirichlet(nsfv1_disc* h, int64_t n, const int32_t* dofs, const double* values);
 
+/* ---- boundary-condition element discs (host arrays) ---------------------- */
+
+/* NavierStokesWall::add(subsets) (incompressible/bnd/wall_impl.h:57-69): every
+ * velocity component of the given nodes is a Dirichlet row with value 0.
+ * Rows accumulate with earlier nsfv1_add_wall / nsfv1_add_inflow calls (a later
+ * value of the same unknown wins); nsfv1_set_dirichlet replaces them all. */
+int nsfv1_add_wall(nsfv1_disc* h, int64_t n_nodes, const int32_t* nodes);
+/* NavierStokesInflowFV1::add(velocity, subsets) (incompressible/fv1/bnd/
+ * inflow_fv1_impl.h:57-82) for a constant inflow velocity vel[dim] on the given
+ * boundary sides (n_sides x side_nco node ids; 2D: edges of 2 nodes, 3D:
+ * triangles of 3 or quadrilaterals of 4 nodes, in the element's side order):
+ *  - Dirichlet rows velocity = vel at every node of the sides (the reference's
+ *    DirichletBoundary on the velocity functions);
+ *  - the Neumann flux of the continuity equation (the reference's
+ *    NeumannBoundaryFV1 on the pressure function with the same vector data):
+ *    the continuity defect of each side corner gets + vel . n_bf, n_bf the
+ *    outward, area-weighted normal of that corner's part of the side in the
+ *    FV1 dual mesh ({corner, edge midpoints, side centre}); scaled by dt in
+ *    the implicit-Euler defect, like every right-hand side.
+ * A side must belong to exactly one element (NSFV1_ERR_ARGUMENT otherwise). */
+int nsfv1_add_inflow(nsfv1_disc* h, int64_t n_sides, int side_nco, const int32_t* side_nodes, const double* vel);
+/* removes every Dirichlet row and inflow flux */
+int nsfv1_clear_boundary(nsfv1_disc* h);
+
 /* ---- assembly (device pointers) ----------------------------------------- */
 
 /* Global defect d = A(u) - F (stationary, u_old == NULL) or

@@ -54,6 +54,8 @@ def load():
             "ora_assemble": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p, c_int]),
             "ora_newton": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_double, c_int, c_double, c_int, c_int, c_int, c_void_p]),
             "ora_bsr_mv": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+            "ora_add_wall": (c_int, [c_void_p, c_int64, c_void_p]),
+            "ora_add_inflow": (c_int, [c_void_p, c_int64, c_int, c_void_p, c_void_p]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)
@@ -144,6 +146,15 @@ class Oracle:
         self.dofs = np.ascontiguousarray(dofs, np.int32)
         self.dvals = np.ascontiguousarray(vals, np.float64)
         self._c(self.lib.ora_set_dirichlet(self.h, self.dofs.size, self.dofs.ctypes.data, self.dvals.ctypes.data))
+
+    def add_wall(self, nodes):
+        a = np.ascontiguousarray(nodes, np.int32)
+        self._c(self.lib.ora_add_wall(self.h, a.size, a.ctypes.data))
+
+    def add_inflow(self, vel, sides):
+        v = np.ascontiguousarray(vel, np.float64).ravel()
+        sd = np.ascontiguousarray(np.atleast_2d(sides), np.int32)
+        self._c(self.lib.ora_add_inflow(self.h, sd.shape[0], sd.shape[1], sd.ctypes.data, v.ctypes.data))
 
     def assemble(self, U, U_old=None, dt=0.0, defect=True, jacobian=True, nthreads=1):
         U = np.ascontiguousarray(U, np.float64).ravel()

@@ -1042,9 +1042,61 @@ struct Problem {
     Mesh mesh;
     std::vector<int32_t> dirRow;   // node * b + fct
     std::vector<number> dirVal;
+    std::vector<number> bndFlux;   // continuity right-hand side of inflow boundaries, per node
     std::string lastError;
     explicit Problem(int dim) : disc(dim) {}
 };
+
+/* ------------------------------------------------------------------------ */
+/* Boundary element discs (incompressible/bnd/wall_impl.h:57-69,            */
+/* incompressible/fv1/bnd/inflow_fv1_impl.h:57-82) with ugcore's            */
+/* DirichletBoundary and NeumannBoundaryFV1 (absent) restated:              */
+/*  - Dirichlet rows: defect u - g, Jacobian identity row; a later value for */
+/*    the same unknown replaces an earlier one;                             */
+/*  - NeumannBoundaryFV1 with vector data j on the pressure function: the    */
+/*    right-hand side of the continuity row of every boundary corner gets    */
+/*    -(j . n_bf), n_bf the outward normal of the corner's boundary face     */
+/*    (the part {corner, side-edge midpoints, side centre} of the side), so  */
+/*    the defect d = A(u) - F gets + j . n_bf (dt-scaled when transient).    */
+/* ------------------------------------------------------------------------ */
+static void merge_dirichlet(Problem& P, const std::vector<int32_t>& rows, const std::vector<number>& vals) {
+    std::vector<std::pair<int32_t, number>> all;
+    for (size_t k = 0; k < P.dirRow.size(); ++k) all.emplace_back(P.dirRow[k], P.dirVal[k]);
+    for (size_t k = 0; k < rows.size(); ++k) all.emplace_back(rows[k], vals[k]);
+    std::stable_sort(all.begin(), all.end(), [](const std::pair<int32_t, number>& a, const std::pair<int32_t, number>& c) { return a.first < c.first; });
+    P.dirRow.clear();
+    P.dirVal.clear();
+    for (auto& x : all) {
+        if (!P.dirRow.empty() && P.dirRow.back() == x.first) P.dirVal.back() = x.second;
+        else { P.dirRow.push_back(x.first); P.dirVal.push_back(x.second); }
+    }
+}
+
+// outward area-weighted normal of the boundary face of side corner j
+static void boundary_face_normal(int dim, int nco, const number x[][3], int j, const number* elemCen, number* n) {
+    number sc[3] = {0, 0, 0};
+    for (int k = 0; k < nco; ++k) for (int d = 0; d < 3; ++d) sc[d] += x[k][d];
+    for (int d = 0; d < 3; ++d) sc[d] /= nco;
+    if (dim == 2) {
+        // the half side from corner j to the side midpoint
+        const number* a = x[j];
+        const number* o = x[1 - j];
+        number t[2] = {0.5 * (o[0] - a[0]), 0.5 * (o[1] - a[1])};
+        n[0] = t[1]; n[1] = -t[0]; n[2] = 0.0;
+    } else {
+        // quadrilateral {a, mid(a, next), side centre, mid(prev, a)}: half the cross product of its diagonals
+        const number* a = x[j];
+        const number* nx = x[(j + 1) % nco];
+        const number* pv = x[(j + nco - 1) % nco];
+        number d1[3], d2[3];
+        for (int d = 0; d < 3; ++d) { d1[d] = sc[d] - a[d]; d2[d] = 0.5 * (pv[d] + a[d]) - 0.5 * (a[d] + nx[d]); }
+        cross3(d1, d2, n);
+        for (int d = 0; d < 3; ++d) n[d] *= 0.5;
+    }
+    number dot = 0;
+    for (int d = 0; d < dim; ++d) dot += n[d] * (sc[d] - elemCen[d]);
+    if (dot < 0) for (int d = 0; d < 3; ++d) n[d] = -n[d];
+}
 
 static void gather_elem(const Mesh& m, int64_t e, const number* U, number* corners, number* uloc, int b) {
     const int nsh = m.nsh, dim = m.dim;
@@ -1131,6 +1183,9 @@ static void assemble(Problem& P, const number* U, const number* Uold, number dt,
             }
         }
     }
+    // inflow boundaries: the continuity rows' Neumann flux (a right-hand side: dt-scaled when transient)
+    if (D && !P.bndFlux.empty())
+        for (int64_t r = 0; r < m.nNodes; ++r) D[r * b + (b - 1)] += (transient ? dt : 1.0) * P.bndFlux[r];
     // Dirichlet rows: defect = u - g, Jacobian row = identity (off-diagonal blocks kept in the pattern)
     for (size_t k = 0; k < P.dirRow.size(); ++k) {
         const int64_t row = P.dirRow[k] / b;
@@ -1483,6 +1538,53 @@ int ora_newton(void* h, double* U, const double* Uold, double dt, double rtol, i
 }
 
 /* BSR mat-vec with the oracle's own loop (for SpMV parity tests). */
+int ora_add_wall(void* h, int64_t n, const int32_t* nodes) {
+    auto* P = static_cast<Problem*>(h);
+    const int dim = P->mesh.dim, b = dim + 1;
+    std::vector<int32_t> rows;
+    std::vector<number> vals;
+    for (int64_t k = 0; k < n; ++k) {
+        if (nodes[k] < 0 || nodes[k] >= P->mesh.nNodes) { P->lastError = "wall node out of range"; return 1; }
+        for (int d = 0; d < dim; ++d) { rows.push_back(nodes[k] * b + d); vals.push_back(0.0); }
+    }
+    merge_dirichlet(*P, rows, vals);
+    return 0;
+}
+
+int ora_add_inflow(void* h, int64_t nSides, int nco, const int32_t* sides, const double* vel) {
+    auto* P = static_cast<Problem*>(h);
+    Mesh& m = P->mesh;
+    const int dim = m.dim, b = dim + 1, nsh = m.nsh;
+    if (P->bndFlux.empty()) P->bndFlux.assign(m.nNodes, 0.0);
+    std::vector<int32_t> rows;
+    std::vector<number> vals;
+    for (int64_t s = 0; s < nSides; ++s) {
+        const int32_t* sn = sides + s * nco;
+        int64_t owner = -1;
+        int owners = 0;
+        for (int64_t e = 0; e < m.nElems; ++e) {
+            int found = 0;
+            for (int j = 0; j < nco; ++j)
+                for (int i = 0; i < nsh; ++i) found += (m.conn[e * nsh + i] == sn[j]);
+            if (found == nco) { owner = e; ++owners; }
+        }
+        if (owners != 1) { P->lastError = "inflow side is not a boundary side of exactly one element"; return 1; }
+        number x[4][3] = {{0}}, cen[3] = {0, 0, 0};
+        for (int j = 0; j < nco; ++j) for (int d = 0; d < dim; ++d) x[j][d] = m.coords[(int64_t)sn[j] * dim + d];
+        for (int i = 0; i < nsh; ++i) for (int d = 0; d < dim; ++d) cen[d] += m.coords[(int64_t)m.conn[owner * nsh + i] * dim + d] / nsh;
+        for (int j = 0; j < nco; ++j) {
+            number n[3];
+            boundary_face_normal(dim, nco, x, j, cen, n);
+            number vn = 0;
+            for (int d = 0; d < dim; ++d) vn += vel[d] * n[d];
+            P->bndFlux[sn[j]] += vn;
+            for (int d = 0; d < dim; ++d) { rows.push_back(sn[j] * b + d); vals.push_back(vel[d]); }
+        }
+    }
+    merge_dirichlet(*P, rows, vals);
+    return 0;
+}
+
 int ora_bsr_mv(void* h, const double* V, const double* x, double* y) {
     auto* P = static_cast<Problem*>(h);
     bsr_mv(P->mesh, P->mesh.dim + 1, V, x, y);

@@ -7,6 +7,6 @@ reference's NavierStokesFV1 interface.
 """
 from . import _capi, mesh
 from ._capi import NSFV1Error
-from .navier_stokes_fv1 import NavierStokesFV1, mesh_pattern
+from .navier_stokes_fv1 import NavierStokesFV1, NavierStokesInflowFV1, NavierStokesWall, mesh_pattern
 
-__all__ = ["NavierStokesFV1", "NSFV1Error", "mesh", "mesh_pattern", "_capi"]
+__all__ = ["NavierStokesFV1", "NavierStokesInflowFV1", "NavierStokesWall", "NSFV1Error", "mesh", "mesh_pattern", "_capi"]

@@ -372,6 +372,14 @@ __global__ void k_dirichlet(int b, int64_t n, const int32_t* __restrict__ rows, 
     }
 }
 
+// ---- inflow boundary flux of the continuity rows ---------------------------------
+__global__ void k_bnd_flux(int b, int64_t n, double scale, const double* __restrict__ flux, double* D) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double f = flux[i];
+    if (f != 0.0) D[i * b + b - 1] += scale * f;
+}
+
 // ---- launchers ------------------------------------------------------------------
 
 template <class F>
@@ -432,6 +440,12 @@ cudaError_t launch_elem_batch(int roid, const DiscParams& P, const ElemBatchArgs
     if (a.n <= 0) return cudaSuccess;
     const int grid = (int)((a.n + kThreads - 1) / kThreads);
     return dispatch_roid(roid, [&](auto r) { k_elem_batch<decltype(r)::value><<<grid, kThreads, 0, s>>>(P, a); });
+}
+
+cudaError_t launch_bnd_flux(int b, int64_t nNodes, double scale, const double* flux, double* D, cudaStream_t s) {
+    if (!flux || nNodes <= 0) return cudaSuccess;
+    k_bnd_flux<<<(int)((nNodes + 255) / 256), 256, 0, s>>>(b, nNodes, scale, flux, D);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_dirichlet(int b, int64_t n, const int32_t* rows, const double* vals, const int32_t* rowPtr,

@@ -76,7 +76,8 @@ template <class T> static cudaError_t dupload(T*& dst, const T* src, size_t n) {
 
 void Disc::free_mesh() {
     dfree(d_coords); dfree(d_conn); dfree(d_elemBlk); dfree(d_colorElems); dfree(d_rowPtr); dfree(d_colIdx);
-    dfree(d_dirRow); dfree(d_dirVal); dfree(d_diagPos); dfree(d_bjDinv); dfree(d_nuElem);
+    dfree(d_dirRow); dfree(d_dirVal); dfree(d_diagPos); dfree(d_bjDinv); dfree(d_nuElem); dfree(d_bndFlux);
+    bndFluxHost.clear();
     dfree(d_instNode0); dfree(d_elemInst); dfree(d_nodeInst); dfree(d_instActive);
     nInst = 0; instNode0.clear(); instSkip = false;
     // the batched solver's levels, graphs and buffers belong to this mesh
@@ -428,6 +429,156 @@ int nsfv1_set_dirichlet(nsfv1_disc* h, int64_t n, const int32_t* dofs, const dou
     return NSFV1_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// merges Dirichlet rows into the handle's (a later value of the same dof wins), rows sorted by dof
+int merge_dirichlet(nsfv1_disc* h, Disc* D, const std::vector<int32_t>& dofs, const std::vector<double>& vals) {
+    std::vector<std::pair<int32_t, double>> all;
+    for (size_t k = 0; k < D->dirRowHost.size(); ++k) all.emplace_back(D->dirRowHost[k], D->dirValHost[k]);
+    for (size_t k = 0; k < dofs.size(); ++k) all.emplace_back(dofs[k], vals[k]);
+    std::stable_sort(all.begin(), all.end(), [](const auto& a, const auto& c) { return a.first < c.first; });
+    std::vector<int32_t> rows;
+    std::vector<double> v;
+    for (size_t k = 0; k < all.size(); ++k) {
+        if (!rows.empty() && rows.back() == all[k].first) v.back() = all[k].second;
+        else { rows.push_back(all[k].first); v.push_back(all[k].second); }
+    }
+    return nsfv1_set_dirichlet(h, (int64_t)rows.size(), rows.data(), v.data());
+}
+
+// FV1 boundary faces of one element side (ugcore's boundary faces of the box
+// dual mesh, restated): side corner a owns the part {a, mid(a, next), side centre,
+// mid(prev, a)} (2D: {a, mid(a, other)}); its normal is area-weighted and points
+// out of the element. nrm[j][d] receives the normal of side corner j.
+bool side_bf_normals(int dim, int nco, const double (*x)[3], const double* elemCentre, double (*nrm)[3]) {
+    double sc[3] = {0, 0, 0};
+    for (int j = 0; j < nco; ++j)
+        for (int d = 0; d < 3; ++d) sc[d] += x[j][d] / nco;
+    for (int j = 0; j < nco; ++j) {
+        for (int d = 0; d < 3; ++d) nrm[j][d] = 0.0;
+        if (dim == 2) {
+            const double* a = x[j];
+            const double* o = x[1 - j];
+            const double m[2] = {0.5 * (a[0] + o[0]), 0.5 * (a[1] + o[1])};
+            nrm[j][0] = m[1] - a[1];
+            nrm[j][1] = -(m[0] - a[0]);
+        } else {
+            const double* a = x[j];
+            const double* nx = x[(j + 1) % nco];
+            const double* pv = x[(j + nco - 1) % nco];
+            double mn[3], mp[3], d1[3], d2[3];
+            for (int d = 0; d < 3; ++d) {
+                mn[d] = 0.5 * (a[d] + nx[d]); mp[d] = 0.5 * (pv[d] + a[d]);
+                d1[d] = sc[d] - a[d]; d2[d] = mp[d] - mn[d];
+            }
+            nrm[j][0] = 0.5 * (d1[1] * d2[2] - d1[2] * d2[1]);
+            nrm[j][1] = 0.5 * (d1[2] * d2[0] - d1[0] * d2[2]);
+            nrm[j][2] = 0.5 * (d1[0] * d2[1] - d1[1] * d2[0]);
+        }
+        double dot = 0;
+        for (int d = 0; d < dim; ++d) dot += nrm[j][d] * (sc[d] - elemCentre[d]);
+        if (dot < 0) for (int d = 0; d < 3; ++d) nrm[j][d] = -nrm[j][d];
+        if (!(dot != 0.0)) return false;   // degenerate side (or NaN)
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nsfv1_add_wall(nsfv1_disc* h, int64_t n, const int32_t* nodes) {
+    NSFV1_H;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "NavierStokesWall::add: no mesh"); return D->status; }
+    if (n < 0 || (n > 0 && !nodes)) { D->fail(NSFV1_ERR_ARGUMENT, "NavierStokesWall::add: bad arguments"); return D->status; }
+    const int b = D->dim + 1;
+    std::vector<int32_t> dofs;
+    std::vector<double> vals;
+    for (int64_t k = 0; k < n; ++k) {
+        if (nodes[k] < 0 || nodes[k] >= D->nNodes) { D->fail(NSFV1_ERR_ARGUMENT, "NavierStokesWall::add: node out of range"); return D->status; }
+        for (int d = 0; d < D->dim; ++d) { dofs.push_back(nodes[k] * b + d); vals.push_back(0.0); }
+    }
+    return merge_dirichlet(h, D, dofs, vals);
+}
+
+int nsfv1_add_inflow(nsfv1_disc* h, int64_t n_sides, int side_nco, const int32_t* side_nodes, const double* vel) {
+    NSFV1_H;
+    const int dim = D->dim, b = dim + 1, nsh = D->nsh;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "NavierStokesInflow::add: no mesh"); return D->status; }
+    if (n_sides < 0 || (n_sides > 0 && (!side_nodes || !vel)) || (dim == 2 && side_nco != 2) || (dim == 3 && side_nco != 3 && side_nco != 4)) {
+        D->fail(NSFV1_ERR_ARGUMENT, "NavierStokesInflow::add: sides of 2 (2D) or 3 / 4 (3D) nodes and a velocity of dim components");
+        return D->status;
+    }
+    for (int64_t k = 0; k < n_sides * side_nco; ++k)
+        if (side_nodes[k] < 0 || side_nodes[k] >= D->nNodes) { D->fail(NSFV1_ERR_ARGUMENT, "NavierStokesInflow::add: node out of range"); return D->status; }
+    // node -> incident elements
+    std::vector<int64_t> nptr(D->nNodes + 1, 0);
+    for (int64_t k = 0; k < D->nElems * nsh; ++k) nptr[D->connHost[k] + 1]++;
+    for (int64_t r = 0; r < D->nNodes; ++r) nptr[r + 1] += nptr[r];
+    std::vector<int32_t> nel(nptr[D->nNodes]);
+    {
+        std::vector<int64_t> fill(nptr.begin(), nptr.end() - 1);
+        for (int64_t e = 0; e < D->nElems; ++e)
+            for (int i = 0; i < nsh; ++i) nel[fill[D->connHost[e * nsh + i]]++] = (int32_t)e;
+    }
+    std::vector<double> flux = D->bndFluxHost;
+    flux.resize(D->nNodes, 0.0);
+    std::vector<int32_t> dofs;
+    std::vector<double> vals;
+    for (int64_t sIdx = 0; sIdx < n_sides; ++sIdx) {
+        const int32_t* sn = side_nodes + sIdx * side_nco;
+        // the one element that has every node of the side
+        int64_t owner = -1;
+        int owners = 0;
+        for (int64_t q = nptr[sn[0]]; q < nptr[sn[0] + 1]; ++q) {
+            const int64_t e = nel[q];
+            bool all = true;
+            for (int j = 1; j < side_nco && all; ++j) {
+                bool has = false;
+                for (int i = 0; i < nsh; ++i) has |= D->connHost[e * nsh + i] == sn[j];
+                all = has;
+            }
+            if (all) { owner = e; ++owners; }
+        }
+        if (owners != 1) {
+            D->fail(NSFV1_ERR_ARGUMENT, "NavierStokesInflow::add: side " + std::to_string(sIdx) + " is not a boundary side of exactly one element");
+            return D->status;
+        }
+        double x[4][3] = {{0}}, cen[3] = {0, 0, 0}, nrm[4][3];
+        for (int j = 0; j < side_nco; ++j)
+            for (int d = 0; d < dim; ++d) x[j][d] = D->coordsHost[(size_t)sn[j] * dim + d];
+        for (int i = 0; i < nsh; ++i)
+            for (int d = 0; d < dim; ++d) cen[d] += D->coordsHost[(size_t)D->connHost[owner * nsh + i] * dim + d] / nsh;
+        if (!side_bf_normals(dim, side_nco, x, cen, nrm)) {
+            D->fail(NSFV1_ERR_GEOMETRY, "NavierStokesInflow::add: degenerate side " + std::to_string(sIdx));
+            return D->status;
+        }
+        for (int j = 0; j < side_nco; ++j) {
+            double vn = 0.0;
+            for (int d = 0; d < dim; ++d) vn += vel[d] * nrm[j][d];
+            flux[sn[j]] += vn;
+            for (int d = 0; d < dim; ++d) { dofs.push_back(sn[j] * b + d); vals.push_back(vel[d]); }
+        }
+    }
+    if (!D->cuda_ok(dupload(D->d_bndFlux, flux.data(), flux.size()), "upload inflow flux")) return D->status;
+    D->bndFluxHost.swap(flux);
+    return merge_dirichlet(h, D, dofs, vals);
+}
+
+int nsfv1_clear_boundary(nsfv1_disc* h) {
+    NSFV1_H;
+    dfree(D->d_bndFlux);
+    D->bndFluxHost.clear();
+    dfree(D->d_dirRow);
+    dfree(D->d_dirVal);
+    D->dirRowHost.clear();
+    D->dirValHost.clear();
+    D->nDir = 0;
+    return NSFV1_OK;
+}
+
 int nsfv1_assemble_defect(nsfv1_disc* h, const double* u, const double* u_old, double dt, double* d, void* stream) {
     NSFV1_H;
     return D->assemble_defect(u, u_old, dt, d, (cudaStream_t)stream) ? NSFV1_OK : D->status;
@@ -606,6 +757,7 @@ bool Disc::assemble_defect(const double* u, const double* u_old, double dt, doub
                   d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive};
         if (!cuda_ok(launch_defect(roid, P, a, s, asmThreads), "defect kernel")) return false;
     }
+    if (!cuda_ok(launch_bnd_flux(b, nNodes, u_old ? dt : 1.0, d_bndFlux, d, s), "inflow flux")) return false;
     if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, d, nullptr, 0, s), "dirichlet")) return false;
     return check_err_word(s);
 }
@@ -627,6 +779,7 @@ bool Disc::assemble_defect_jacobian(const double* u, const double* u_old, double
                   d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive};
         if (!cuda_ok(launch_defect_jacobian(roid, P, a, prec, s, asmThreads), "defect+jacobian kernel")) return false;
     }
+    if (!cuda_ok(launch_bnd_flux(b, nNodes, u_old ? dt : 1.0, d_bndFlux, d, s), "inflow flux")) return false;
     if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, d, vals, prec, s), "dirichlet")) return false;
     return check_err_word(s);
 }

@@ -56,6 +56,9 @@ struct Disc {
     std::vector<double> coordsHost, nuElemHost, dirValHost;
     std::vector<int32_t> connHost, dirRowHost;
     std::vector<int32_t> instCells;          // cells per side of each structured instance (nsfv1_set_instance_grids)
+    // continuity-row flux of inflow boundaries (nsfv1_add_inflow), per node; added to the defect
+    std::vector<double> bndFluxHost;
+    double* d_bndFlux = nullptr;
     double* d_bjDinv = nullptr;     // nsfv1_block_jacobi scratch: inverted diagonal blocks
     int32_t* d_dirRow = nullptr;
     double* d_dirVal = nullptr;

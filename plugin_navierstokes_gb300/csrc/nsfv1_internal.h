@@ -42,6 +42,8 @@ cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int
 // state) at the same state, one launch per colour
 cudaError_t launch_defect_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s, int threads = 128);
 cudaError_t launch_elem_batch(int roid, const DiscParams& P, const ElemBatchArgs& a, cudaStream_t s);
+// D[node * b + b - 1] += scale * flux[node] (the inflow boundaries' continuity flux)
+cudaError_t launch_bnd_flux(int b, int64_t nNodes, double scale, const double* flux, double* D, cudaStream_t s);
 cudaError_t launch_dirichlet(int b, int64_t n, const int32_t* rows, const double* vals, const int32_t* rowPtr,
                              const int32_t* colIdx, const double* U, double* D, void* J, int prec, cudaStream_t s);
 

@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from ._capi import HEXAHEDRON, QUADRILATERAL, TRIANGLE
+from ._capi import HEXAHEDRON, QUADRILATERAL, TETRAHEDRON, TRIANGLE
 
 _GOLDEN = np.uint64(0x9E3779B97F4A7C15)
 
@@ -163,3 +163,30 @@ def cavity_batch(sizes, Re, lid):
     return {"elem_type": QUADRILATERAL, "coords": np.concatenate(coords), "conn": np.concatenate(conns).astype(np.int32),
             "node_offsets": np.array(offs, np.int32), "nu_elem": np.concatenate(nus),
             "dofs": np.concatenate(dofs).astype(np.int32), "values": np.concatenate(vals)}
+
+
+# element sides in ugcore's reference order (corner ids of each side)
+_SIDES = {
+    TRIANGLE: [[0, 1], [1, 2], [2, 0]],
+    QUADRILATERAL: [[0, 1], [1, 2], [2, 3], [3, 0]],
+    TETRAHEDRON: [[0, 2, 1], [0, 1, 3], [1, 2, 3], [0, 3, 2]],
+    HEXAHEDRON: [[0, 3, 2, 1], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [0, 4, 7, 3], [4, 5, 6, 7]],
+}
+
+
+def boundary_sides(elem_type: int, coords: np.ndarray, conn: np.ndarray, axis: int, value: float, tol: float = 1e-12) -> np.ndarray:
+    """Node lists of the element sides that lie on the plane coords[:, axis] == value
+    (corners in the element's side order), e.g. the inflow boundary of a channel
+    for NavierStokesInflowFV1.add."""
+    out = []
+    on = np.abs(coords[:, axis] - value) <= tol
+    for s in _SIDES[elem_type]:
+        nodes = conn[:, s]
+        hit = np.all(on[nodes], axis=1)
+        out.append(nodes[hit])
+    return np.concatenate(out).astype(np.int32) if out else np.zeros((0, len(_SIDES[elem_type][0])), np.int32)
+
+
+def boundary_nodes(coords: np.ndarray, axis: int, value: float, tol: float = 1e-12) -> np.ndarray:
+    """Ids of the nodes on the plane coords[:, axis] == value."""
+    return np.nonzero(np.abs(coords[:, axis] - value) <= tol)[0].astype(np.int32)

@@ -137,6 +137,10 @@ class NavierStokesFV1:
         values = np.ascontiguousarray(values, dtype=np.float64)
         self._c(self._lib.nsfv1_set_dirichlet(self._h, dofs.size, dofs.ctypes.data, values.ctypes.data))
 
+    def clear_boundary(self) -> None:
+        """Removes every Dirichlet row and inflow flux (nsfv1_clear_boundary)."""
+        self._c(self._lib.nsfv1_clear_boundary(self._h))
+
     # ---- assembly (torch CUDA tensors) ----------------------------------------
     def assemble_defect(self, u, d, u_old=None, dt: float = 0.0, stream=None) -> None:
         self._c(self._lib.nsfv1_assemble_defect(self._h, _ptr(u), _ptr(u_old), float(dt), _ptr(d), _stream_ptr(stream)))
@@ -295,3 +299,36 @@ def mesh_pattern(elem_type: int, n_nodes: int, conn: np.ndarray):
     if st != _capi.OK:
         raise NSFV1Error(st, "nsfv1_mesh_pattern failed")
     return rp, ci, col, nc.value
+
+
+class NavierStokesWall:
+    """``NavierStokesWall(master)`` (incompressible/bnd/wall.h, wall_impl.h:44-69):
+    ``add(nodes)`` makes every velocity component of the nodes a zero Dirichlet row.
+    The reference's ``add(subsets)`` takes subset names of ugcore's grid; here the
+    caller passes the node ids of those subsets (nsfv1_add_wall)."""
+
+    def __init__(self, master: NavierStokesFV1):
+        self.master = master
+
+    def add(self, nodes) -> None:
+        a = np.ascontiguousarray(nodes, dtype=np.int32)
+        self.master._c(self.master._lib.nsfv1_add_wall(self.master._h, a.size, a.ctypes.data))
+
+
+class NavierStokesInflowFV1:
+    """``NavierStokesInflowFV1(master)`` (incompressible/fv1/bnd/inflow_fv1.h,
+    inflow_fv1_impl.h:42-82): ``add(velocity, sides)`` sets Dirichlet velocity rows
+    on the nodes of the boundary sides and the continuity equation's Neumann flux
+    vel . n over each corner's part of the sides (nsfv1_add_inflow). ``sides`` is
+    an (n_sides, nodes per side) array of node ids (edges in 2D; triangles or
+    quadrilaterals in 3D) standing for the reference's boundary subset names."""
+
+    def __init__(self, master: NavierStokesFV1):
+        self.master = master
+
+    def add(self, velocity, sides) -> None:
+        v = np.ascontiguousarray(np.asarray(velocity, dtype=np.float64).ravel())
+        sd = np.ascontiguousarray(np.atleast_2d(np.asarray(sides, dtype=np.int32)))
+        if v.size != self.master.dim:
+            raise NSFV1Error(_capi.ERR_ARGUMENT, "NavierStokesInflow::add: the velocity needs dim components")
+        self.master._c(self.master._lib.nsfv1_add_inflow(self.master._h, sd.shape[0], sd.shape[1], sd.ctypes.data, v.ctypes.data))

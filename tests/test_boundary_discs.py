@@ -1,0 +1,130 @@
+"""Boundary-condition element discs: NavierStokesWall (zero-velocity Dirichlet
+rows, incompressible/bnd/wall_impl.h:57-69) and NavierStokesInflowFV1
+(Dirichlet inflow velocity + the continuity equation's Neumann flux vel . n over
+each boundary corner's dual face, incompressible/fv1/bnd/inflow_fv1_impl.h:57-82).
+
+CPU: the oracle's inflow flux integrates to vel . n over the inflow boundary,
+in 2D and 3D, and interior sides are refused. GPU: defect and Jacobian of a
+channel (walls, inflow, natural outflow) match the oracle to 1e-12, stationary
+and implicit Euler, and a Newton solve of the channel meets the oracle defect.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from _cases import rel_err
+from plugin_navierstokes_gb300 import NavierStokesFV1, NavierStokesInflowFV1, NavierStokesWall, NSFV1Error, mesh
+
+
+def _channel(dim, n):
+    if dim == 2:
+        roid, X, C = mesh.structured_quads(n)
+        X = X * np.array([2.0, 1.0])
+    else:
+        roid, X, C = mesh.structured_hexes(n)
+        X = X * np.array([2.0, 1.0, 1.0])
+    inflow = mesh.boundary_sides(roid, X, C, 0, 0.0)
+    walls = np.unique(np.concatenate([mesh.boundary_nodes(X, a, v) for a in range(1, dim) for v in (0.0, 1.0)]))
+    return roid, X, C, inflow, walls
+
+
+def _setup(disc, dim, roid, X, C, inflow, walls, vel):
+    disc.set_kinematic_viscosity(0.02)
+    disc.set_upwind("lps" if dim == 3 else "full")
+    disc.set_stabilization("flow" if dim == 3 else "fields")
+    disc.set_mesh(roid, X, C)
+    if isinstance(disc, oracle.Oracle):
+        disc.add_wall(walls)
+        disc.add_inflow(vel, inflow)
+    else:
+        NavierStokesWall(disc).add(walls)
+        NavierStokesInflowFV1(disc).add(vel, inflow)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_inflow_flux_integrates_to_the_inflow(dim):
+    roid, X, C, inflow, walls = _channel(dim, 6)
+    o = oracle.Oracle(dim)
+    vel = [1.5] + [0.0] * (dim - 1)
+    _setup(o, dim, roid, X, C, inflow, walls, vel)
+    U = np.zeros(X.shape[0] * (dim + 1))
+    D, _ = o.assemble(U, jacobian=False)
+    D = D.reshape(-1, dim + 1)
+    # at rest only the inflow flux drives the continuity rows; its sum is vel . n over x = 0 (area 1)
+    in_nodes = np.unique(inflow)
+    assert abs(D[:, dim].sum() - (-1.5)) < 1e-13
+    assert np.all(D[np.setdiff1d(np.arange(X.shape[0]), in_nodes), dim] == 0.0)
+    # Dirichlet velocity rows: u - g on the inflow (the wall corners are later inflow rows: inflow wins)
+    assert np.allclose(D[in_nodes, 0], -1.5)
+
+
+def test_oracle_refuses_interior_sides():
+    roid, X, C, inflow, walls = _channel(2, 4)
+    o = oracle.Oracle(2)
+    o.set_kinematic_viscosity(0.01); o.set_upwind("full"); o.set_stabilization("fields"); o.set_mesh(roid, X, C)
+    interior = np.array([[C[0, 1], C[0, 2]]])   # the side shared by elements 0 and 1
+    with pytest.raises(RuntimeError):
+        o.add_inflow([1.0, 0.0], interior)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("transient", [False, True])
+def test_channel_defect_and_jacobian_match_the_oracle(cuda, dim, transient):
+    import torch
+    roid, X, C, inflow, walls = _channel(dim, 8 if dim == 2 else 5)
+    vel = [1.0, 0.25, -0.1][:dim]
+    b = dim + 1
+    d = NavierStokesFV1(dim=dim)
+    o = oracle.Oracle(dim)
+    for disc in (d, o):
+        _setup(disc, dim, roid, X, C, inflow, walls, vel)
+    U = (mesh.uniform(17, X.shape[0] * b) * 2 - 1)
+    Uo = U * 0.7 if transient else None
+    dt = 0.05 if transient else 0.0
+    Dref, Jref = o.assemble(U, Uo, dt)
+    tu = torch.tensor(U, dtype=torch.float64, device=cuda)
+    tuo = None if Uo is None else torch.tensor(Uo, dtype=torch.float64, device=cuda)
+    D = torch.empty_like(tu)
+    J = torch.empty(Jref.size, dtype=torch.float64, device=cuda)
+    d.assemble_defect_jacobian(tu, D, J, tuo, dt)
+    torch.cuda.synchronize()
+    assert rel_err(D.cpu().numpy(), Dref) <= 1e-12
+    assert rel_err(J.cpu().numpy(), Jref) <= 1e-12
+    d.assemble_defect(tu, D, tuo, dt)
+    torch.cuda.synchronize()
+    assert rel_err(D.cpu().numpy(), Dref) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_channel_newton_meets_the_oracle_defect(cuda):
+    import torch
+    roid, X, C, inflow, walls = _channel(2, 16)
+    d = NavierStokesFV1(dim=2)
+    o = oracle.Oracle(2)
+    for disc in (d, o):
+        _setup(disc, 2, roid, X, C, inflow, walls, [1.0, 0.0])
+    u = torch.zeros(X.shape[0] * 3, dtype=torch.float64, device=cuda)
+    r = d.newton_solve(u, rtol=1e-8, lin_rtol=1e-4, lin_max_iter=5000)
+    Dn, _ = o.assemble(u.cpu().numpy(), jacobian=False)
+    assert r["status"] == 0 and np.linalg.norm(Dn) <= 1.01e-8 * r["initial_defect"], r
+    # mass balance: the outflow through x = 2 carries what the inflow brings in (natural outflow)
+    U = u.cpu().numpy().reshape(-1, 3)
+    right = mesh.boundary_nodes(X, 0, 2.0)
+    ys = X[right, 1]
+    order = np.argsort(ys)
+    q_out = np.trapezoid(U[right[order], 0], ys[order])
+    assert abs(q_out - 1.0) < 0.05
+
+
+@pytest.mark.gpu
+def test_inflow_rejects_interior_sides_and_bad_sizes(cuda):
+    roid, X, C, inflow, walls = _channel(2, 4)
+    d = NavierStokesFV1(dim=2)
+    d.set_kinematic_viscosity(0.01); d.set_upwind("full"); d.set_stabilization("fields"); d.set_mesh(roid, X, C)
+    with pytest.raises(NSFV1Error):
+        NavierStokesInflowFV1(d).add([1.0, 0.0], np.array([[C[0, 1], C[0, 2]]]))
+    with pytest.raises(NSFV1Error):
+        NavierStokesInflowFV1(d).add([1.0, 0.0, 0.0], inflow)
+    with pytest.raises(NSFV1Error):
+        NavierStokesWall(d).add([X.shape[0] + 3])
