@@ -89,6 +89,16 @@ int nsfv1_set_upwind(nsfv1_disc* h, const char* name);
  * stabilization.cpp:86-100): "fields", "flow" (+ "without" for
  * NavierStokesFV1WithoutStabilization); diff_length "raw" (NULL), "fivepoint", "cor". */
 int nsfv1_set_stabilization(nsfv1_disc* h, const char* name, const char* diff_length);
+/* NavierStokesFV1::set_pac_upwind(bool) (navier_stokes_fv1.h:217-225): with on != 0
+ * the stabilisation takes the convection's upwind object and its stabilised
+ * velocity becomes the convective upwind velocity (PAC), in the defect and in
+ * the Jacobian (navier_stokes_fv1.cpp:382-384, 398-427, 477-518); needs an
+ * upwind and a stabilisation set before (NSFV1_ERR_STATE with the reference's
+ * texts otherwise). on == 0 changes nothing, as in the reference; a later
+ * nsfv1_set_upwind ends PAC. (The reference's convection keeps its old
+ * stabilisation object if set_stabilization follows; here PAC uses the current
+ * stabilisation.) */
+int nsfv1_set_pac_upwind(nsfv1_disc* h, int on);
 /* INavierStokesFV1Stabilization::set_upwind with an upwind object of its own
  * (stabilization.h:91-95, registered at register_fv1.cpp:246-249). */
 int nsfv1_set_stabilization_upwind(nsfv1_disc* h, const char* name);

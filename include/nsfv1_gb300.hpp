@@ -90,6 +90,7 @@ class NavierStokesFV1 {
         check(nsfv1_set_stabilization(m_h, name.c_str(), diffLength.c_str()));
     }
     void set_stabilization_upwind(const std::string& name) { check(nsfv1_set_stabilization_upwind(m_h, name.c_str())); }
+    void set_pac_upwind(bool on) { check(nsfv1_set_pac_upwind(m_h, on ? 1 : 0)); }
 
     /* ---- per-element callbacks (navier_stokes_fv1.h:254-281) --------------- */
     /* checks of prep_elem_loop (navier_stokes_fv1.cpp:136-199) for element type roid */

@@ -43,6 +43,7 @@ def load():
             "ora_set_peclet_blend": (c_int, [c_void_p, c_int]), "ora_set_upwind": (c_int, [c_void_p, c_char_p]),
             "ora_set_stabilization": (c_int, [c_void_p, c_char_p, c_char_p]),
             "ora_set_stabilization_upwind": (c_int, [c_void_p, c_char_p]),
+            "ora_set_pac_upwind": (c_int, [c_void_p, c_int]),
             "ora_geometry": (c_int, [c_int, c_void_p, c_void_p]),
             "ora_ref_tables": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
             "ora_elem_batch": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
@@ -99,6 +100,7 @@ class Oracle:
     def set_peclet_blend(self, v): self._c(self.lib.ora_set_peclet_blend(self.h, int(bool(v))))
     def set_upwind(self, n): self._c(self.lib.ora_set_upwind(self.h, n.encode()))
     def set_stabilization_upwind(self, n): self._c(self.lib.ora_set_stabilization_upwind(self.h, n.encode()))
+    def set_pac_upwind(self, on): self._c(self.lib.ora_set_pac_upwind(self.h, int(bool(on))))
 
     def set_source(self, f):
         a = np.ascontiguousarray(f, dtype=np.float64)

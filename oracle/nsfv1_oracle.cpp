@@ -731,11 +731,25 @@ struct Disc {
     bool convUpwindSet = false;
     Upwind ownStabUpwind;          // used when the stabilisation's upwind differs from the convection upwind
     bool stabHasOwnUpwind = false;
+    bool pac = false;              // the stabilisation is the convective upwind (set_pac_upwind)
 
     explicit Disc(int d) : dim(d) {}
 
+    // set_pac_upwind(true) (navier_stokes_fv1.h:217-225): the stabilisation takes the
+    // convection's upwind object and becomes the convective upwind itself
+    // (m_spConvStab = m_spStab, m_spConvUpwind = SPNULL); false changes nothing
+    void set_pac_upwind(bool on) {
+        if (!on) return;
+        if (!convUpwindSet) throw std::runtime_error("Upwind must be specified previously.");
+        if (!stabSet) throw std::runtime_error("Stabilization must be specified previously.");
+        stab.upwind = &convUpwind;
+        stabHasOwnUpwind = false;
+        pac = true;
+    }
+
     // set_upwind(name) (navier_stokes_fv1.h:213-215); upwind shared with the stabilisation
     void set_upwind(int t) {
+        pac = false;   // set_upwind(name) clears m_spConvStab
         // a new upwind object: a stabilisation that shared the previous one keeps it
         if (stab.upwind == &convUpwind) { ownStabUpwind = convUpwind; stabHasOwnUpwind = true; stab.upwind = &ownStabUpwind; }
         convUpwind.type = t; convUpwindSet = true;
@@ -817,7 +831,9 @@ struct Disc {
             }
             if (!bStokes) {
                 number UpwindVel[3];
-                convUpwind.upwind_vel(geo, ip, u, UpwindVel);
+                // PAC: the stabilised velocity is the upwind velocity (navier_stokes_fv1.cpp:707-712)
+                if (pac) for (int d = 0; d < 3; ++d) UpwindVel[d] = stab.stabVel[ip][d];
+                else convUpwind.upwind_vel(geo, ip, u, UpwindVel);
                 if (bPecletBlend) peclet_blend(UpwindVel, geo, ip, StdVel[ip], nu);
                 number prod = 0;
                 for (int d = 0; d < dim; ++d) prod += StdVel[ip][d] * scvf.normal[d];
@@ -874,21 +890,66 @@ struct Disc {
                 // convection (:377-552)
                 if (!bStokes) {
                     number UpwindVel[3];
-                    convUpwind.upwind_vel(geo, ip, u, UpwindVel);
+                    if (pac) for (int d = 0; d < 3; ++d) UpwindVel[d] = stab.stabVel[ip][d];
+                    else convUpwind.upwind_vel(geo, ip, u, UpwindVel);
                     number w = 1.0;
                     if (bPecletBlend) w = peclet_blend(UpwindVel, geo, ip, StdVel[ip], nu);
                     number prod = 0;
                     for (int d = 0; d < dim; ++d) prod += StdVel[ip][d] * scvf.normal[d];
                     prod *= rho;
-                    number convFlux_vel = convUpwind.upShapeSh[ip][sh];
-                    convFlux_vel *= prod * w;
-                    for (int d1 = 0; d1 < dim; ++d1) { Jx(d1, from, d1, sh) += convFlux_vel; Jx(d1, to, d1, sh) -= convFlux_vel; }
+                    if (pac) {
+                        // stabilisation used as upwind, fixpoint part (:398-427)
+                        if (stab.vel_comp_connected())
+                            for (int d1 = 0; d1 < dim; ++d1)
+                                for (int d2 = 0; d2 < dim; ++d2) {
+                                    const number cf = prod * w * stab.stabShapeVel[ip][d1][d2][sh];
+                                    Jx(d1, from, d2, sh) += cf;
+                                    Jx(d1, to, d2, sh) -= cf;
+                                }
+                        else
+                            for (int d1 = 0; d1 < dim; ++d1) {
+                                const number cf = prod * w * stab.stabShapeVel[ip][d1][d1][sh];
+                                Jx(d1, from, d1, sh) += cf;
+                                Jx(d1, to, d1, sh) -= cf;
+                            }
+                        for (int d1 = 0; d1 < dim; ++d1) {
+                            const number cfp = prod * w * stab.stabShapeP[ip][d1][sh];
+                            Jx(d1, from, P, sh) += cfp;
+                            Jx(d1, to, P, sh) -= cfp;
+                        }
+                    } else {
+                        number convFlux_vel = convUpwind.upShapeSh[ip][sh];
+                        convFlux_vel *= prod * w;
+                        for (int d1 = 0; d1 < dim; ++d1) { Jx(d1, from, d1, sh) += convFlux_vel; Jx(d1, to, d1, sh) -= convFlux_vel; }
+                    }
                     if (bPecletBlend) {
                         const number convFluxPe = prod * (1.0 - w) * scvf.shape[sh];
                         for (int d1 = 0; d1 < dim; ++d1) { Jx(d1, from, d1, sh) += convFluxPe; Jx(d1, to, d1, sh) -= convFluxPe; }
                     }
+                    if (fullNewtonFactor != 0.0 && pac) {
+                        // stabilisation used as upwind (:477-518): the non-connected branch takes the
+                        // (d1, d1) shape for every column d2 and no blending weight, as the reference does
+                        for (int d1 = 0; d1 < dim; ++d1) {
+                            for (int d2 = 0; d2 < dim; ++d2) {
+                                number prod_vel = 0.0;
+                                if (stab.vel_comp_connected())
+                                    for (int k = 0; k < dim; ++k) prod_vel += w * stab.stabShapeVel[ip][k][d2][sh] * scvf.normal[k];
+                                else
+                                    prod_vel = stab.stabShapeVel[ip][d1][d1][sh] * scvf.normal[d1];
+                                prod_vel *= fullNewtonFactor * rho;
+                                Jx(d1, from, d2, sh) += prod_vel * UpwindVel[d1];
+                                Jx(d1, to, d2, sh) -= prod_vel * UpwindVel[d1];
+                            }
+                            number prod_p = 0.0;
+                            for (int k = 0; k < dim; ++k) prod_p += stab.stabShapeP[ip][k][sh] * scvf.normal[k];
+                            prod_p *= fullNewtonFactor * rho;
+                            Jx(d1, from, P, sh) += prod_p * UpwindVel[d1];
+                            Jx(d1, to, P, sh) -= prod_p * UpwindVel[d1];
+                        }
+                    }
                     if (fullNewtonFactor != 0.0) {
                         // upwind branch (:521-534): the factor itself is not applied here
+                        if (!pac)
                         for (int d1 = 0; d1 < dim; ++d1)
                             for (int d2 = 0; d2 < dim; ++d2) {
                                 const number prod_vel = w * convUpwind.upShapeSh[ip][sh] * scvf.normal[d2] * rho;
@@ -1367,6 +1428,11 @@ int ora_set_stabilization(void* h, const char* name, const char* diffLength) {
     const int dl = diffLength ? ora_difflen_id(diffLength) : DL_RAW;
     if (t < 0 || dl < 0) return 1;
     static_cast<Problem*>(h)->disc.set_stabilization(t, dl);
+    return 0;
+}
+int ora_set_pac_upwind(void* h, int on) {
+    auto* P = static_cast<Problem*>(h);
+    try { P->disc.set_pac_upwind(on != 0); } catch (std::exception& e) { P->lastError = e.what(); return 1; }
     return 0;
 }
 int ora_set_stabilization_upwind(void* h, const char* name) {

@@ -99,6 +99,7 @@ _SIGS = {
     "nsfv1_set_upwind": (c_int, [c_void_p, c_char_p]),
     "nsfv1_set_stabilization": (c_int, [c_void_p, c_char_p, c_char_p]),
     "nsfv1_set_stabilization_upwind": (c_int, [c_void_p, c_char_p]),
+    "nsfv1_set_pac_upwind": (c_int, [c_void_p, c_int]),
     "nsfv1_set_mesh": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_int64, c_void_p]),
     "nsfv1_pattern_info": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int), POINTER(c_int)]),
     "nsfv1_mesh_pattern": (c_int, [c_int, c_int64, c_int64, c_void_p, POINTER(c_int64), POINTER(c_int), c_void_p, c_void_p, c_void_p]),

@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kThreads) k_defect(const DiscParams P, const A
     }
 }
 
-template <int ROID, typename T, typename VT>
+template <int ROID, typename T, typename VT, bool PAC>
 __global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const AsmArgs A) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, b = R::b;
@@ -201,9 +201,25 @@ __global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const
     elem_setup<ROID, T>(E);
     T u[b][nsh];
     load_u<ROID, T>(A.U, nodes, u);
+    // the old-time state enters the Jacobian only through the stabilised velocity of
+    // the exact-Jacobian PAC terms
+    T uo[dim][nsh];
+    if (PAC && P.transient && P.pac && P.fullNewton != 0.0) {
+        T t4[b][nsh];
+        load_u<ROID, T>(A.Uold, nodes, t4);
+#pragma unroll
+        for (int d = 0; d < dim; ++d)
+#pragma unroll
+            for (int k = 0; k < nsh; ++k) uo[d][k] = t4[d][k];
+    } else {
+#pragma unroll
+        for (int d = 0; d < dim; ++d)
+#pragma unroll
+            for (int k = 0; k < nsh; ++k) uo[d][k] = T(0);
+    }
     GlobalJacSink<VT, nsh> sink{reinterpret_cast<VT*>(A.vals), A.elemBlk + (int64_t)e * nsh * nsh};
     const T scale = P.transient ? (T)P.dt : T(1);
-    if (!elem_jac_A<ROID, T>(P, E, u, scale, sink, nuEl)) atomicOr(A.err, 1);
+    if (!elem_jac_A<ROID, T, PAC>(P, E, u, uo, scale, sink, nuEl)) atomicOr(A.err, 1);
     if (P.transient) {
         // mass part: J(d, sh, d, sh) += |SCV| rho
 #pragma unroll
@@ -218,7 +234,7 @@ __global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const
 // Defect and FP64 Jacobian at the same state in one pass over the elements of a
 // colour (one launch per colour instead of two): the per-SCVF geometry, upwinds
 // and stabilisation are evaluated once for both outputs.
-template <int ROID, bool TRANSIENT, typename VT>
+template <int ROID, bool TRANSIENT, typename VT, bool PAC>
 __global__ void __launch_bounds__(kThreads) k_defect_jacobian(const DiscParams P, const AsmArgs A) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, b = R::b;
@@ -256,11 +272,11 @@ __global__ void __launch_bounds__(kThreads) k_defect_jacobian(const DiscParams P
     const double* uoPtr = TRANSIENT ? &uo[0][0] : &u[0][0];
     const double(&uoRef)[dim][nsh] = *reinterpret_cast<const double(*)[dim][nsh]>(uoPtr);
     if constexpr (std::is_same<VT, double>::value) {
-        if constexpr (TRANSIENT) ok = elem_def_jac_A<ROID, double>(Q, E, u, uoRef, ss, P.dt, jsink, nuEl);
-        else ok = elem_def_jac_A<ROID, double>(Q, E, u, uoRef, sink, 1.0, jsink, nuEl);
+        if constexpr (TRANSIENT) ok = elem_def_jac_A<ROID, double, PAC>(Q, E, u, uoRef, ss, P.dt, jsink, nuEl);
+        else ok = elem_def_jac_A<ROID, double, PAC>(Q, E, u, uoRef, sink, 1.0, jsink, nuEl);
     } else {
-        if constexpr (TRANSIENT) ok = elem_def_jac_A_mixed<ROID>(Q, E, u, uoRef, ss, (float)P.dt, jsink, nuEl);
-        else ok = elem_def_jac_A_mixed<ROID>(Q, E, u, uoRef, sink, 1.0f, jsink, nuEl);
+        if constexpr (TRANSIENT) ok = elem_def_jac_A_mixed<ROID, PAC>(Q, E, u, uoRef, ss, (float)P.dt, jsink, nuEl);
+        else ok = elem_def_jac_A_mixed<ROID, PAC>(Q, E, u, uoRef, sink, 1.0f, jsink, nuEl);
     }
     if (!ok) atomicOr(A.err, 1);
     // mass (implicit Euler) and source parts, per SCV: defect as in k_defect, Jacobian as in k_jacobian
@@ -324,7 +340,10 @@ __global__ void __launch_bounds__(kThreads) k_elem_batch(const DiscParams P, con
         double* J = A.jacA + e * n * n;
         for (int q = 0; q < n * n; ++q) J[q] = 0.0;
         LocalJacSink<nsh> sink{J};
-        if (!elem_jac_A<ROID, double>(Q, E, u, 1.0, sink, P.nu)) atomicOr(A.err, 1);
+        const double(&uoRef)[dim][nsh] = reinterpret_cast<const double(&)[dim][nsh]>(uo);
+        const bool ok = P.pac ? elem_jac_A<ROID, double, true>(Q, E, u, uoRef, 1.0, sink, P.nu)
+                              : elem_jac_A<ROID, double, false>(Q, E, u, uoRef, 1.0, sink, P.nu);
+        if (!ok) atomicOr(A.err, 1);
     }
     if (A.defM) {
         for (int q = 0; q < n; ++q) A.defM[e * n + q] = 0.0;
@@ -415,8 +434,13 @@ cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int
     const int grid = (a.count + t - 1) / t;
     return dispatch_roid(roid, [&](auto r) {
         constexpr int RO = decltype(r)::value;
-        if (prec == 0) k_jacobian<RO, double, double><<<grid, t, 0, s>>>(P, a);
-        else k_jacobian<RO, float, float><<<grid, t, 0, s>>>(P, a);
+        if (P.pac && !P.stokes) {
+            if (prec == 0) k_jacobian<RO, double, double, true><<<grid, t, 0, s>>>(P, a);
+            else k_jacobian<RO, float, float, true><<<grid, t, 0, s>>>(P, a);
+        } else {
+            if (prec == 0) k_jacobian<RO, double, double, false><<<grid, t, 0, s>>>(P, a);
+            else k_jacobian<RO, float, float, false><<<grid, t, 0, s>>>(P, a);
+        }
     });
 }
 
@@ -426,12 +450,23 @@ cudaError_t launch_defect_jacobian(int roid, const DiscParams& P, const AsmArgs&
     const int grid = (a.count + t - 1) / t;
     return dispatch_roid(roid, [&](auto r) {
         constexpr int RO = decltype(r)::value;
+        const bool pac = P.pac && !P.stokes;
         if (prec == 0) {
-            if (P.transient) k_defect_jacobian<RO, true, double><<<grid, t, 0, s>>>(P, a);
-            else k_defect_jacobian<RO, false, double><<<grid, t, 0, s>>>(P, a);
+            if (P.transient) {
+                if (pac) k_defect_jacobian<RO, true, double, true><<<grid, t, 0, s>>>(P, a);
+                else k_defect_jacobian<RO, true, double, false><<<grid, t, 0, s>>>(P, a);
+            } else {
+                if (pac) k_defect_jacobian<RO, false, double, true><<<grid, t, 0, s>>>(P, a);
+                else k_defect_jacobian<RO, false, double, false><<<grid, t, 0, s>>>(P, a);
+            }
         } else {
-            if (P.transient) k_defect_jacobian<RO, true, float><<<grid, t, 0, s>>>(P, a);
-            else k_defect_jacobian<RO, false, float><<<grid, t, 0, s>>>(P, a);
+            if (P.transient) {
+                if (pac) k_defect_jacobian<RO, true, float, true><<<grid, t, 0, s>>>(P, a);
+                else k_defect_jacobian<RO, true, float, false><<<grid, t, 0, s>>>(P, a);
+            } else {
+                if (pac) k_defect_jacobian<RO, false, float, true><<<grid, t, 0, s>>>(P, a);
+                else k_defect_jacobian<RO, false, float, false><<<grid, t, 0, s>>>(P, a);
+            }
         }
     });
 }

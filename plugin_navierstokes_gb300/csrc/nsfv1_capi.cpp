@@ -105,6 +105,7 @@ bool Disc::params(DiscParams& P, bool transient, double dt) {
     P.sameUpwind = stabSharesConv ? 1 : 0;
     P.stab = stabType; P.diffLen = diffLen;
     P.stokes = stokes; P.laplace = laplace; P.peclet = peclet; P.hasSource = hasSource; P.transient = transient ? 1 : 0;
+    P.pac = pac ? 1 : 0;
     return true;
 }
 
@@ -267,6 +268,7 @@ int nsfv1_set_upwind(nsfv1_disc* h, const char* name) {
                 "' not found. Options are: no, full, skewed, LinearProfileSkewed (lps)");
         return D->status;
     }
+    D->pac = false;   // set_upwind(name) clears the stabilisation-as-upwind (m_spConvStab = SPNULL)
     // navier_stokes_fv1.h:213-215: a new upwind object for the convection; a
     // stabilisation without an upwind gets this object, one that already has an
     // upwind keeps its (possibly previously shared) object and type
@@ -293,6 +295,19 @@ int nsfv1_set_stabilization(nsfv1_disc* h, const char* name, const char* diff_le
     // a new stabilisation object: it takes the convection upwind if one is set (navier_stokes_fv1.h:192,199)
     if (D->convUpwindSet) { D->stabUpwindType = D->convUpwindType; D->stabSharesConv = true; }
     else { D->stabUpwindType = -1; D->stabSharesConv = false; }
+    return NSFV1_OK;
+}
+
+int nsfv1_set_pac_upwind(nsfv1_disc* h, int on) {
+    NSFV1_H;
+    if (!on) return NSFV1_OK;   // the reference's set_pac_upwind(false) changes nothing
+    if (!D->convUpwindSet) { D->fail(NSFV1_ERR_STATE, "Upwind must be specified previously.\n"); return D->status; }
+    if (!D->stabSet) { D->fail(NSFV1_ERR_STATE, "Stabilization must be specified previously.\n"); return D->status; }
+    // navier_stokes_fv1.h:217-225: the stabilisation takes the convection upwind object and
+    // becomes the convective upwind
+    D->stabUpwindType = D->convUpwindType;
+    D->stabSharesConv = true;
+    D->pac = true;
     return NSFV1_OK;
 }
 

@@ -778,6 +778,91 @@ __device__ __forceinline__ T peclet_blend(const IpGeo<T>& G, const T* StdVel, T 
 // uo is read only when P.transient (pass any array otherwise).
 // Returns false if an upwind ray found no side.
 // ---------------------------------------------------------------------------
+// velocity and pressure gradients at the integration point of SCVF ip: local
+// gradients first, then one J^-T (grad_k = J^-T lgrad_k, so
+// sum_k u_k grad_k = J^-T sum_k u_k lgrad_k)
+template <int ROID, typename T>
+__device__ __forceinline__ void ip_gradients(const IpGeo<T>& G, const int ip, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
+                                             T (&gradVel)[3][3], T (&gradP)[3]) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh;
+    const auto& tb = tab<ROID, T>();
+    T gl[4][3];
+#pragma unroll
+    for (int f = 0; f <= dim; ++f)
+#pragma unroll
+        for (int c = 0; c < dim; ++c) {
+            T acc = T(0);
+#pragma unroll
+            for (int sh = 0; sh < nsh; ++sh) acc += u[f][sh] * T(tb.ipLGrad[ip][sh][c]);
+            gl[f][c] = acc;
+        }
+#pragma unroll
+    for (int f = 0; f <= dim; ++f)
+#pragma unroll
+        for (int d2 = 0; d2 < dim; ++d2) {
+            T acc = T(0);
+#pragma unroll
+            for (int c = 0; c < dim; ++c) acc += G.JtInv[d2][c] * gl[f][c];
+            if (f < dim) gradVel[f][d2] = acc;
+            else gradP[d2] = acc;
+        }
+}
+
+// The stabilised velocity of SCVF ip (stab_vel of the diagonal FIELDS / FLOW
+// update, stabilization.cpp:163-241, 486-588; the interpolated velocity without
+// stabilisation, :805-850). upShared: the stabilisation's upwind velocity
+// sum_k upS_k u_k when already known (the convection shares the upwind), else null.
+template <int ROID, typename T>
+__device__ __forceinline__ void stab_velocity(const DiscParams& P, const IpState<ROID, T>& S, const int ip,
+                                              const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh], const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh],
+                                              const T (&gradVel)[3][3], const T (&gradP)[3], const T rho, const T* upShared,
+                                              T (&stabVel)[3]) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, nsh = R::nsh;
+    if (P.stab == STAB_WITHOUT) {
+#pragma unroll
+        for (int d = 0; d < dim; ++d) stabVel[d] = S.StdVel[d];
+        return;
+    }
+    T trace = T(0);
+#pragma unroll
+    for (int d = 0; d < dim; ++d) trace += gradVel[d][d];
+    const T idiag = S.idiag, irho = T(1) / rho;
+#pragma unroll
+    for (int d = 0; d < dim; ++d) {
+        T rhs = T(0);
+        if (P.hasSource) rhs = T(P.src[d]);
+        if (P.transient) {
+            T oldIPVel = T(0);
+#pragma unroll
+            for (int sh = 0; sh < nsh; ++sh) oldIPVel += ipN<ROID, T>(ip, sh) * uo[d][sh];
+            rhs += oldIPVel / T(P.dt);
+        }
+        rhs += S.nuL * S.StdVel[d];
+        if (!P.stokes) {
+            T UpS = T(0), DnS = T(0);
+            if (upShared) UpS = upShared[d];
+#pragma unroll
+            for (int sh = 0; sh < nsh; ++sh) {
+                if (!upShared) UpS += S.upS[sh] * u[d][sh];
+                if (P.stab == STAB_FLOW) DnS += S.dnS[sh] * u[d][sh];
+            }
+            rhs += S.nsvcl * UpS;
+            if (P.stab == STAB_FLOW) rhs += S.nsvdl * (DnS - UpS);
+        }
+        if (P.stab == STAB_FLOW) {
+            T cross = T(0);
+#pragma unroll
+            for (int d2 = 0; d2 < dim; ++d2)
+                if (d2 != d) cross += S.StdVel[d2] * gradVel[d][d2];
+            rhs += S.StdVel[d] * (trace - gradVel[d][d]) - cross;
+        }
+        rhs -= gradP[d] * irho;
+        stabVel[d] = rhs * idiag;
+    }
+}
+
 template <int ROID, typename T, class DSink>
 __device__ __forceinline__ void scvf_def_A(const DiscParams& P, const Elem<ROID, T>& E, const IpGeo<T>& G, const IpState<ROID, T>& S,
                                            const int ip, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
@@ -785,124 +870,65 @@ __device__ __forceinline__ void scvf_def_A(const DiscParams& P, const Elem<ROID,
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, Pc = dim;
     const T rho = T(P.rho);
-    {
-        // velocity and pressure gradients: local gradients first, then one J^-T
-        // (grad_k = J^-T lgrad_k, so sum_k u_k grad_k = J^-T sum_k u_k lgrad_k)
-        T gradVel[3][3], gradP[3];
-        {
-            const auto& tb = tab<ROID, T>();
-            T gl[4][3];
+    T gradVel[3][3], gradP[3];
+    ip_gradients<ROID, T>(G, ip, u, gradVel, gradP);
+    // diffusion
+    T flux[3];
 #pragma unroll
-            for (int f = 0; f <= dim; ++f)
+    for (int d1 = 0; d1 < dim; ++d1) {
+        T s = T(0);
 #pragma unroll
-                for (int c = 0; c < dim; ++c) {
-                    T acc = T(0);
+        for (int d2 = 0; d2 < dim; ++d2) s += gradVel[d1][d2] * G.n[d2];
+        if (!P.laplace) {
 #pragma unroll
-                    for (int sh = 0; sh < nsh; ++sh) acc += u[f][sh] * T(tb.ipLGrad[ip][sh][c]);
-                    gl[f][c] = acc;
-                }
-#pragma unroll
-            for (int f = 0; f <= dim; ++f)
-#pragma unroll
-                for (int d2 = 0; d2 < dim; ++d2) {
-                    T acc = T(0);
-#pragma unroll
-                    for (int c = 0; c < dim; ++c) acc += G.JtInv[d2][c] * gl[f][c];
-                    if (f < dim) gradVel[f][d2] = acc;
-                    else gradP[d2] = acc;
-                }
+            for (int d2 = 0; d2 < dim; ++d2) s += gradVel[d2][d1] * G.n[d2];
         }
-        // diffusion
-        T flux[3];
+        flux[d1] = s * (T(-1.0) * nu * rho);
+    }
+    // the convection's upwind velocity (before blending); with a shared upwind object
+    // it is also the stabilisation's
+    T UpConv[3] = {T(0), T(0), T(0)};
+    const bool upwindConv = !P.stokes && !P.pac;
+    if (upwindConv) {
 #pragma unroll
-        for (int d1 = 0; d1 < dim; ++d1) {
+        for (int d = 0; d < dim; ++d) {
             T s = T(0);
 #pragma unroll
-            for (int d2 = 0; d2 < dim; ++d2) s += gradVel[d1][d2] * G.n[d2];
-            if (!P.laplace) {
-#pragma unroll
-                for (int d2 = 0; d2 < dim; ++d2) s += gradVel[d2][d1] * G.n[d2];
-            }
-            flux[d1] = s * (T(-1.0) * nu * rho);
+            for (int sh = 0; sh < nsh; ++sh) s += S.upC[sh] * u[d][sh];
+            UpConv[d] = s;
         }
-        // convection
-        T UpVelShared[3] = {T(0), T(0), T(0)};   // upwind velocity before blending (= the stabilisation's when shared)
-        if (!P.stokes) {
-            T UpwindVel[3];
-#pragma unroll
-            for (int d = 0; d < dim; ++d) {
-                T s = T(0);
-#pragma unroll
-                for (int sh = 0; sh < nsh; ++sh) s += S.upC[sh] * u[d][sh];
-                UpwindVel[d] = s;
-                UpVelShared[d] = s;
-            }
-            if (P.peclet) peclet_blend<ROID, T>(G, S.StdVel, nu, UpwindVel);
-            T prod = T(0);
-#pragma unroll
-            for (int d = 0; d < dim; ++d) prod += S.StdVel[d] * G.n[d];
-            prod *= rho;
-#pragma unroll
-            for (int d1 = 0; d1 < dim; ++d1) flux[d1] += UpwindVel[d1] * prod;
-        }
-        // pressure
-        T pressure = T(0);
-#pragma unroll
-        for (int sh = 0; sh < nsh; ++sh) pressure += ipN<ROID, T>(ip, sh) * u[Pc][sh];
-#pragma unroll
-        for (int d1 = 0; d1 < dim; ++d1) flux[d1] += pressure * G.n[d1];
-        // continuity with the stabilised velocity
-        T stabVel[3];
-        if (P.stab == STAB_WITHOUT) {
-#pragma unroll
-            for (int d = 0; d < dim; ++d) stabVel[d] = S.StdVel[d];
-        } else {
-            T trace = T(0);
-#pragma unroll
-            for (int d = 0; d < dim; ++d) trace += gradVel[d][d];
-            const T idiag = S.idiag, irho = T(1) / rho;
-#pragma unroll
-            for (int d = 0; d < dim; ++d) {
-                T rhs = T(0);
-                if (P.hasSource) rhs = T(P.src[d]);
-                if (P.transient) {
-                    T oldIPVel = T(0);
-#pragma unroll
-                    for (int sh = 0; sh < nsh; ++sh) oldIPVel += ipN<ROID, T>(ip, sh) * uo[d][sh];
-                    rhs += oldIPVel / T(P.dt);
-                }
-                rhs += S.nuL * S.StdVel[d];
-                if (!P.stokes) {
-                    T UpS = T(0), DnS = T(0);
-                    if (P.sameUpwind) UpS = UpVelShared[d];
-#pragma unroll
-                    for (int sh = 0; sh < nsh; ++sh) {
-                        if (!P.sameUpwind) UpS += S.upS[sh] * u[d][sh];
-                        if (P.stab == STAB_FLOW) DnS += S.dnS[sh] * u[d][sh];
-                    }
-                    rhs += S.nsvcl * UpS;
-                    if (P.stab == STAB_FLOW) rhs += S.nsvdl * (DnS - UpS);
-                }
-                if (P.stab == STAB_FLOW) {
-                    T cross = T(0);
-#pragma unroll
-                    for (int d2 = 0; d2 < dim; ++d2)
-                        if (d2 != d) cross += S.StdVel[d2] * gradVel[d][d2];
-                    rhs += S.StdVel[d] * (trace - gradVel[d][d]) - cross;
-                }
-                rhs -= gradP[d] * irho;
-                stabVel[d] = rhs * idiag;
-            }
-        }
-        T contFlux = T(0);
-#pragma unroll
-        for (int d = 0; d < dim; ++d) contFlux += stabVel[d] * G.n[d];
-        contFlux *= rho;
-#pragma unroll
-        for (int d1 = 0; d1 < dim; ++d1) { sink.add(G.from, d1, flux[d1]); sink.add(G.to, d1, -flux[d1]); }
-        sink.add(G.from, Pc, contFlux);
-        sink.add(G.to, Pc, -contFlux);
     }
+    T stabVel[3];
+    stab_velocity<ROID, T>(P, S, ip, u, uo, gradVel, gradP, rho, (upwindConv && P.sameUpwind) ? UpConv : nullptr, stabVel);
+    // convection: the upwind velocity, or the stabilised velocity with PAC
+    // (navier_stokes_fv1.cpp:707-712)
+    if (!P.stokes) {
+        T UpwindVel[3];
+#pragma unroll
+        for (int d = 0; d < dim; ++d) UpwindVel[d] = P.pac ? stabVel[d] : UpConv[d];
+        if (P.peclet) peclet_blend<ROID, T>(G, S.StdVel, nu, UpwindVel);
+        T prod = T(0);
+#pragma unroll
+        for (int d = 0; d < dim; ++d) prod += S.StdVel[d] * G.n[d];
+        prod *= rho;
+#pragma unroll
+        for (int d1 = 0; d1 < dim; ++d1) flux[d1] += UpwindVel[d1] * prod;
+    }
+    // pressure
+    T pressure = T(0);
+#pragma unroll
+    for (int sh = 0; sh < nsh; ++sh) pressure += ipN<ROID, T>(ip, sh) * u[Pc][sh];
+#pragma unroll
+    for (int d1 = 0; d1 < dim; ++d1) flux[d1] += pressure * G.n[d1];
+    // continuity with the stabilised velocity
+    T contFlux = T(0);
+#pragma unroll
+    for (int d = 0; d < dim; ++d) contFlux += stabVel[d] * G.n[d];
+    contFlux *= rho;
+#pragma unroll
+    for (int d1 = 0; d1 < dim; ++d1) { sink.add(G.from, d1, flux[d1]); sink.add(G.to, d1, -flux[d1]); }
+    sink.add(G.from, Pc, contFlux);
+    sink.add(G.to, Pc, -contFlux);
 }
 
 template <int ROID, typename T, class DSink>
@@ -930,10 +956,12 @@ __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID,
 // through the sink (sink.add(i, k, B, plus)); 'scale' multiplies B (dt for the
 // implicit-Euler Jacobian M + dt dA/du).
 // ---------------------------------------------------------------------------
-template <int ROID, typename T, class Sink>
+// PAC: compile the stabilisation-as-upwind branches (set_pac_upwind); without it
+// those branches cost registers in every configuration
+template <int ROID, typename T, bool PAC, class Sink>
 __device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const IpGeo<T>& G, const IpState<ROID, T>& S,
-                                           const int ip, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh], const T scale, Sink& sink,
-                                           const T nu) {
+                                           const int ip, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
+                                           const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], const T scale, Sink& sink, const T nu) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, b = R::b, Pc = dim;
     const T rho = T(P.rho);
@@ -943,24 +971,37 @@ __device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const IpGeo<T>& 
         T w = T(1), prod = T(0), Vn = T(0);
 #pragma unroll
         for (int d = 0; d < dim; ++d) Vn += S.StdVel[d] * G.n[d];
+        const bool pac = PAC && !P.stokes && P.pac;
+        const bool fullNewton = !P.stokes && P.fullNewton != 0.0;
         if (!P.stokes) {
+            if (pac) {
+                // the stabilised velocity is the upwind velocity (navier_stokes_fv1.cpp:382-384); the
+                // Jacobian needs it only for the exact-Jacobian terms
+                if (fullNewton) {
+                    T gradVel[3][3], gradP[3];
+                    ip_gradients<ROID, T>(G, ip, u, gradVel, gradP);
+                    stab_velocity<ROID, T>(P, S, ip, u, uo, gradVel, gradP, rho, nullptr, UpwindVel);
+                }
+            } else {
 #pragma unroll
-            for (int d = 0; d < dim; ++d) {
-                T s = T(0);
+                for (int d = 0; d < dim; ++d) {
+                    T s = T(0);
 #pragma unroll
-                for (int sh = 0; sh < nsh; ++sh) s += S.upC[sh] * u[d][sh];
-                UpwindVel[d] = s;
+                    for (int sh = 0; sh < nsh; ++sh) s += S.upC[sh] * u[d][sh];
+                    UpwindVel[d] = s;
+                }
             }
             if (P.peclet) w = peclet_blend<ROID, T>(G, S.StdVel, nu, UpwindVel);
             prod = Vn * rho;
         }
-        const T idiag = S.idiag;
+        const T idiag = S.idiag, irho = T(1) / rho;
         const T ri = rho * idiag;
         // per-SCVF factors of the column loop
         T mn[3], rin[3], nrho[3];
 #pragma unroll
         for (int d = 0; d < dim; ++d) { mn[d] = mnr * G.n[d]; rin[d] = ri * G.n[d]; nrho[d] = G.n[d] * rho; }
-        const T riVn = ri * Vn, pw = prod * w, ppe = prod * (T(1) - w), ppr = -ri * (T(1) / rho);
+        const T riVn = ri * Vn, pw = prod * w, ppe = prod * (T(1) - w), ppr = -ri * irho;
+        const T fr = T(P.fullNewton) * rho;
 #pragma unroll
         for (int k = 0; k < nsh; ++k) {
             T g[3];
@@ -972,9 +1013,9 @@ __device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const IpGeo<T>& 
             T B[b][b];
             // diffusion: -nu rho ((g.n) I + g (x) n)
             T dd = mnr * gn;
-            // convection (fixpoint part) on the diagonal
+            // convection (fixpoint part) on the diagonal: the upwind shape, the Peclet blend
             if (!P.stokes) {
-                dd += S.upC[k] * pw;
+                if (!pac) dd += S.upC[k] * pw;
                 if (P.peclet) dd += ppe * N;
             }
 #pragma unroll
@@ -985,10 +1026,11 @@ __device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const IpGeo<T>& 
                     if (d1 == d2) v += dd;
                     B[d1][d2] = v;
                 }
-            if (!P.stokes && P.fullNewton != 0.0) {
+            if (fullNewton) {
 #pragma unroll
                 for (int d2 = 0; d2 < dim; ++d2) {
-                    T pv = w * S.upC[k] * nrho[d2];
+                    // upwind used as upwind (:521-534, the factor is not applied there) and the Peclet blend
+                    T pv = pac ? T(0) : w * S.upC[k] * nrho[d2];
                     if (P.peclet) pv += (T(1) - w) * N * nrho[d2];
 #pragma unroll
                     for (int d1 = 0; d1 < dim; ++d1) B[d1][d2] += pv * UpwindVel[d1];
@@ -997,13 +1039,14 @@ __device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const IpGeo<T>& 
             // pressure
 #pragma unroll
             for (int d1 = 0; d1 < dim; ++d1) B[d1][Pc] = N * G.n[d1];
-            // continuity
+            // continuity: the stabilised-velocity shapes of corner k (diagonal branch)
+            T Sk = T(0);
             if (P.stab == STAB_WITHOUT) {
 #pragma unroll
                 for (int d1 = 0; d1 < dim; ++d1) B[Pc][d1] = N * nrho[d1];
                 B[Pc][Pc] = T(0);
             } else {
-                T Sk = S.nuL * N;
+                Sk = S.nuL * N;
                 if (!P.stokes) {
                     Sk += S.nsvcl * S.upS[k];
                     if (P.stab == STAB_FLOW) Sk += S.nsvdl * (S.dnS[k] - S.upS[k]);
@@ -1018,6 +1061,55 @@ __device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const IpGeo<T>& 
                 }
                 B[Pc][Pc] = gn * ppr;
             }
+            if (pac) {
+                // the stabilisation's shapes stab_shape_vel(ip, a, c, k) = V[a][c] and
+                // stab_shape_p(ip, a, k) = Q[a] (diagonal branch; without stabilisation the
+                // interpolation shape)
+                T V[3][3], Q[3];
+                const bool flow = P.stab == STAB_FLOW, without = P.stab == STAB_WITHOUT;
+#pragma unroll
+                for (int a = 0; a < dim; ++a) {
+#pragma unroll
+                    for (int c = 0; c < dim; ++c) {
+                        T v;
+                        if (without) v = (a == c) ? N : T(0);
+                        else if (flow) v = ((a == c) ? (Sk - Vg + S.StdVel[a] * g[a]) : S.StdVel[a] * g[c]) * idiag;
+                        else v = (a == c) ? Sk * idiag : T(0);
+                        V[a][c] = v;
+                    }
+                    Q[a] = without ? T(0) : T(-1) * g[a] * irho * idiag;
+                }
+                // stabilisation used as upwind, fixpoint part (navier_stokes_fv1.cpp:398-427)
+#pragma unroll
+                for (int d1 = 0; d1 < dim; ++d1) {
+#pragma unroll
+                    for (int d2 = 0; d2 < dim; ++d2)
+                        if (flow || d1 == d2) B[d1][d2] += pw * V[d1][d2];
+                    B[d1][Pc] += pw * Q[d1];
+                }
+                if (fullNewton) {
+                    // exact-Jacobian part (:477-518); without connected velocity components the
+                    // (d1, d1) shape serves every column d2 and the blend weight is not applied
+                    T pp = T(0);
+#pragma unroll
+                    for (int q = 0; q < dim; ++q) pp += Q[q] * G.n[q];
+#pragma unroll
+                    for (int d1 = 0; d1 < dim; ++d1) {
+#pragma unroll
+                        for (int d2 = 0; d2 < dim; ++d2) {
+                            T pv = T(0);
+                            if (flow) {
+#pragma unroll
+                                for (int q = 0; q < dim; ++q) pv += w * V[q][d2] * G.n[q];
+                            } else {
+                                pv = V[d1][d1] * G.n[d1];
+                            }
+                            B[d1][d2] += pv * fr * UpwindVel[d1];
+                        }
+                        B[d1][Pc] += pp * fr * UpwindVel[d1];
+                    }
+                }
+            }
             if (scale != T(1)) {
 #pragma unroll
                 for (int r = 0; r < b; ++r)
@@ -1030,9 +1122,9 @@ __device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const IpGeo<T>& 
     }
 }
 
-template <int ROID, typename T, class Sink>
+template <int ROID, typename T, bool PAC, class Sink>
 __device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
-                                           const T scale, Sink& sink, const T nu) {
+                                           const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], const T scale, Sink& sink, const T nu) {
     using R = Ref<ROID>;
     T corMinN = T(0), corMinD = T(0), corAvgN = T(1);
     if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, T>(E, corMinN, corMinD, corAvgN);
@@ -1044,7 +1136,7 @@ __device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID,
         IpState<ROID, T> S;
         ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
         ok &= S.ok;
-        scvf_jac_A<ROID, T>(P, G, S, ip, u, scale, sink, nu);
+        scvf_jac_A<ROID, T, PAC>(P, G, S, ip, u, uo, scale, sink, nu);
     }
     return ok;
 }
@@ -1073,7 +1165,7 @@ __device__ __forceinline__ void narrow(const IpState<ROID, double>& a, IpState<R
 
 // FP64 defect and FP32 Jacobian of one element in one pass: geometry, upwinds,
 // stabilisation and defect in FP64; the Jacobian blocks in FP32 from that state.
-template <int ROID, class DSink, class JSink>
+template <int ROID, bool PAC, class DSink, class JSink>
 __device__ __forceinline__ bool elem_def_jac_A_mixed(const DiscParams& P, const Elem<ROID, double>& E,
                                                      const double (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
                                                      const double (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], DSink& dsink, const float jscale,
@@ -1082,11 +1174,16 @@ __device__ __forceinline__ bool elem_def_jac_A_mixed(const DiscParams& P, const 
     constexpr int b = R::b, nsh = R::nsh;
     double corMinN = 0.0, corMinD = 0.0, corAvgN = 1.0;
     if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, double>(E, corMinN, corMinD, corAvgN);
-    float uf[b][nsh];
+    constexpr int dim = R::dim;
+    float uf[b][nsh], uof[dim][nsh];
 #pragma unroll
     for (int f = 0; f < b; ++f)
 #pragma unroll
         for (int k = 0; k < nsh; ++k) uf[f][k] = (float)u[f][k];
+#pragma unroll
+    for (int f = 0; f < dim; ++f)
+#pragma unroll
+        for (int k = 0; k < nsh; ++k) uof[f][k] = P.transient ? (float)uo[f][k] : 0.0f;
     bool ok = true;
 #pragma unroll 1
     for (int ip = 0; ip < R::nip; ++ip) {
@@ -1100,7 +1197,7 @@ __device__ __forceinline__ bool elem_def_jac_A_mixed(const DiscParams& P, const 
         IpState<ROID, float> Sf;
         narrow(G, Gf);
         narrow<ROID>(S, Sf);
-        scvf_jac_A<ROID, float>(P, Gf, Sf, ip, uf, jscale, jsink, (float)nu);
+        scvf_jac_A<ROID, float, PAC>(P, Gf, Sf, ip, uf, uof, jscale, jsink, (float)nu);
     }
     return ok;
 }
@@ -1111,7 +1208,7 @@ __device__ __forceinline__ bool elem_def_jac_A_mixed(const DiscParams& P, const 
 // add_jac_A_elem, navier_stokes_fv1.cpp:296-309, 645-659). 'jscale' multiplies
 // the Jacobian blocks (dt for the implicit-Euler Jacobian); the defect sink
 // applies its own scaling.
-template <int ROID, typename T, class DSink, class JSink>
+template <int ROID, typename T, bool PAC, class DSink, class JSink>
 __device__ __forceinline__ bool elem_def_jac_A(const DiscParams& P, const Elem<ROID, T>& E, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
                                                const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], DSink& dsink, const T jscale,
                                                JSink& jsink, const T nu) {
@@ -1127,7 +1224,7 @@ __device__ __forceinline__ bool elem_def_jac_A(const DiscParams& P, const Elem<R
         ip_state<ROID, T>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
         ok &= S.ok;
         scvf_def_A<ROID, T>(P, E, G, S, ip, u, uo, dsink, nu);
-        scvf_jac_A<ROID, T>(P, G, S, ip, u, jscale, jsink, nu);
+        scvf_jac_A<ROID, T, PAC>(P, G, S, ip, u, uo, jscale, jsink, nu);
     }
     return ok;
 }

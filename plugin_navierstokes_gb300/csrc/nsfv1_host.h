@@ -33,6 +33,7 @@ struct Disc {
     double src[3] = {0, 0, 0};
     int hasSource = 0, stokes = 0, laplace = 0, peclet = 0;
     bool viscoSet = false, stabSet = false, convUpwindSet = false, stabSharesConv = false;
+    bool pac = false;   // set_pac_upwind(true): the stabilisation is the convective upwind
     int convUpwindType = -1, stabUpwindType = -1, stabType = -1, diffLen = DL_RAW;
 
     // mesh

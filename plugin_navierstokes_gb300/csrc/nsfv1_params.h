@@ -17,6 +17,7 @@ struct DiscParams {
     int sameUpwind;   // 1: the stabilisation shares the convection upwind object
     int stab, diffLen;
     int stokes, laplace, peclet, hasSource, transient;
+    int pac;          // the stabilisation is the convective upwind (set_pac_upwind)
 };
 
 }  // namespace nsfv1

@@ -100,6 +100,10 @@ class NavierStokesFV1:
     def set_stabilization(self, name: str, diff_length: str | None = None) -> None:
         self._c(self._lib.nsfv1_set_stabilization(self._h, name.encode(), diff_length.encode() if diff_length else None))
 
+    def set_pac_upwind(self, on: bool) -> None:
+        """set_pac_upwind (navier_stokes_fv1.h:217-225): the stabilised velocity as the convective upwind."""
+        self._c(self._lib.nsfv1_set_pac_upwind(self._h, int(bool(on))))
+
     def set_stabilization_upwind(self, name: str) -> None:
         self._c(self._lib.nsfv1_set_stabilization_upwind(self._h, name.encode()))
 

@@ -43,6 +43,11 @@ def fixtures():
                 out[key + "_uold"] = uo
             for k, v in r.items():
                 out[key + "_" + k] = v
+            # the same elements with the stabilisation as the convective upwind (set_pac_upwind)
+            if not cfg[7]:
+                r = oracle.ref_elem_batch(roid, dict(ref_config(dim, cfg), pac=True), corners, u, uo, DT)
+                for k, v in r.items():
+                    out[key + "_pac_" + k] = v
     return out
 
 

@@ -151,3 +151,18 @@ def test_pattern_and_coloring_bit_exact_at_benchmark_size_host():
     ocol, onc = o.coloring()
     assert ci.size == 193 ** 3 and nc == onc == 8
     assert np.array_equal(rp, orp) and np.array_equal(ci, oci) and np.array_equal(col, ocol)
+
+
+def test_pac_upwind_needs_an_upwind_and_a_stabilisation():
+    """set_pac_upwind(true) (navier_stokes_fv1.h:217-225) with the reference's texts."""
+    d = NavierStokesFV1("u,v,p")
+    with pytest.raises(NSFV1Error) as ex:
+        d.set_pac_upwind(True)
+    assert ex.value.status == _capi.ERR_STATE and "Upwind must be specified previously" in str(ex.value)
+    d.set_upwind("full")
+    with pytest.raises(NSFV1Error) as ex:
+        d.set_pac_upwind(True)
+    assert "Stabilization must be specified previously" in str(ex.value)
+    d.set_stabilization("fields")
+    d.set_pac_upwind(True)
+    d.set_pac_upwind(False)   # changes nothing, as in the reference

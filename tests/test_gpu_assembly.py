@@ -62,6 +62,68 @@ def test_element_callbacks_match_reference_fixtures(cuda, tname, ci):
 
 
 @pytest.mark.parametrize("tname", list(ROIDS))
+@pytest.mark.parametrize("ci", [i for i, c in enumerate(DISC_CASES) if not c[7]])
+def test_pac_element_callbacks_match_reference_fixtures(cuda, tname, ci):
+    """set_pac_upwind(true) on the GPU against the reference's own PAC outputs."""
+    import torch
+    g = np.load(os.path.join(GOLDEN, "reference_elements.npz"))
+    roid = ROIDS[tname]
+    dim = DIM[roid]
+    key = f"{tname}_{ci}"
+    uo = g[key + "_uold"] if (key + "_uold") in g else None
+    d = NavierStokesFV1(dim=dim)
+    configure(d, dim, DISC_CASES[ci])
+    d.set_pac_upwind(True)
+    corners, u = g[key + "_corners"], g[key + "_u"]
+    n = corners.shape[0]
+    nloc = (dim + 1) * NSH[roid]
+    t = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=cuda)
+    out = {k: torch.zeros((n, nloc), dtype=torch.float64, device=cuda) for k in ("defA", "defM", "rhs")}
+    out.update({k: torch.zeros((n, nloc * nloc), dtype=torch.float64, device=cuda) for k in ("jacA", "jacM")})
+    d.elem_batch(roid, t(corners), t(u), None if uo is None else t(uo), 0.01, **out)
+    torch.cuda.synchronize()
+    for k in ("defA", "jacA", "defM", "jacM", "rhs"):
+        r = out[k].cpu().numpy()
+        assert rel_err(r, g[key + "_pac_" + k]) <= TOL64, (key, "pac", k, rel_err(r, g[key + "_pac_" + k]))
+
+
+@pytest.mark.parametrize("gen", ["quads", "hexes", "tris"])
+@pytest.mark.parametrize("cfgi", [1, 2, 3])
+def test_pac_global_assembly_matches_oracle(cuda, gen, cfgi):
+    """PAC through the global kernels (separate and fused, FP64 and FP32 values)."""
+    import torch
+    roid, X, C = {"quads": lambda: mesh.structured_quads(12), "hexes": lambda: mesh.structured_hexes(4),
+                  "tris": lambda: mesh.jittered_triangles(10, seed=6)}[gen]()
+    dim = DIM[roid]
+    cfg = DISC_CASES[cfgi]
+    b = dim + 1
+    U = mesh.solenoidal_state(X, seed=13) if dim == 3 else (mesh.uniform(14, X.shape[0] * 3) * 2 - 1).reshape(-1, 3)
+    Uo = (U * 0.85) if cfg[3] else None
+    dt = 0.02 if cfg[3] else 0.0
+    o = oracle.Oracle(dim); configure(o, dim, cfg); o.set_pac_upwind(True); o.set_mesh(roid, X, C)
+    d = NavierStokesFV1(dim=dim); configure(d, dim, cfg); d.set_pac_upwind(True); d.set_mesh(roid, X, C)
+    Dref, Jref = o.assemble(U, Uo, dt)
+    tu = torch.tensor(U.ravel(), dtype=torch.float64, device=cuda)
+    tuo = None if Uo is None else torch.tensor(Uo.ravel(), dtype=torch.float64, device=cuda)
+    D = torch.empty_like(tu)
+    J = torch.empty(o.nnzb * b * b, dtype=torch.float64, device=cuda)
+    d.assemble_defect(tu, D, tuo, dt)
+    d.assemble_jacobian(tu, J, tuo, dt)
+    torch.cuda.synchronize()
+    assert rel_err(D.cpu().numpy(), Dref) <= TOL64 and rel_err(J.cpu().numpy(), Jref) <= TOL64
+    d.assemble_defect_jacobian(tu, D, J, tuo, dt)
+    torch.cuda.synchronize()
+    assert rel_err(D.cpu().numpy(), Dref) <= TOL64 and rel_err(J.cpu().numpy(), Jref) <= TOL64
+    J32 = torch.empty(o.nnzb * b * b, dtype=torch.float32, device=cuda)
+    d.assemble_jacobian(tu, J32, tuo, dt)
+    torch.cuda.synchronize()
+    assert rel_err(J32.double().cpu().numpy(), Jref) <= TOL32
+    d.assemble_defect_jacobian(tu, D, J32, tuo, dt)
+    torch.cuda.synchronize()
+    assert rel_err(J32.double().cpu().numpy(), Jref) <= TOL32
+
+
+@pytest.mark.parametrize("tname", list(ROIDS))
 @pytest.mark.parametrize("ci", range(len(DISC_CASES)))
 def test_element_callbacks_match_oracle_random(cuda, tname, ci):
     roid = ROIDS[tname]

@@ -39,6 +39,23 @@ def test_oracle_reproduces_the_reference_fixtures(tname, ci):
         assert rel_err(r[k], g[key + "_" + k]) <= TOL, (key, cfg_name(DISC_CASES[ci]), k, rel_err(r[k], g[key + "_" + k]))
 
 
+@pytest.mark.parametrize("tname", list(ROIDS))
+@pytest.mark.parametrize("ci", [i for i, c in enumerate(DISC_CASES) if not c[7]])
+def test_oracle_pac_reproduces_the_reference_fixtures(tname, ci):
+    """set_pac_upwind(true): the stabilised velocity as the convective upwind."""
+    g = np.load(GOLDEN)
+    roid = ROIDS[tname]
+    dim = DIM[roid]
+    key = f"{tname}_{ci}"
+    uo = g[key + "_uold"] if (key + "_uold") in g else None
+    o = oracle.Oracle(dim)
+    configure(o, dim, DISC_CASES[ci])
+    o.set_pac_upwind(True)
+    r = o.elem_batch(roid, g[key + "_corners"], g[key + "_u"], uo, 0.01)
+    for k in ("defA", "jacA", "defM", "jacM", "rhs"):
+        assert rel_err(r[k], g[key + "_pac_" + k]) <= TOL, (key, "pac", k, rel_err(r[k], g[key + "_pac_" + k]))
+
+
 @pytest.mark.skipif(not has_ref, reason="reference checkout not present")
 @pytest.mark.parametrize("tname", list(ROIDS))
 @pytest.mark.parametrize("ci", range(len(DISC_CASES)))
