@@ -130,6 +130,11 @@ int nsfv1_set_dirichlet(nsfv1_disc* h, int64_t n, const int32_t* dofs, const dou
 
 /* ---- boundary-condition element discs (host arrays) ---------------------- */
 
+/* ugcore's DirichletBoundary::add, for single unknowns: appends Dirichlet rows
+ * (dofs[k] = node * b + fct, value g_k) to the handle's, a later value of the same
+ * unknown replacing an earlier one (nsfv1_set_dirichlet replaces them all). */
+int nsfv1_add_dirichlet(nsfv1_disc* h, int64_t n, const int32_t* dofs, const double* values);
+
 /* NavierStokesWall::add(subsets) (incompressible/bnd/wall_impl.h:57-69): every
  * velocity component of the given nodes is a Dirichlet row with value 0.
  * Rows accumulate with earlier nsfv1_add_wall / nsfv1_add_inflow calls (a later

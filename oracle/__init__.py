@@ -56,6 +56,7 @@ def load():
             "ora_newton": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_double, c_int, c_double, c_int, c_int, c_int, c_void_p]),
             "ora_bsr_mv": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
             "ora_add_wall": (c_int, [c_void_p, c_int64, c_void_p]),
+            "ora_add_dirichlet": (c_int, [c_void_p, c_int64, c_void_p, c_void_p]),
             "ora_add_inflow": (c_int, [c_void_p, c_int64, c_int, c_void_p, c_void_p]),
         }
         for k, (r, a) in sig.items():
@@ -148,6 +149,11 @@ class Oracle:
         self.dofs = np.ascontiguousarray(dofs, np.int32)
         self.dvals = np.ascontiguousarray(vals, np.float64)
         self._c(self.lib.ora_set_dirichlet(self.h, self.dofs.size, self.dofs.ctypes.data, self.dvals.ctypes.data))
+
+    def add_dirichlet(self, dofs, vals):
+        r = np.ascontiguousarray(dofs, np.int32)
+        v = np.ascontiguousarray(vals, np.float64)
+        self._c(self.lib.ora_add_dirichlet(self.h, r.size, r.ctypes.data, v.ctypes.data))
 
     def add_wall(self, nodes):
         a = np.ascontiguousarray(nodes, np.int32)

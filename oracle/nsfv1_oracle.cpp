@@ -1604,6 +1604,12 @@ int ora_newton(void* h, double* U, const double* Uold, double dt, double rtol, i
 }
 
 /* BSR mat-vec with the oracle's own loop (for SpMV parity tests). */
+int ora_add_dirichlet(void* h, int64_t n, const int32_t* rows, const double* vals) {
+    auto* P = static_cast<Problem*>(h);
+    merge_dirichlet(*P, std::vector<int32_t>(rows, rows + n), std::vector<number>(vals, vals + n));
+    return 0;
+}
+
 int ora_add_wall(void* h, int64_t n, const int32_t* nodes) {
     auto* P = static_cast<Problem*>(h);
     const int dim = P->mesh.dim, b = dim + 1;

@@ -107,6 +107,7 @@ _SIGS = {
     "nsfv1_get_coloring": (c_int, [c_void_p, c_void_p]),
     "nsfv1_device_pattern": (c_int, [c_void_p, POINTER(c_void_p), POINTER(c_void_p)]),
     "nsfv1_set_dirichlet": (c_int, [c_void_p, c_int64, c_void_p, c_void_p]),
+    "nsfv1_add_dirichlet": (c_int, [c_void_p, c_int64, c_void_p, c_void_p]),
     "nsfv1_add_wall": (c_int, [c_void_p, c_int64, c_void_p]),
     "nsfv1_add_inflow": (c_int, [c_void_p, c_int64, c_int, c_void_p, c_void_p]),
     "nsfv1_clear_boundary": (c_int, [c_void_p]),

@@ -35,6 +35,17 @@ def _flags(extra: list[str] | None = None) -> list[str]:
     return f + (extra or [])
 
 
+def compile_bounds_checked(out: Path) -> Path:
+    """Compiles the assembly kernels with NSFV1_BOUNDS_CHECK (every node id and
+    block index checked, out-of-range accesses skipped and reported through the
+    error word) into the object file out."""
+    cmd = [nvcc_path()] + _flags(["-DNSFV1_BOUNDS_CHECK"]) + ["-c", str(CSRC / "nsfv1_assemble.cu"), "-o", str(out)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for the bounds-checked assembly:\n" + r.stdout + r.stderr)
+    return out
+
+
 def _needs_rebuild() -> bool:
     if not LIB.exists():
         return True

@@ -8,6 +8,18 @@
 #include "nsfv1_internal.h"
 #include "nsfv1_elem.cuh"
 
+// NSFV1_BOUNDS_CHECK (compile-time; the bounds-checked library variant): every
+// node id read from the connectivity and every block index of the scatter is
+// checked against the mesh; an index out of range sets bit 2 of the handle's
+// error word (NSFV1_ERR_ARGUMENT on the host) and the access is skipped. This
+// replaces the reference's UG_NSUPWIND_ASSERT / UG_NSSTAB_ASSERT bounds asserts
+// (upwind_interface.h:36-38, stabilization.h:36-38) without trapping the GPU.
+#ifdef NSFV1_BOUNDS_CHECK
+#define NSFV1_IN_RANGE(i, n, err) (((int64_t)(i) >= 0 && (int64_t)(i) < (int64_t)(n)) ? true : (atomicOr((err), 4), false))
+#else
+#define NSFV1_IN_RANGE(i, n, err) true
+#endif
+
 namespace nsfv1 {
 
 static constexpr int kThreads = 128;
@@ -59,12 +71,16 @@ template <typename VT, int nsh>
 struct GlobalJacSink {
     VT* __restrict__ vals;
     const int32_t* __restrict__ blk;   // this element's [nsh][nsh] block indices
+    int64_t nnzb = 0;                  // checked with NSFV1_BOUNDS_CHECK
+    int* err = nullptr;
     template <int b, typename T>
     __device__ __forceinline__ void add(const int i, const int k, const T (&B)[b][b], const bool plus) {
         // fire-and-forget reductions (executed in L2, no load latency); within a
         // colour no other thread touches this block and one thread's updates to an
         // address apply in program order, so the sums stay deterministic
-        VT* p = vals + (int64_t)__ldg(blk + i * nsh + k) * (b * b);
+        const int32_t q = __ldg(blk + i * nsh + k);
+        if (!NSFV1_IN_RANGE(q, nnzb, err)) return;
+        VT* p = vals + (int64_t)q * (b * b);
         if constexpr (std::is_same<VT, float>::value && b == 4) {
             // one 16-byte vector reduction per block row (the value array is 16-byte aligned)
 #pragma unroll
@@ -139,7 +155,10 @@ __global__ void __launch_bounds__(kThreads) k_defect(const DiscParams P, const A
     GlobalDefSink<nsh, b> sink;
     sink.D = A.D;
 #pragma unroll
-    for (int k = 0; k < nsh; ++k) sink.nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
+    for (int k = 0; k < nsh; ++k) {
+        sink.nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
+        if (!NSFV1_IN_RANGE(sink.nodes[k], A.nNodes, A.err)) return;
+    }
     Elem<ROID, double> E;
     load_corners<ROID, double>(A.coords, sink.nodes, E);
     elem_setup<ROID, double>(E);
@@ -195,7 +214,10 @@ __global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const
     const T nuEl = (T)(A.nuElem ? __ldg(A.nuElem + e) : P.nu);
     int32_t nodes[nsh];
 #pragma unroll
-    for (int k = 0; k < nsh; ++k) nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
+    for (int k = 0; k < nsh; ++k) {
+        nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
+        if (!NSFV1_IN_RANGE(nodes[k], A.nNodes, A.err)) return;
+    }
     Elem<ROID, T> E;
     load_corners<ROID, T>(A.coords, nodes, E);
     elem_setup<ROID, T>(E);
@@ -217,14 +239,16 @@ __global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const
 #pragma unroll
             for (int k = 0; k < nsh; ++k) uo[d][k] = T(0);
     }
-    GlobalJacSink<VT, nsh> sink{reinterpret_cast<VT*>(A.vals), A.elemBlk + (int64_t)e * nsh * nsh};
+    GlobalJacSink<VT, nsh> sink{reinterpret_cast<VT*>(A.vals), A.elemBlk + (int64_t)e * nsh * nsh, A.nnzb, A.err};
     const T scale = P.transient ? (T)P.dt : T(1);
     if (!elem_jac_A<ROID, T, PAC>(P, E, u, uo, scale, sink, nuEl)) atomicOr(A.err, 1);
     if (P.transient) {
         // mass part: J(d, sh, d, sh) += |SCV| rho
 #pragma unroll
         for (int k = 0; k < nsh; ++k) {
-            VT* p = sink.vals + (int64_t)__ldg(sink.blk + k * nsh + k) * (b * b);
+            const int32_t q = __ldg(sink.blk + k * nsh + k);
+            if (!NSFV1_IN_RANGE(q, A.nnzb, A.err)) continue;
+            VT* p = sink.vals + (int64_t)q * (b * b);
 #pragma unroll
             for (int d = 0; d < dim; ++d) atomicAdd(p + d * b + d, (VT)(E.vol[k] * T(P.rho)));
         }
@@ -246,7 +270,10 @@ __global__ void __launch_bounds__(kThreads) k_defect_jacobian(const DiscParams P
     GlobalDefSink<nsh, b> sink;
     sink.D = A.D;
 #pragma unroll
-    for (int k = 0; k < nsh; ++k) sink.nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
+    for (int k = 0; k < nsh; ++k) {
+        sink.nodes[k] = __ldg(A.conn + (int64_t)e * nsh + k);
+        if (!NSFV1_IN_RANGE(sink.nodes[k], A.nNodes, A.err)) return;
+    }
     Elem<ROID, double> E;
     load_corners<ROID, double>(A.coords, sink.nodes, E);
     elem_setup<ROID, double>(E);
@@ -261,7 +288,7 @@ __global__ void __launch_bounds__(kThreads) k_defect_jacobian(const DiscParams P
 #pragma unroll
             for (int k = 0; k < nsh; ++k) uo[d][k] = t4[d][k];
     }
-    GlobalJacSink<VT, nsh> jsink{reinterpret_cast<VT*>(A.vals), A.elemBlk + (int64_t)e * nsh * nsh};
+    GlobalJacSink<VT, nsh> jsink{reinterpret_cast<VT*>(A.vals), A.elemBlk + (int64_t)e * nsh * nsh, A.nnzb, A.err};
     DiscParams Q = P;
     Q.transient = TRANSIENT ? 1 : 0;
     bool ok;
@@ -292,7 +319,9 @@ __global__ void __launch_bounds__(kThreads) k_defect_jacobian(const DiscParams P
             if (any) atomicAdd(A.D + (int64_t)sink.nodes[k] * b + f, v);
         }
         if constexpr (TRANSIENT) {
-            VT* p = jsink.vals + (int64_t)__ldg(jsink.blk + k * nsh + k) * (b * b);
+            const int32_t q = __ldg(jsink.blk + k * nsh + k);
+            if (!NSFV1_IN_RANGE(q, A.nnzb, A.err)) continue;
+            VT* p = jsink.vals + (int64_t)q * (b * b);
 #pragma unroll
             for (int d = 0; d < dim; ++d) atomicAdd(p + d * b + d, (VT)(E.vol[k] * rho));
         }

@@ -124,6 +124,10 @@ bool Disc::check_err_word(cudaStream_t s) {
     int err = 0;
     if (!cuda_ok(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "error word")) return false;
     if (!cuda_ok(cudaStreamSynchronize(s), "sync")) return false;
+    if (err & 4) {
+        cudaMemsetAsync(d_err, 0, sizeof(int), s);
+        return fail(NSFV1_ERR_ARGUMENT, "an index out of range was skipped (bounds-checked build)");
+    }
     if (err & 1) {
         cudaMemsetAsync(d_err, 0, sizeof(int), s);
         return fail(NSFV1_ERR_GEOMETRY, "GetLinearProfileSkewedUpwindShapes: Cannot find cut side.");
@@ -504,6 +508,16 @@ bool side_bf_normals(int dim, int nco, const double (*x)[3], const double* elemC
 
 extern "C" {
 
+int nsfv1_add_dirichlet(nsfv1_disc* h, int64_t n, const int32_t* dofs, const double* values) {
+    NSFV1_H;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "add_dirichlet: no mesh"); return D->status; }
+    if (n < 0 || (n > 0 && (!dofs || !values))) { D->fail(NSFV1_ERR_ARGUMENT, "add_dirichlet: bad arguments"); return D->status; }
+    const int b = D->dim + 1;
+    for (int64_t k = 0; k < n; ++k)
+        if (dofs[k] < 0 || dofs[k] >= D->nNodes * b) { D->fail(NSFV1_ERR_ARGUMENT, "Dirichlet dof out of range"); return D->status; }
+    return merge_dirichlet(h, D, std::vector<int32_t>(dofs, dofs + n), std::vector<double>(values, values + n));
+}
+
 int nsfv1_add_wall(nsfv1_disc* h, int64_t n, const int32_t* nodes) {
     NSFV1_H;
     if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "NavierStokesWall::add: no mesh"); return D->status; }
@@ -769,7 +783,7 @@ bool Disc::assemble_defect(const double* u, const double* u_old, double dt, doub
     if (!cuda_ok(cudaMemsetAsync(d, 0, sizeof(double) * nNodes * b, s), "memset defect")) return false;
     for (int c = 0; c < nColors; ++c) {
         AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, d, nullptr,
-                  d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive};
+                  d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive, nNodes, (int64_t)colIdx.size()};
         if (!cuda_ok(launch_defect(roid, P, a, s, asmThreads), "defect kernel")) return false;
     }
     if (!cuda_ok(launch_bnd_flux(b, nNodes, u_old ? dt : 1.0, d_bndFlux, d, s), "inflow flux")) return false;
@@ -791,7 +805,7 @@ bool Disc::assemble_defect_jacobian(const double* u, const double* u_old, double
     if (!cuda_ok(cudaMemsetAsync(vals, 0, colIdx.size() * b * b * vsize, s), "memset jacobian")) return false;
     for (int c = 0; c < nColors; ++c) {
         AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, d, vals,
-                  d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive};
+                  d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive, nNodes, (int64_t)colIdx.size()};
         if (!cuda_ok(launch_defect_jacobian(roid, P, a, prec, s, asmThreads), "defect+jacobian kernel")) return false;
     }
     if (!cuda_ok(launch_bnd_flux(b, nNodes, u_old ? dt : 1.0, d_bndFlux, d, s), "inflow flux")) return false;
@@ -812,7 +826,7 @@ bool Disc::assemble_jacobian(const double* u, const double* u_old, double dt, vo
     if (!cuda_ok(cudaMemsetAsync(vals, 0, bytes, s), "memset jacobian")) return false;
     for (int c = 0; c < nColors; ++c) {
         AsmArgs a{d_coords, d_conn, d_elemBlk, d_colorElems + colorPtr[c], colorPtr[c + 1] - colorPtr[c], d_err, u, u_old, nullptr, vals,
-                  d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive};
+                  d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive, nNodes, (int64_t)colIdx.size()};
         if (!cuda_ok(launch_jacobian(roid, P, a, prec, s, asmThreads), "jacobian kernel")) return false;
     }
     if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, nullptr, vals, prec, s), "dirichlet")) return false;

@@ -23,6 +23,8 @@ struct AsmArgs {
     const double* nuElem;     // per-element kinematic viscosity, or null (the disc's constant)
     const int32_t* elemInst;  // per-element instance id, or null (no instance skipping)
     const int32_t* instActive;// per-instance flag: elements of inactive instances are skipped
+    int64_t nNodes = 0;       // index bounds checked by a build with NSFV1_BOUNDS_CHECK
+    int64_t nnzb = 0;
 };
 
 // Batched element-local callbacks (no global scatter).

@@ -141,6 +141,12 @@ class NavierStokesFV1:
         values = np.ascontiguousarray(values, dtype=np.float64)
         self._c(self._lib.nsfv1_set_dirichlet(self._h, dofs.size, dofs.ctypes.data, values.ctypes.data))
 
+    def add_dirichlet(self, dofs, values) -> None:
+        """Appends Dirichlet rows (later values of the same unknown win; nsfv1_add_dirichlet)."""
+        dofs = np.ascontiguousarray(dofs, dtype=np.int32)
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        self._c(self._lib.nsfv1_add_dirichlet(self._h, dofs.size, dofs.ctypes.data, values.ctypes.data))
+
     def clear_boundary(self) -> None:
         """Removes every Dirichlet row and inflow flux (nsfv1_clear_boundary)."""
         self._c(self._lib.nsfv1_clear_boundary(self._h))

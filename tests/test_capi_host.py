@@ -166,3 +166,12 @@ def test_pac_upwind_needs_an_upwind_and_a_stabilisation():
     d.set_stabilization("fields")
     d.set_pac_upwind(True)
     d.set_pac_upwind(False)   # changes nothing, as in the reference
+
+
+def test_bounds_checked_assembly_compiles(tmp_path):
+    """The NSFV1_BOUNDS_CHECK variant of the assembly kernels (index checks that set
+    an error bit instead of trapping) builds for sm_103a."""
+    from plugin_navierstokes_gb300 import build
+
+    obj = build.compile_bounds_checked(tmp_path / "assemble_bc.o")
+    assert obj.exists() and obj.stat().st_size > 0
