@@ -391,6 +391,17 @@ def main():
     except OSError:
         pass
     traffic = prof.get("defect_jacobian_f64_bytes_per_assembly")
+    # FP64-pipe roofline of the fused pass: FP64 instructions per element (ncu instruction mix,
+    # profiles/) x elements over this run's time, against one warp instruction per 16 cycles per SM
+    fp64_pipe = None
+    if prof.get("fp64_inst_per_element"):
+        props = torch.cuda.get_device_properties(dev)
+        sm_mhz = 2070.0   # maximum SM clock of GB300 (the clock samples of this run are in "clocks")
+        peak_wi = props.multi_processor_count * sm_mhz * 1e6 / 16.0
+        ach_wi = prof["fp64_inst_per_element"] * n_el / 32.0 / (ms64 * 1e-3)
+        fp64_pipe = {"achieved_warp_inst_per_s": ach_wi, "peak_warp_inst_per_s": peak_wi, "frac": ach_wi / peak_wi,
+                     "fp64_inst_per_element": prof["fp64_inst_per_element"], "sm_mhz": sm_mhz,
+                     "source": "FP64 instruction count per element from ncu (profiles/k_defect_jacobian_hex_fp64.md)"}
     traffic32 = prof.get("jacobian_f32_bytes_per_assembly")
 
     cpu, check = None, None
@@ -431,8 +442,8 @@ def main():
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "traffic_source": prof.get("source_f64"),
                          "algorithmic_bytes": alg_bytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
-                         "fp64_pipe_active_frac": prof.get("fp64_pipe_active_frac"),
-                         "note": "FP64-pipe bound (GB300: 2 FP64 lanes per clock per SM)"},
+                         "fp64_pipe": fp64_pipe,
+                         "note": "FP64-pipe bound (GB300: 2 FP64 lanes per clock per SM); HBM traffic runs underneath"},
             "cpu_baseline": cpu,
             "gpu_launches": (launches64["ours"] * args.steps) if launches64.get("ours") is not None else None,
             "gpu_launches_per_step": {"f64": launches64, "f32_mode": launches32},
@@ -546,7 +557,8 @@ def run_solves(args):
         tRe, tlid = cavity_draws(2048, 4)
         coords, targets, cond, tres = generate_training_set(tRe, tlid, N=128, batch=256, cluster_size=16)
         tgen = time.perf_counter() - t0
-        model = CoordinateMLP(max_points=65536, max_slots=64, seed=4)
+        # one slot holds a whole instance: the capacity covers the largest mesh of the batch
+        model = CoordinateMLP(max_points=max(65536, int((np.max(N) + 1) ** 2)), max_slots=64, seed=4)
         t0 = time.perf_counter()
         hist = model.train(coords, targets, cond, steps=6000, slots=64, points_per_slot=1024, lr=2e-3, lr_final=2e-5, seed=4)
         torch.cuda.synchronize()

@@ -958,59 +958,103 @@ __device__ __forceinline__ bool elem_def_A(const DiscParams& P, const Elem<ROID,
 // ---------------------------------------------------------------------------
 // PAC: compile the stabilisation-as-upwind branches (set_pac_upwind); without it
 // those branches cost registers in every configuration
-template <int ROID, typename T, bool PAC, class Sink>
-__device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const IpGeo<T>& G, const IpState<ROID, T>& S,
-                                           const int ip, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
-                                           const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], const T scale, Sink& sink, const T nu) {
+// Per-SCVF factors of the Jacobian blocks (everything the block of one column
+// corner needs besides the reference-element tables).
+template <int ROID, typename T>
+struct JacIp {
+    static constexpr int nsh = Ref<ROID>::nsh;
+    int from, to;
+    T n[3], JtInv[3][3], StdVel[3], UpwindVel[3];
+    T upC[nsh], upS[nsh], dnS[nsh];
+    T nuL, nsvcl, nsvdl, idiag;
+    T pw, ppe, w, riVn;
+};
+
+template <int ROID, typename T, bool PAC>
+__device__ __forceinline__ void jac_ip_factors(const DiscParams& P, const IpGeo<T>& G, const IpState<ROID, T>& S, const int ip,
+                                               const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
+                                               const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], const T nu, JacIp<ROID, T>& J) {
     using R = Ref<ROID>;
-    constexpr int dim = R::dim, nsh = R::nsh, b = R::b, Pc = dim;
+    constexpr int dim = R::dim, nsh = R::nsh;
     const T rho = T(P.rho);
+    T w = T(1), prod = T(0), Vn = T(0);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) J.UpwindVel[d] = T(0);
+#pragma unroll
+    for (int d = 0; d < dim; ++d) Vn += S.StdVel[d] * G.n[d];
+    const bool pac = PAC && !P.stokes && P.pac;
+    const bool fullNewton = !P.stokes && P.fullNewton != 0.0;
+    if (!P.stokes) {
+        if (pac) {
+            // the stabilised velocity is the upwind velocity (navier_stokes_fv1.cpp:382-384); the
+            // Jacobian needs it only for the exact-Jacobian terms
+            if (fullNewton) {
+                T gradVel[3][3], gradP[3];
+                ip_gradients<ROID, T>(G, ip, u, gradVel, gradP);
+                stab_velocity<ROID, T>(P, S, ip, u, uo, gradVel, gradP, rho, nullptr, J.UpwindVel);
+            }
+        } else {
+#pragma unroll
+            for (int d = 0; d < dim; ++d) {
+                T s = T(0);
+#pragma unroll
+                for (int sh = 0; sh < nsh; ++sh) s += S.upC[sh] * u[d][sh];
+                J.UpwindVel[d] = s;
+            }
+        }
+        if (P.peclet) w = peclet_blend<ROID, T>(G, S.StdVel, nu, J.UpwindVel);
+        prod = Vn * rho;
+    }
+    J.from = G.from; J.to = G.to;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        J.n[d] = G.n[d]; J.StdVel[d] = S.StdVel[d];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) J.JtInv[d][c] = G.JtInv[d][c];
+    }
+#pragma unroll
+    for (int k = 0; k < nsh; ++k) { J.upC[k] = S.upC[k]; J.upS[k] = S.upS[k]; J.dnS[k] = S.dnS[k]; }
+    J.nuL = S.nuL; J.nsvcl = S.nsvcl; J.nsvdl = S.nsvdl; J.idiag = S.idiag;
+    J.pw = prod * w; J.ppe = prod * (T(1) - w); J.w = w;
+    J.riVn = rho * S.idiag * Vn;
+}
+
+// The b x b block of SCVF ip and column corner k (added to row 'from', subtracted
+// from row 'to' by the caller), from the SCVF's factors.
+template <int ROID, typename T, bool PAC>
+__device__ __forceinline__ void jac_block(const DiscParams& P, const JacIp<ROID, T>& Jf, const int ip, const int k, const T nu,
+                                          T (&B)[Ref<ROID>::b][Ref<ROID>::b]) {
+    using R = Ref<ROID>;
+    constexpr int dim = R::dim, Pc = dim;
+    const T rho = T(P.rho), irho = T(1) / rho;
     const T mnr = T(-1.0) * nu * rho;
+    const bool pac = PAC && !P.stokes && P.pac;
+    const bool fullNewton = !P.stokes && P.fullNewton != 0.0;
+    const T idiag = Jf.idiag, ri = rho * idiag, riVn = Jf.riVn, pw = Jf.pw, ppe = Jf.ppe, w = Jf.w, ppr = -ri * irho;
+    const T fr = T(P.fullNewton) * rho;
+    T mn[3], rin[3], nrho[3];
+#pragma unroll
+    for (int d = 0; d < dim; ++d) { mn[d] = mnr * Jf.n[d]; rin[d] = ri * Jf.n[d]; nrho[d] = Jf.n[d] * rho; }
+    const auto& S = Jf;
+    const T (&UpwindVel)[3] = Jf.UpwindVel;
+    struct { const T (&n)[3]; const T (&JtInv)[3][3]; } G{Jf.n, Jf.JtInv};
     {
-        T UpwindVel[3] = {T(0), T(0), T(0)};
-        T w = T(1), prod = T(0), Vn = T(0);
+        {
+            T g[3];
+            {
+                const auto& tb = tab<ROID, T>();
 #pragma unroll
-        for (int d = 0; d < dim; ++d) Vn += S.StdVel[d] * G.n[d];
-        const bool pac = PAC && !P.stokes && P.pac;
-        const bool fullNewton = !P.stokes && P.fullNewton != 0.0;
-        if (!P.stokes) {
-            if (pac) {
-                // the stabilised velocity is the upwind velocity (navier_stokes_fv1.cpp:382-384); the
-                // Jacobian needs it only for the exact-Jacobian terms
-                if (fullNewton) {
-                    T gradVel[3][3], gradP[3];
-                    ip_gradients<ROID, T>(G, ip, u, gradVel, gradP);
-                    stab_velocity<ROID, T>(P, S, ip, u, uo, gradVel, gradP, rho, nullptr, UpwindVel);
-                }
-            } else {
+                for (int r = 0; r < dim; ++r) {
+                    T sacc = T(0);
 #pragma unroll
-                for (int d = 0; d < dim; ++d) {
-                    T s = T(0);
-#pragma unroll
-                    for (int sh = 0; sh < nsh; ++sh) s += S.upC[sh] * u[d][sh];
-                    UpwindVel[d] = s;
+                    for (int c = 0; c < dim; ++c) sacc += G.JtInv[r][c] * T(tb.ipLGrad[ip][k][c]);
+                    g[r] = sacc;
                 }
             }
-            if (P.peclet) w = peclet_blend<ROID, T>(G, S.StdVel, nu, UpwindVel);
-            prod = Vn * rho;
-        }
-        const T idiag = S.idiag, irho = T(1) / rho;
-        const T ri = rho * idiag;
-        // per-SCVF factors of the column loop
-        T mn[3], rin[3], nrho[3];
-#pragma unroll
-        for (int d = 0; d < dim; ++d) { mn[d] = mnr * G.n[d]; rin[d] = ri * G.n[d]; nrho[d] = G.n[d] * rho; }
-        const T riVn = ri * Vn, pw = prod * w, ppe = prod * (T(1) - w), ppr = -ri * irho;
-        const T fr = T(P.fullNewton) * rho;
-#pragma unroll
-        for (int k = 0; k < nsh; ++k) {
-            T g[3];
-            ip_grad<ROID, T>(G, ip, k, g);
             const T N = ipN<ROID, T>(ip, k);
             T gn = T(0), Vg = T(0);
 #pragma unroll
             for (int d = 0; d < dim; ++d) { gn += g[d] * G.n[d]; Vg += S.StdVel[d] * g[d]; }
-            T B[b][b];
             // diffusion: -nu rho ((g.n) I + g (x) n)
             T dd = mnr * gn;
             // convection (fixpoint part) on the diagonal: the upwind shape, the Peclet blend
@@ -1110,15 +1154,30 @@ __device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const IpGeo<T>& 
                     }
                 }
             }
-            if (scale != T(1)) {
-#pragma unroll
-                for (int r = 0; r < b; ++r)
-#pragma unroll
-                    for (int c = 0; c < b; ++c) B[r][c] *= scale;
-            }
-            sink.add(G.from, k, B, true);
-            sink.add(G.to, k, B, false);
         }
+    }
+}
+
+template <int ROID, typename T, bool PAC, class Sink>
+__device__ __forceinline__ void scvf_jac_A(const DiscParams& P, const IpGeo<T>& G, const IpState<ROID, T>& S,
+                                           const int ip, const T (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
+                                           const T (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], const T scale, Sink& sink, const T nu) {
+    using R = Ref<ROID>;
+    constexpr int nsh = R::nsh, b = R::b;
+    JacIp<ROID, T> Jf;
+    jac_ip_factors<ROID, T, PAC>(P, G, S, ip, u, uo, nu, Jf);
+#pragma unroll
+    for (int k = 0; k < nsh; ++k) {
+        T B[b][b];
+        jac_block<ROID, T, PAC>(P, Jf, ip, k, nu, B);
+        if (scale != T(1)) {
+#pragma unroll
+            for (int r = 0; r < b; ++r)
+#pragma unroll
+                for (int c = 0; c < b; ++c) B[r][c] *= scale;
+        }
+        sink.add(Jf.from, k, B, true);
+        sink.add(Jf.to, k, B, false);
     }
 }
 
