@@ -132,6 +132,16 @@ def cpu_baseline_run(roid, X, C, U, nthreads):
     return C.shape[0] / dt, o, Dref, Jref
 
 
+def measured_peak():
+    """(HBM GB/s, source): the measured copy bandwidth of this GPU type, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+        return float(peaks["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
 def rel_err(a, b):
     """max |a - b| / max |b| over whole arrays (the parity tests' measure), in chunks."""
     import numpy as np
@@ -597,10 +607,14 @@ def run_solves(args):
     stats = lambda r: {"converged": int(sum(x["status"] == 0 for x in r)), "newton_its_mean": float(np.mean([x["iterations"] for x in r])),
                        "newton_its_max": int(max(x["iterations"] for x in r)),
                        "linear_its_mean": float(np.mean([x["linear_iterations"] for x in r]))}
-    # learned workload: warm start + FP32 Jacobian + exact Jacobian + adaptive tolerances; the uneven
-    # batch: FP32 Jacobian with the reference's Newton options (the exact-Jacobian variant costs
-    # more on its 192^2 and 256^2 instances, see the ablation)
-    main = setting(cb_fast, "f32", "learned", FAST_FORCING) if learned else setting(cb_plain, "f32", "zero", 0.0)
+    # learned workload (uniform 128^2): warm start + FP32 Jacobian + exact Jacobian + adaptive
+    # tolerances; the uneven batch: FP32 Jacobian with the reference's Newton options, from the warm
+    # start with --warm-start learned (the exact-Jacobian variant costs more on its 192^2 and 256^2
+    # instances, see the ablations)
+    if args.workload == "learned":
+        main = setting(cb_fast, "f32", "learned", FAST_FORCING)
+    else:
+        main = setting(cb_plain, "f32", "learned" if learned else "zero", 0.0)
     if learned and args.workload == "batched":
         wl += "; main path from the warm start of the network trained on 2048 solves of 128^2 cavities (seed 4)"
     for _ in range(args.warmup):
@@ -625,9 +639,13 @@ def run_solves(args):
         ablations += [("f32_exact_forcing", setting(cb_fast, "f32", "zero", FAST_FORCING))]
     else:
         ablations += [("f32_plain_newton", setting(cb_plain, "f32", "zero", 0.0))]
-        ablations += [("f32_exact_forcing_zero_init", setting(cb_fast, "f32", "zero", FAST_FORCING)),
-                      ("learned_f32_plain_newton", setting(cb_plain, "f32", "learned", 0.0)),
-                      ("learned_f64_exact_forcing", setting(cb_fast, "f64", "learned", FAST_FORCING))]
+        ablations += [("f32_exact_forcing_zero_init", setting(cb_fast, "f32", "zero", FAST_FORCING))]
+        if args.workload == "learned":
+            ablations += [("learned_f32_plain_newton", setting(cb_plain, "f32", "learned", 0.0))]
+        else:
+            ablations += [("learned_f32_exact_forcing", setting(cb_fast, "f32", "learned", FAST_FORCING))]
+        ablations += [("learned_f64_exact_forcing", setting(cb_fast, "f64", "learned", FAST_FORCING)),
+                      ("learned_f64_plain_newton", setting(cb_plain, "f64", "learned", 0.0))]
     for name, st in ablations:
         solve_once(st)
         t1, r1 = timed(st, 1)
@@ -740,6 +758,29 @@ RTOL_STEP = 1e-6
 ATOL_FRACTION = 1e-5
 
 
+def _transient_cpu_sample(nu, dt, nthreads):
+    """The oracle's first backward-Euler step (Newton + block-Jacobi BiCGStab) on a 128^2 grid
+    of the transient workload's construction; returns (seconds, triangles, Newton result)."""
+    import numpy as np
+
+    import oracle
+    from plugin_navierstokes_gb300 import mesh
+
+    rs, rX, rC = mesh.jittered_triangles(128, seed=2)
+    rd, rv = mesh.cavity_dirichlet(rX, 1.0)
+    o = oracle.Oracle(2)
+    o.set_kinematic_viscosity(nu)
+    o.set_upwind("full")
+    o.set_stabilization("fields")
+    o.set_mesh(rs, rX, rC)
+    o.set_dirichlet(rd, rv)
+    U0 = np.zeros(rX.shape[0] * 3)
+    U0[rd] = rv
+    t0 = time.perf_counter()
+    _, st = o.newton(U0.copy(), U_old=U0, dt=dt, rtol=1e-8, lin_rtol=1e-4, lin_maxit=20000, nthreads=nthreads)
+    return time.perf_counter() - t0, int(rC.shape[0]), st
+
+
 def run_transient(args):
     import numpy as np
     import torch
@@ -753,31 +794,19 @@ def run_transient(args):
           f"nu={nu}, full upwind + FIELDS, lid-driven cavity walls")
     roid, X, C = mesh.jittered_triangles(n_cells, seed=2)
     dofs, vals = mesh.cavity_dirichlet(X, 1.0)
+    nthreads = os.cpu_count() or 1
     if args.impl == "reference":
         if rank != 0:
             return 0
-        import oracle
-
         # bounded sample: the first time step on a 128^2 grid of the same construction, scaled by elements
-        rs, rX, rC = mesh.jittered_triangles(128, seed=2)
-        rd, rv = mesh.cavity_dirichlet(rX, 1.0)
-        o = oracle.Oracle(2)
-        o.set_kinematic_viscosity(nu)
-        o.set_upwind("full")
-        o.set_stabilization("fields")
-        o.set_mesh(rs, rX, rC)
-        o.set_dirichlet(rd, rv)
-        U0 = np.zeros(rX.shape[0] * 3)
-        U0[rd] = rv
-        t0 = time.perf_counter()
-        o.newton(U0.copy(), U_old=U0, dt=dt, rtol=1e-8, lin_rtol=1e-4, lin_maxit=20000)
-        el = time.perf_counter() - t0
-        v = (rC.shape[0] / C.shape[0]) / el
+        el, tri, _ = _transient_cpu_sample(nu, dt, nthreads)
+        v = (tri / C.shape[0]) / el
         line = {"impl": "reference", "metric": "time steps/s", "value": v, "unit": "steps/s", "n_gpus": args.gpus, "steps": 1,
                 "warmup": 0, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "config": {"workload": wl},
-                "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
-                                 "sample": f"first time step on the 128^2 grid of the same construction ({el:.1f} s), scaled by elements"},
+                "cpu_baseline": {"value": v, "unit": "steps/s", "cores": nthreads, "kind": "port",
+                                 "sample": f"first time step on the 128^2 grid of the same construction ({el:.1f} s, oracle Newton, "
+                                           f"OpenMP assembly), scaled by elements"},
                 "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return 0
@@ -798,15 +827,18 @@ def run_transient(args):
     d.assemble_defect(u0, D0, u0, dt)
     atol = ATOL_FRACTION * float(D0.norm().item())
 
+    def step(u, prec):
+        uo = u.clone()
+        return d.newton_solve(u, uo, dt=dt, rtol=RTOL_STEP, atol=atol, lin_rtol=1e-4, lin_max_iter=5000, jacobian_prec=prec,
+                              linear_solver="bicgstab")
+
     def march(prec, k):
         u = u0.clone()
         its, lin, times = [], [], []
         for _ in range(k):
-            uo = u.clone()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            r = d.newton_solve(u, uo, dt=dt, rtol=RTOL_STEP, atol=atol, lin_rtol=1e-4, lin_max_iter=5000, jacobian_prec=prec,
-                               linear_solver="bicgstab")
+            r = step(u, prec)
             e1.record()
             e1.synchronize()
             times.append(e0.elapsed_time(e1) * 1e-3)
@@ -814,7 +846,21 @@ def run_transient(args):
             lin.append(r["linear_iterations"])
         return u, its, lin, times
 
-    march("f32", min(max(args.warmup, 3), n_steps))
+    n_warm = min(max(args.warmup, 3), n_steps)
+    # the warm-up steps run under the profiler interface: kernel launches per Krylov iteration
+    launch = None
+    march("f32", n_warm)
+    if not args.no_launch_count:
+        wres = {}
+
+        def one_step():
+            wres["r"] = march("f32", 1)
+
+        count_launches(one_step)   # the first profiling session can miss the first launches
+        launch = count_launches(one_step)
+        launch["steps"] = 1
+        launch["linear_its"] = int(sum(wres["r"][2]))
+        launch["newton_its"] = int(sum(wres["r"][1]))
     with ClockSampler(local) as clk:
         u32, its32, lin32, t32 = march("f32", n_steps)
     u64, its64, lin64, t64 = march("f64", n_steps)
@@ -830,24 +876,96 @@ def run_transient(args):
     e0.record()
     u = hu.to(dev, non_blocking=True)
     for _ in range(n_steps):
-        uo = u.clone()
-        d.newton_solve(u, uo, dt=dt, rtol=RTOL_STEP, atol=atol, lin_rtol=1e-4, lin_max_iter=5000, jacobian_prec="f32",
-                       linear_solver="bicgstab")
+        step(u, "f32")
     hout.copy_(u, non_blocking=True)
     e1.record()
     e1.synchronize()
     e2e = n_steps / (e0.elapsed_time(e1) * 1e-3)
-    line = {"metric": "time steps/s", "value": value, "unit": "steps/s", "n_gpus": 1, "steps": n_steps, "warmup": max(args.warmup, 3),
+
+    # full-size parity at the second time step's first Newton iterate (u = u_old = the state after the
+    # first step, where the defect is dt A(u), not the cancellation left at a converged iterate): FP64
+    # defect, FP64 and FP32 Jacobians, pattern and colouring against the FP64 oracle
+    u1 = u0.clone()
+    step(u1, "f32")
+    u0 = u1.clone()
+    info = d.pattern_info()
+    nnzb = int(info["nnz_blocks"])
+    Dg = torch.empty_like(u1)
+    J64 = torch.empty(nnzb * 9, dtype=torch.float64, device=dev)
+    J32 = torch.empty(nnzb * 9, dtype=torch.float32, device=dev)
+    d.assemble_defect(u1, Dg, u0, dt)
+    d.assemble_jacobian(u1, J64, u0, dt)
+    d.assemble_jacobian(u1, J32, u0, dt)
+    torch.cuda.synchronize()
+    check = None
+    if not args.no_cpu_baseline:
+        import oracle
+
+        o = oracle.Oracle(2)
+        o.set_kinematic_viscosity(nu)
+        o.set_upwind("full")
+        o.set_stabilization("fields")
+        o.set_mesh(roid, X, C)
+        o.set_dirichlet(dofs, vals)
+        Dref, Jref = o.assemble(u1.cpu().numpy(), U_old=u0.cpu().numpy(), dt=dt, nthreads=nthreads)
+        check = oracle_check(o, d, Dref, Jref, Dg.cpu().numpy(), J64.cpu().numpy(), J32.cpu().numpy())
+        check["state"] = "first Newton iterate of the second time step (u = u_old = the first step's solution)"
+        del Jref, o
+    del J64
+    # the dominant kernel: the FP32-matrix x FP64-vector block SpMV of BiCGStab, timed alone
+    x = u1.clone()
+    y = torch.empty_like(x)
+    for _ in range(3):
+        d.bsr_mv(J32, x, y)
+    torch.cuda.synchronize()
+    k_mv = 50
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(k_mv):
+        d.bsr_mv(J32, x, y)
+    e1.record()
+    e1.synchronize()
+    mv_s = e0.elapsed_time(e1) * 1e-3 / k_mv
+    nrows = X.shape[0]
+    mv_bytes = nnzb * (9 * 4 + 4) + (nrows + 1) * 4 + 2 * n * 8
+    peak, peak_src = measured_peak()
+    prof = {}
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            prof = json.load(f)
+    except OSError:
+        pass
+    mv_traffic = prof.get("spmv_tri1024_f32_bytes") if n_cells == 1024 else None
+    roofline = {"bound": "hbm", "kernel": "k_bsr_mv<float, double, 3, 8> (FP32 Jacobian x FP64 vector, the BiCGStab SpMV)",
+                "achieved": mv_bytes / mv_s / 1e9, "peak": peak, "unit": "GB/s", "frac": mv_bytes / mv_s / 1e9 / peak,
+                "traffic": mv_traffic, "traffic_source": prof.get("source_spmv") if mv_traffic else None,
+                "algorithmic_bytes": mv_bytes, "us_per_launch": mv_s * 1e6, "peak_source": peak_src,
+                "note": "algorithmic bytes = FP32 blocks + column indices + row pointers + x read + y written"}
+    cpu = None
+    if not args.no_cpu_baseline:
+        el, tri, _ = _transient_cpu_sample(nu, dt, nthreads)
+        cv = (tri / C.shape[0]) / el
+        cpu = {"value": cv, "unit": "steps/s", "cores": nthreads, "kind": "port",
+               "sample": f"first time step on the 128^2 grid of the same construction ({el:.1f} s, oracle Newton, OpenMP assembly), "
+                         f"scaled by elements"}
+    gpu_launches = None
+    if launch and launch.get("ours") and launch["linear_its"]:
+        # launches scale with the Krylov iterations; the timed march's count from the warm-up's rate
+        gpu_launches = int(round(launch["ours"] * sum(lin32) / launch["linear_its"]))
+    line = {"metric": "time steps/s", "value": value, "unit": "steps/s", "n_gpus": 1, "steps": n_steps, "warmup": n_warm,
             "ms_per_step": 1e3 * sec / n_steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64 defect / f32 jacobian", "data": "synthetic (seeded jittered grid)",
             "config": {"workload": wl, "triangles": int(C.shape[0]), "nodes": int(X.shape[0]),
                        "l2": "inputs larger than L2",
                        "mixed": {"newton_its": its32, "linear_its": lin32, "seconds": sec},
                        "all_f64": {"newton_its": its64, "linear_its": lin64, "seconds": sum(t64), "steps_per_s": n_steps / sum(t64)},
-                       "final_state_rel_diff_vs_all_f64": rel_diff},
+                       "final_state_rel_diff_vs_all_f64": rel_diff, "oracle_check": check},
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": hu.numel() * 8 / n_steps,
                     "d2h_bytes_per_step": hout.numel() * 8 / n_steps},
-            "roofline": None, "cpu_baseline": None, "gpu_launches": None, "clocks": clk.summary()}
+            "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": gpu_launches,
+            "gpu_launches_measured": launch, "clocks": clk.summary()}
+    if launch:
+        line["gpu_launches_note"] = "the first time step profiled (untimed), scaled to the timed steps by Krylov iterations"
     print(json.dumps(line))
     return 0
 

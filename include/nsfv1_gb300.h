@@ -81,8 +81,15 @@ int nsfv1_set_laplace(nsfv1_disc* h, int on);
 int nsfv1_set_peclet_blend(nsfv1_disc* h, int on);
 /* NavierStokesFV1::set_upwind(const std::string&) (navier_stokes_fv1.h:213-215,
  * ids of CreateNavierStokesUpwind, upwind_interface.cpp:43-62): "no", "full",
- * "skewed", "lps" / "linearprofileskewed" (case-insensitive, trimmed). The
- * object is shared with a stabilisation that has no upwind yet. */
+ * "skewed", "lps" / "linearprofileskewed", "pos" / "positive" (case-insensitive,
+ * trimmed). The object is shared with a stabilisation that has no upwind yet.
+ * The positive upwind (upwind.cpp:643-786) has shapes at the other integration
+ * points of an element, which selects the non-diagonal FIELDS / FLOW branches
+ * (stabilization.cpp:244-403, 589-771); its element path needs a device
+ * workspace of 12 KB per thread for hexahedra at 64 threads per SM (120 MB on
+ * 152 SMs), allocated with the mesh or at the first device use after this call. A singular ip-ip system of
+ * that branch gives NSFV1_ERR_BREAKDOWN ("Could not compute inverse."). The
+ * regular upwind ("reg") is not provided. */
 int nsfv1_set_upwind(nsfv1_disc* h, const char* name);
 /* NavierStokesFV1::set_stabilization(name[, diffLength]) (navier_stokes_fv1.h:190-199,
  * CreateNavierStokesStabilization stabilization.cpp:46-57, set_diffusion_length
@@ -100,7 +107,8 @@ int nsfv1_set_stabilization(nsfv1_disc* h, const char* name, const char* diff_le
  * stabilisation.) */
 int nsfv1_set_pac_upwind(nsfv1_disc* h, int on);
 /* INavierStokesFV1Stabilization::set_upwind with an upwind object of its own
- * (stabilization.h:91-95, registered at register_fv1.cpp:246-249). */
+ * (stabilization.h:91-95, registered at register_fv1.cpp:246-249); ids as for
+ * nsfv1_set_upwind. */
 int nsfv1_set_stabilization_upwind(nsfv1_disc* h, const char* name);
 
 /* ---- mesh, sparsity pattern, colouring ---------------------------------- */
@@ -154,6 +162,21 @@ int nsfv1_add_wall(nsfv1_disc* h, int64_t n_nodes, const int32_t* nodes);
  *    the implicit-Euler defect, like every right-hand side.
  * A side must belong to exactly one element (NSFV1_ERR_ARGUMENT otherwise). */
 int nsfv1_add_inflow(nsfv1_disc* h, int64_t n_sides, int side_nco, const int32_t* side_nodes, const double* vel);
+/* NavierStokesNoNormalStressOutflowFV1::add(subsets) (incompressible/fv1/bnd/
+ * no_normal_stress_outflow_fv1.cpp:343-504) on the given boundary sides (as for
+ * nsfv1_add_inflow): every corner's part of a side (the FV1 boundary face, with
+ * its outward area-weighted normal n and the P1 shapes and gradients at its
+ * integration point) adds to the corner's rows
+ *  - momentum: the viscous flux -nu rho ((grad u + grad u^T) n) without its
+ *    component along n (v - (v.n) n with the area-weighted n, as the reference
+ *    computes it), and the outgoing convective flux max(rho u.n, 0) u (not with
+ *    the Stokes option);
+ *  - continuity: rho u.n;
+ * and the Jacobian: the viscous and continuity terms exactly, the convective one
+ * with the flux frozen, as the reference's add_jac_A_elem does. Part of every
+ * defect / Jacobian assembly (dt-scaled when transient) until
+ * nsfv1_clear_boundary. Sides accumulate over calls. */
+int nsfv1_add_outflow(nsfv1_disc* h, int64_t n_sides, int side_nco, const int32_t* side_nodes);
 /* removes every Dirichlet row and inflow flux */
 int nsfv1_clear_boundary(nsfv1_disc* h);
 
@@ -187,12 +210,56 @@ int nsfv1_assemble_defect_jacobian(nsfv1_disc* h, const double* u, const double*
 int nsfv1_elem_batch(nsfv1_disc* h, int elem_type, int64_t n, const double* corners, const double* u, const double* u_old,
                      double dt, double* defA, double* jacA, double* defM, double* jacM, double* rhs, void* stream);
 
+/* ---- data exports ---------------------------------------------------------
+ * NavierStokesFV1's data exports (navier_stokes_fv1.cpp:894-1491, registered per
+ * element type at :1573-1577): ex_nodal_velocity, ex_velocity_grad,
+ * ex_velocity_ip (the stabilised velocity), ex_nodal_pressure, ex_pressure_grad,
+ * for n elements at once (device arrays; layouts as nsfv1_elem_batch):
+ *   points  ip_kind NSFV1_IPS_SCVF: the SCVF integration points (the exports'
+ *           FV1 branch, nip = number of SCVFs); NSFV1_IPS_SCV: the SCV ips = the
+ *           corners (nip = corners); NSFV1_IPS_GIVEN: nip (1..64) local points
+ *           local_ips[nip][dim] (a HOST array), the exports' general branch;
+ *   values  [n][nip][vs], vs = dim, dim*dim (row d1: d u_d1 / d x_d2), dim, 1, dim;
+ *   derivs  [n][nip][dim+1][corners][vs] (may be NULL): the derivative of each
+ *           value w.r.t. the element's unknowns (function, corner), as the
+ *           reference fills its vvvDeriv: entries it leaves alone are zero, and
+ *           where it assigns a scalar to a vector entry every component holds it.
+ * Both outputs are overwritten (the reference adds the nodal velocity into the
+ * caller's array). As in the reference, the velocity gradient's general branch
+ * is taken in local (reference-element) coordinates, while the pressure
+ * gradient's is mapped with J^-T at the point. The call waits for its stream. */
+#define NSFV1_EX_VELOCITY       0
+#define NSFV1_EX_VELOCITY_GRAD  1
+#define NSFV1_EX_VELOCITY_IP    2
+#define NSFV1_EX_PRESSURE       3
+#define NSFV1_EX_PRESSURE_GRAD  4
+#define NSFV1_IPS_SCVF          0
+#define NSFV1_IPS_SCV           1
+#define NSFV1_IPS_GIVEN         2
+int nsfv1_export(nsfv1_disc* h, int which, int elem_type, int64_t n, const double* corners, const double* u, const double* u_old, double dt,
+                 int ip_kind, int nip, const double* local_ips, double* values, double* derivs, void* stream);
+
+/* ---- post-processing (incompressible/navier_stokes_tools.h) ----------------
+ * vorticityFV1 (:387-525): vort[n_nodes] = sum over the node's SCVs of |SCV| times
+ * the curl d u_y/dx - d u_x/dy of the P1 velocity at the corner, divided by the
+ * summed |SCV| (the first two velocity components, also in 3D, as the reference's
+ * formula takes them); u[n_nodes * b] on the device. Deterministic (element
+ * colours in order). The call waits for its stream. */
+int nsfv1_vorticity(nsfv1_disc* h, const double* u, double* vort, void* stream);
+/* The value of function fct (0..dim; dim = pressure) of the P1 solution u at n
+ * global points points[n][dim] (device arrays): the first element in mesh order
+ * containing the point, interpolated with the P1 shapes there; NaN outside the
+ * mesh. The point evaluation of DrivenCavityEvalAtPoints / DrivenCavityLinesEval
+ * (:540-729). The call waits for its stream. */
+int nsfv1_eval_points(nsfv1_disc* h, const double* u, int64_t n, const double* points, int fct, double* values, void* stream);
+
 /* The same callbacks with HOST arrays (same layouts): the library stages them
  * through device memory it allocates for the call and returns when the outputs
  * are on the host. For host-side element loops such as a ugcore IElemDisc
  * adapter (navier_stokes_fv1.cpp:1553-1579 registers the reference's). */
 int nsfv1_elem_batch_host(nsfv1_disc* h, int elem_type, int64_t n, const double* corners, const double* u, const double* u_old,
                           double dt, double* defA, double* jacA, double* defM, double* jacM, double* rhs);
+
 
 /* ---- linear algebra on the handle's pattern (device pointers) ------------ */
 

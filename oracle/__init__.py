@@ -58,6 +58,11 @@ def load():
             "ora_add_wall": (c_int, [c_void_p, c_int64, c_void_p]),
             "ora_add_dirichlet": (c_int, [c_void_p, c_int64, c_void_p, c_void_p]),
             "ora_add_inflow": (c_int, [c_void_p, c_int64, c_int, c_void_p, c_void_p]),
+            "ora_vorticity": (c_int, [c_void_p, c_void_p, c_void_p]),
+            "ora_add_outflow": (c_int, [c_void_p, c_int64, c_int, c_void_p]),
+            "ora_eval_points": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int, c_void_p]),
+            "ora_export": (c_int, [c_void_p, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_double, c_int, c_int, c_void_p,
+                                   c_void_p, c_void_p]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)
@@ -124,6 +129,40 @@ class Oracle:
         self._c(self.lib.ora_elem_batch(self.h, roid, ne, corners.ctypes.data, u.ctypes.data, _p(uo), float(dt),
                                         _p(out["defA"]), _p(out["jacA"]), _p(out["defM"]), _p(out["jacM"]), _p(out["rhs"])))
         return {k: v for k, v in out.items() if v is not None}
+
+    def add_outflow(self, sides):
+        """NavierStokesNoNormalStressOutflowFV1 on the given boundary sides [n][nco]."""
+        sides = np.ascontiguousarray(sides, np.int32)
+        self._c(self.lib.ora_add_outflow(self.h, sides.shape[0], sides.shape[1], sides.ctypes.data))
+
+    def vorticity(self, U):
+        """vorticityFV1 of the nodal state U[n_nodes * b] on the mesh: one value per node."""
+        U = np.ascontiguousarray(U, np.float64).ravel()
+        out = np.zeros(self.coords.shape[0])
+        self._c(self.lib.ora_vorticity(self.h, U.ctypes.data, out.ctypes.data))
+        return out
+
+    def eval_points(self, U, points, fct):
+        """Function fct of the nodal state at global points [n][dim] (NaN outside the mesh)."""
+        U = np.ascontiguousarray(U, np.float64).ravel()
+        pts = np.ascontiguousarray(points, np.float64)
+        out = np.zeros(pts.shape[0])
+        self._c(self.lib.ora_eval_points(self.h, U.ctypes.data, pts.shape[0], pts.ctypes.data, int(fct), out.ctypes.data))
+        return out
+
+    def export(self, which, roid, corners, u, u_old=None, dt=0.0, ip_kind=0, local_ips=None, derivs=True):
+        """The disc's data export `which` (EXPORTS index) of n elements: (values [n][nip][vs],
+        derivatives [n][nip][b][nsh][vs] or None); ip_kind 0: SCVF ips, 1: SCV ips, 2: local_ips."""
+        corners = np.ascontiguousarray(corners, np.float64)
+        u = np.ascontiguousarray(u, np.float64)
+        lips = None if local_ips is None else np.ascontiguousarray(local_ips, np.float64)
+        ne, nip, vs, b = corners.shape[0], export_nip(roid, ip_kind, lips), export_size(which, roid), DIM[roid] + 1
+        val = np.zeros((ne, nip, vs))
+        der = np.zeros((ne, nip, b, NSH[roid], vs)) if derivs else None
+        uo = None if u_old is None else np.ascontiguousarray(u_old, np.float64)
+        self._c(self.lib.ora_export(self.h, int(which), roid, ne, corners.ctypes.data, u.ctypes.data, _p(uo), float(dt), int(ip_kind),
+                                    nip if ip_kind == 2 else 0, _p(lips), val.ctypes.data, _p(der)))
+        return val, der
 
     def set_mesh(self, roid, coords, conn):
         self.coords = np.ascontiguousarray(coords, np.float64)
@@ -257,9 +296,22 @@ def load_ref():
                                        c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
         lib.ref_geometry.restype = c_int
         lib.ref_geometry.argtypes = [c_int, c_void_p, c_void_p]
+        lib.ref_export.restype = c_int
+        lib.ref_export.argtypes = [c_int, c_int, c_int64, ctypes.POINTER(RefConfig), c_void_p, c_void_p, c_void_p, c_double, c_int, c_int,
+                                   c_void_p, c_void_p, c_void_p]
         lib.ref_last_error.restype = c_char_p
         _ref_lib = lib
     return _ref_lib
+
+
+def _ref_cfg(cfg: dict):
+    src = cfg.get("source")
+    enc = lambda s: None if s is None else s.encode()
+    return RefConfig(float(cfg.get("nu", 0.01)), float(cfg.get("rho", 1.0)), float(cfg.get("full_newton", 0.0)),
+                     (c_double * 3)(*(list(src) + [0.0] * (3 - len(src)) if src is not None else [0.0, 0.0, 0.0])),
+                     int(src is not None), int(bool(cfg.get("stokes"))), int(bool(cfg.get("laplace"))), int(bool(cfg.get("peclet"))),
+                     int(bool(cfg.get("pac"))), enc(cfg["upwind"]), enc(cfg["stab"]), enc(cfg.get("diff_length")),
+                     enc(cfg.get("stab_upwind")))
 
 
 def ref_elem_batch(roid, cfg: dict, corners, u, u_old=None, dt=0.0, want=("defA", "jacA", "defM", "jacM", "rhs")):
@@ -277,18 +329,44 @@ def ref_elem_batch(roid, cfg: dict, corners, u, u_old=None, dt=0.0, want=("defA"
     for k in ("jacA", "jacM"):
         out[k] = np.zeros((ne, nloc * nloc)) if k in want else None
     uo = None if u_old is None else np.ascontiguousarray(u_old, np.float64)
-    src = cfg.get("source")
-    enc = lambda s: None if s is None else s.encode()
-    c = RefConfig(float(cfg.get("nu", 0.01)), float(cfg.get("rho", 1.0)), float(cfg.get("full_newton", 0.0)),
-                  (c_double * 3)(*(list(src) + [0.0] * (3 - len(src)) if src is not None else [0.0, 0.0, 0.0])),
-                  int(src is not None), int(bool(cfg.get("stokes"))), int(bool(cfg.get("laplace"))), int(bool(cfg.get("peclet"))),
-                  int(bool(cfg.get("pac"))), enc(cfg["upwind"]), enc(cfg["stab"]), enc(cfg.get("diff_length")),
-                  enc(cfg.get("stab_upwind")))
+    c = _ref_cfg(cfg)
     st = lib.ref_elem_batch(roid, ne, ctypes.byref(c), corners.ctypes.data, u.ctypes.data, _p(uo), float(dt), _p(out["defA"]),
                             _p(out["jacA"]), _p(out["defM"]), _p(out["jacM"]), _p(out["rhs"]))
     if st != 0:
         raise RuntimeError(f"reference error {st}: {lib.ref_last_error().decode()}")
     return {k: v for k, v in out.items() if v is not None}
+
+
+# data exports of the disc (navier_stokes_fv1.cpp:894-1491), in the index order of ora_export / ref_export
+EXPORTS = ("velocity", "velocity_grad", "velocity_ip", "pressure", "pressure_grad")
+NSCVF = {2: 3, 3: 4, 4: 6, 8: 12}
+
+
+def export_size(which, roid):
+    dim = DIM[roid]
+    return {0: dim, 1: dim * dim, 2: dim, 3: 1, 4: dim}[int(which)]
+
+
+def export_nip(roid, ip_kind, local_ips=None):
+    return NSCVF[roid] if ip_kind == 0 else NSH[roid] if ip_kind == 1 else int(np.asarray(local_ips).shape[0])
+
+
+def ref_export(which, roid, cfg: dict, corners, u, u_old=None, dt=0.0, ip_kind=0, local_ips=None, derivs=True):
+    """The reference's own data export `which` of n elements (layouts as Oracle.export)."""
+    lib = load_ref()
+    corners = np.ascontiguousarray(corners, np.float64)
+    u = np.ascontiguousarray(u, np.float64)
+    lips = None if local_ips is None else np.ascontiguousarray(local_ips, np.float64)
+    ne, nip, vs, b = corners.shape[0], export_nip(roid, ip_kind, lips), export_size(which, roid), DIM[roid] + 1
+    val = np.zeros((ne, nip, vs))
+    der = np.zeros((ne, nip, b, NSH[roid], vs)) if derivs else None
+    uo = None if u_old is None else np.ascontiguousarray(u_old, np.float64)
+    c = _ref_cfg(cfg)
+    st = lib.ref_export(int(which), roid, ne, ctypes.byref(c), corners.ctypes.data, u.ctypes.data, _p(uo), float(dt), int(ip_kind),
+                        nip if ip_kind == 2 else 0, _p(lips), val.ctypes.data, _p(der))
+    if st != 0:
+        raise RuntimeError(f"reference error {st}: {lib.ref_last_error().decode()}")
+    return val, der
 
 
 def ref_geometry(roid, corners):

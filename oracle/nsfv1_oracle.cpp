@@ -54,7 +54,7 @@ enum { MAXCO = 8, MAXEDGE = 12, MAXSIDE = 6, MAXSCVF = 12 };
 enum { ROID_TRIANGLE = 2, ROID_QUADRILATERAL = 3, ROID_TETRAHEDRON = 4, ROID_HEXAHEDRON = 8 };
 
 // upwind / stabilisation / diffusion-length ids
-enum { UPW_NONE = -1, UPW_NO = 0, UPW_FULL = 1, UPW_SKEWED = 2, UPW_LPS = 3 };
+enum { UPW_NONE = -1, UPW_NO = 0, UPW_FULL = 1, UPW_SKEWED = 2, UPW_LPS = 3, UPW_POS = 4 };
 enum { STAB_NONE = -1, STAB_FIELDS = 0, STAB_FLOW = 1, STAB_WITHOUT = 2 };
 enum { DL_RAW = 0, DL_FIVEPOINT = 1, DL_COR = 2 };
 
@@ -490,12 +490,97 @@ static number vnorm(int dim, const number* a) {
 struct Upwind {
     int type = UPW_NONE;
     number upShapeSh[MAXSCVF][MAXCO], downShapeSh[MAXSCVF][MAXCO];
+    number upShapeIp[MAXSCVF][MAXSCVF], downShapeIp[MAXSCVF][MAXSCVF];
     number upConvLength[MAXSCVF], downConvLength[MAXSCVF];
 
+    // set_shape_ip_flag of the constructors (upwind.h:69-295): only the positive
+    // (and regular) upwinds take values at other integration points
+    bool non_zero_shape_ip() const { return type == UPW_POS; }
+
+    // NavierStokesPositiveUpwind::compute<FV1> (upwind.cpp:643-786): per SCV, every
+    // outflow face takes the SCV's inflow faces (weighted by their share of the
+    // larger of total in- and outflow) as ip shapes and the corner the rest
+    void positive(const FV1Geometry& geo, const number vIPVel[][3], number vUpShapeSh[][MAXCO], number vUpShapeIp[][MAXSCVF],
+                  number vConvLength[]) const {
+        const int dim = geo.dim, nip = geo.nscvf;
+        number massFlux[MAXSCVF];
+        bool hasFlux[MAXSCVF];
+        const number eps = std::numeric_limits<number>::epsilon() * 10;
+        int numNoFlux = 0;
+        for (int ip = 0; ip < nip; ++ip) {
+            const SCVF& scvf = geo.scvf[ip];
+            massFlux[ip] = 0.0;
+            hasFlux[ip] = true;
+            for (int sh = 0; sh < geo.nsh; ++sh) vUpShapeSh[ip][sh] = 0.0;
+            for (int j = 0; j < nip; ++j) vUpShapeIp[ip][j] = 0.0;
+            number normSq = 0;
+            for (int d = 0; d < dim; ++d) normSq += vIPVel[ip][d] * vIPVel[ip][d];
+            if (std::fabs(normSq) <= eps) {
+                vUpShapeSh[ip][scvf.from] = 0.5;
+                vUpShapeSh[ip][scvf.to] = 0.5;
+                hasFlux[ip] = false;
+                ++numNoFlux;
+                continue;
+            }
+            number mf = 0;
+            for (int d = 0; d < dim; ++d) mf += vIPVel[ip][d] * scvf.normal[d];
+            massFlux[ip] = mf;
+            const number vel = std::sqrt(normSq);
+            const number len = vnorm(dim, scvf.normal);
+            if (std::fabs(massFlux[ip] / std::sqrt(vel * len)) <= eps) {
+                vUpShapeSh[ip][scvf.from] = 0.5;
+                vUpShapeSh[ip][scvf.to] = 0.5;
+                hasFlux[ip] = false;
+                ++numNoFlux;
+                continue;
+            }
+        }
+        if (numNoFlux != nip) {
+            for (int sh = 0; sh < geo.nsh; ++sh) {
+                number mIn = 0, mOut = 0;
+                int ips[MAXSCVF], n = 0;
+                number flux[MAXSCVF];
+                for (int ip = 0; ip < nip; ++ip) {
+                    if (!hasFlux[ip]) continue;
+                    const SCVF& scvf = geo.scvf[ip];
+                    if (scvf.from == sh) {
+                        ips[n] = ip; flux[n] = massFlux[ip]; ++n;
+                        mIn += -1.0 * std::min(massFlux[ip], 0.0);
+                        mOut += std::max(massFlux[ip], 0.0);
+                    } else if (scvf.to == sh) {
+                        ips[n] = ip; flux[n] = -1.0 * massFlux[ip]; ++n;
+                        mIn += -1.0 * std::min(-1.0 * massFlux[ip], 0.0);
+                        mOut += std::max(-1.0 * massFlux[ip], 0.0);
+                    }
+                }
+                const number F = std::max(mIn, mOut);
+                for (int i = 0; i < n; ++i) {
+                    if (flux[i] > 0) {
+                        number sum = 0.0;
+                        for (int j = 0; j < n; ++j)
+                            if (flux[j] < 0) sum += vUpShapeIp[ips[i]][ips[j]] = -1.0 * flux[j] / F;
+                        vUpShapeSh[ips[i]][sh] = 1.0 - sum;
+                    }
+                }
+            }
+        }
+        // convection length: distance of the ip from the upwind point the shapes interpolate
+        for (int ip = 0; ip < nip; ++ip) {
+            number up[3] = {0, 0, 0};
+            for (int sh = 0; sh < geo.nsh; ++sh)
+                for (int d = 0; d < dim; ++d) up[d] += vUpShapeSh[ip][sh] * geo.corners[sh][d];
+            for (int j = 0; j < nip; ++j)
+                for (int d = 0; d < dim; ++d) up[d] += vUpShapeIp[ip][j] * geo.scvf[j].globalIP[d];
+            vConvLength[ip] = vdist(dim, geo.scvf[ip].globalIP, up);
+        }
+    }
+
     // INavierStokesUpwind::compute dispatch (upwind_interface.h:243-250)
-    void compute(const FV1Geometry& geo, const number vIPVel[][3], number vUpShapeSh[][MAXCO], number vConvLength[]) const {
+    void compute(const FV1Geometry& geo, const number vIPVel[][3], number vUpShapeSh[][MAXCO], number vUpShapeIp[][MAXSCVF],
+                 number vConvLength[]) const {
         const RefElem& R = ref_elem(geo.roid);
         const int dim = geo.dim;
+        if (type == UPW_POS) { positive(geo, vIPVel, vUpShapeSh, vUpShapeIp, vConvLength); return; }
         for (int ip = 0; ip < geo.nscvf; ++ip) {
             const SCVF& scvf = geo.scvf[ip];
             if (type == UPW_NO) {
@@ -550,17 +635,21 @@ struct Upwind {
         }
     }
     // update_upwind / update_downwind (upwind_interface.h:150-165)
-    void update_upwind(const FV1Geometry& geo, const number vStdVel[][3]) { compute(geo, vStdVel, upShapeSh, upConvLength); }
+    void update_upwind(const FV1Geometry& geo, const number vStdVel[][3]) { compute(geo, vStdVel, upShapeSh, upShapeIp, upConvLength); }
     void update_downwind(const FV1Geometry& geo, const number vStdVel[][3]) {
         number vDown[MAXSCVF][3];
         for (int ip = 0; ip < geo.nscvf; ++ip) for (int d = 0; d < 3; ++d) vDown[ip][d] = vStdVel[ip][d] * -1.0;
-        compute(geo, vDown, downShapeSh, downConvLength);
+        compute(geo, vDown, downShapeSh, downShapeIp, downConvLength);
     }
-    // upwind_vel (upwind_interface.h:333-358), non_zero_shape_ip is false for No/Full/Skewed/LPS
-    void upwind_vel(const FV1Geometry& geo, int scvf, const number* u, number* vel) const {
+    // upwind_vel (upwind_interface.h:333-358): corner shapes, plus the ip shapes times
+    // the ip velocities where the upwind has them
+    void upwind_vel(const FV1Geometry& geo, int scvf, const number* u, const number vStdVel[][3], number* vel) const {
         for (int d = 0; d < 3; ++d) vel[d] = 0.0;
         for (int sh = 0; sh < geo.nsh; ++sh)
             for (int d = 0; d < geo.dim; ++d) vel[d] += upShapeSh[scvf][sh] * u[d * geo.nsh + sh];
+        if (!non_zero_shape_ip()) return;
+        for (int j = 0; j < geo.nscvf; ++j)
+            for (int d = 0; d < geo.dim; ++d) vel[d] += upShapeIp[scvf][j] * vStdVel[j][d];
     }
 };
 
@@ -615,10 +704,44 @@ static void diff_length(int type, const FV1Geometry& geo, number* out) {
 }
 
 /* ------------------------------------------------------------------------ */
-/* Stabilisations (incompressible/fv1/stabilization.{h,cpp}), diagonal branch */
-/* (the only branch reachable with the No/Full/Skewed/LPS upwinds, whose    */
-/* non_zero_shape_ip() is false: upwind.h:69,114,196,232).                  */
+/* Stabilisations (incompressible/fv1/stabilization.{h,cpp}): the diagonal    */
+/* branch (upwinds without ip shapes: no, full, skewed, LPS) and the         */
+/* non-diagonal one (positive upwind), whose ip-ip system is inverted.      */
 /* ------------------------------------------------------------------------ */
+
+// inverse of the n x n matrix A (row-major, leading dimension MAXSCVF) by
+// Gauss-Jordan elimination with partial pivoting; false if a pivot is zero
+static bool dense_inverse(int n, const number A[][MAXSCVF], number inv[][MAXSCVF]) {
+    number w[MAXSCVF][2 * MAXSCVF];
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) { w[i][j] = A[i][j]; w[i][n + j] = (i == j) ? 1.0 : 0.0; }
+    for (int c = 0; c < n; ++c) {
+        int p = c;
+        for (int q = c + 1; q < n; ++q) if (std::fabs(w[q][c]) > std::fabs(w[p][c])) p = q;
+        if (w[p][c] == 0.0) return false;
+        if (p != c) for (int j = 0; j < 2 * n; ++j) std::swap(w[p][j], w[c][j]);
+        const number piv = 1.0 / w[c][c];
+        for (int j = 0; j < 2 * n; ++j) w[c][j] *= piv;
+        for (int q = 0; q < n; ++q) {
+            if (q == c) continue;
+            const number f = w[q][c];
+            if (f == 0.0) continue;
+            for (int j = 0; j < 2 * n; ++j) w[q][j] -= f * w[c][j];
+        }
+    }
+    for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) inv[i][j] = w[i][n + j];
+    return true;
+}
+
+// y = inv x over n entries (the summation order of a dense matrix-vector product)
+static void inv_apply(int n, const number inv[][MAXSCVF], const number* x, number* y) {
+    for (int i = 0; i < n; ++i) {
+        number acc = 0;
+        for (int j = 0; j < n; ++j) acc += inv[i][j] * x[j];
+        y[i] = 1.0 * acc;
+    }
+}
+
 struct Stab {
     int type = STAB_NONE;
     int diffLengthType = DL_RAW;
@@ -628,6 +751,122 @@ struct Stab {
     number stabShapeP[MAXSCVF][3][MAXCO];
     number diffLenSqInv[MAXSCVF];
     bool vel_comp_connected() const { return type == STAB_FLOW; }   // stabilization.h:462,544,612
+
+    // FIELDS, non-diagonal branch (stabilization.cpp:244-403): one ip-ip matrix (time,
+    // diffusion, convection with the upwind's ip shapes), inverted once and applied per
+    // velocity component to the corner contributions and to the right-hand side
+    void nondiag_fields(const FV1Geometry& geo, const number* u, number density, const number* pSource, const number* uOld,
+                        number dt, const number* visc, const number* nsvcl) {
+        const int dim = geo.dim, nsh = geo.nsh, P = dim, N = geo.nscvf;
+        number mat[MAXSCVF][MAXSCVF], inv[MAXSCVF][MAXSCVF];
+        for (int i = 0; i < N; ++i) for (int j = 0; j < N; ++j) mat[i][j] = 0.0;
+        for (int ip = 0; ip < N; ++ip) {
+            if (uOld != nullptr) mat[ip][ip] += 1. / dt;
+            mat[ip][ip] += visc[ip];
+            const number scale = nsvcl[ip];
+            mat[ip][ip] += scale;
+            for (int ip2 = 0; ip2 < N; ++ip2) mat[ip][ip2] -= upwind->upShapeIp[ip][ip2] * scale;
+        }
+        if (!dense_inverse(N, mat, inv)) throw std::runtime_error("Could not compute inverse.");
+        for (int d = 0; d < dim; ++d) {
+            number contVel[MAXCO][MAXSCVF], contP[MAXCO][MAXSCVF], x[MAXSCVF];
+            for (int ip = 0; ip < N; ++ip) {
+                const SCVF& scvf = geo.scvf[ip];
+                for (int k = 0; k < nsh; ++k) {
+                    contVel[k][ip] = visc[ip] * scvf.shape[k];
+                    contVel[k][ip] += nsvcl[ip] * upwind->upShapeSh[ip][k];
+                    contP[k][ip] = -1.0 * scvf.globalGrad[k][d] / density;
+                }
+            }
+            for (int k = 0; k < nsh; ++k) {
+                inv_apply(N, inv, contVel[k], x);
+                for (int ip = 0; ip < N; ++ip) stabShapeVel[ip][d][d][k] = x[ip];
+                inv_apply(N, inv, contP[k], x);
+                for (int ip = 0; ip < N; ++ip) stabShapeP[ip][d][k] = x[ip];
+            }
+            number f[MAXSCVF];
+            for (int ip = 0; ip < N; ++ip) {
+                const SCVF& scvf = geo.scvf[ip];
+                f[ip] = 0.0;
+                if (pSource != nullptr) f[ip] = pSource[d];
+                if (uOld != nullptr) {
+                    number oldIPVel = 0.0;
+                    for (int sh = 0; sh < nsh; ++sh) oldIPVel += scvf.shape[sh] * uOld[d * nsh + sh];
+                    f[ip] += oldIPVel / dt;
+                }
+            }
+            for (int k = 0; k < nsh; ++k) {
+                for (int ip = 0; ip < N; ++ip) f[ip] = 1.0 * f[ip] + u[d * nsh + k] * contVel[k][ip];
+                for (int ip = 0; ip < N; ++ip) f[ip] = 1.0 * f[ip] + u[P * nsh + k] * contP[k][ip];
+            }
+            inv_apply(N, inv, f, x);
+            for (int ip = 0; ip < N; ++ip) stabVel[ip][d] = x[ip];
+        }
+    }
+
+    // FLOW, non-diagonal branch (stabilization.cpp:589-771): the ip-ip matrix adds the
+    // divergence correction with the upwind and downwind ip shapes; the velocity
+    // components stay coupled through the ip velocities and the shape gradients
+    void nondiag_flow(const FV1Geometry& geo, const number* u, const number vStdVel[][3], number density, const number* pSource,
+                      const number* uOld, number dt, const number* visc, const number* nsvcl, const number* nsvdl) {
+        const int dim = geo.dim, nsh = geo.nsh, P = dim, N = geo.nscvf;
+        number mat[MAXSCVF][MAXSCVF], inv[MAXSCVF][MAXSCVF];
+        for (int i = 0; i < N; ++i) for (int j = 0; j < N; ++j) mat[i][j] = 0.0;
+        for (int ip = 0; ip < N; ++ip) {
+            if (uOld != nullptr) mat[ip][ip] += 1. / dt;
+            mat[ip][ip] += visc[ip];
+            mat[ip][ip] += nsvcl[ip];
+            for (int ip2 = 0; ip2 < N; ++ip2) {
+                mat[ip][ip2] -= upwind->upShapeIp[ip][ip2] * nsvcl[ip];
+                mat[ip][ip2] += nsvdl[ip] * (upwind->upShapeIp[ip][ip2] - upwind->downShapeIp[ip][ip2]);
+            }
+        }
+        if (!dense_inverse(N, mat, inv)) throw std::runtime_error("Could not compute inverse.");
+        // contributions per (velocity component, corner); every pass over d rewrites all of them
+        number contVel[3][MAXCO][MAXSCVF], contP[MAXCO][MAXSCVF], x[MAXSCVF];
+        for (int d = 0; d < dim; ++d) {
+            for (int ip = 0; ip < N; ++ip) {
+                const SCVF& scvf = geo.scvf[ip];
+                for (int k = 0; k < nsh; ++k) {
+                    contP[k][ip] = -1.0 * scvf.globalGrad[k][d] / density;
+                    contVel[d][k][ip] = visc[ip] * scvf.shape[k];
+                    contVel[d][k][ip] += nsvcl[ip] * upwind->upShapeSh[ip][k];
+                    contVel[d][k][ip] += nsvdl[ip] * (upwind->downShapeSh[ip][k] - upwind->upShapeSh[ip][k]);
+                    for (int d2 = 0; d2 < dim; ++d2) {
+                        if (d2 == d) continue;
+                        contVel[d][k][ip] -= vStdVel[ip][d2] * scvf.globalGrad[k][d2];
+                        contVel[d2][k][ip] = vStdVel[ip][d] * scvf.globalGrad[k][d2];
+                    }
+                }
+            }
+            for (int k = 0; k < nsh; ++k) {
+                inv_apply(N, inv, contP[k], x);
+                for (int ip = 0; ip < N; ++ip) stabShapeP[ip][d][k] = x[ip];
+                for (int d2 = 0; d2 < dim; ++d2) {
+                    inv_apply(N, inv, contVel[d2][k], x);
+                    for (int ip = 0; ip < N; ++ip) stabShapeVel[ip][d][d2][k] = x[ip];
+                }
+            }
+            number f[MAXSCVF];
+            for (int ip = 0; ip < N; ++ip) f[ip] = 0.0;
+            for (int k = 0; k < nsh; ++k) {
+                for (int d2 = 0; d2 < dim; ++d2)
+                    for (int ip = 0; ip < N; ++ip) f[ip] = 1.0 * f[ip] + u[d2 * nsh + k] * contVel[d2][k][ip];
+                for (int ip = 0; ip < N; ++ip) f[ip] = 1.0 * f[ip] + u[P * nsh + k] * contP[k][ip];
+            }
+            for (int ip = 0; ip < N; ++ip) {
+                const SCVF& scvf = geo.scvf[ip];
+                if (pSource != nullptr) f[ip] += pSource[d];
+                if (uOld != nullptr) {
+                    number oldIPVel = 0.0;
+                    for (int sh = 0; sh < nsh; ++sh) oldIPVel += scvf.shape[sh] * uOld[d * nsh + sh];
+                    f[ip] += oldIPVel / dt;
+                }
+            }
+            inv_apply(N, inv, f, x);
+            for (int ip = 0; ip < N; ++ip) stabVel[ip][d] = x[ip];
+        }
+    }
 
     void update(const FV1Geometry& geo, const number* u, const number vStdVel[][3], bool bStokes,
                 number kinVisco, number density, const number* pSource, const number* uOld, number dt) {
@@ -669,6 +908,11 @@ struct Stab {
                 if (flow) vNormStdVelPerDownLen[ip] = norm / (upwind->downConvLength[ip] + upwind->upConvLength[ip]);
             }
 
+        if (!bStokes && upwind->non_zero_shape_ip()) {
+            if (flow) nondiag_flow(geo, u, vStdVel, density, pSource, uOld, dt, vViscoPerDiffLenSq, vNormStdVelPerConvLen, vNormStdVelPerDownLen);
+            else nondiag_fields(geo, u, density, pSource, uOld, dt, vViscoPerDiffLenSq, vNormStdVelPerConvLen);
+            return;
+        }
         for (int ip = 0; ip < numIp; ++ip) {
             const SCVF& scvf = geo.scvf[ip];
             number diag = vViscoPerDiffLenSq[ip];
@@ -833,7 +1077,7 @@ struct Disc {
                 number UpwindVel[3];
                 // PAC: the stabilised velocity is the upwind velocity (navier_stokes_fv1.cpp:707-712)
                 if (pac) for (int d = 0; d < 3; ++d) UpwindVel[d] = stab.stabVel[ip][d];
-                else convUpwind.upwind_vel(geo, ip, u, UpwindVel);
+                else convUpwind.upwind_vel(geo, ip, u, StdVel, UpwindVel);
                 if (bPecletBlend) peclet_blend(UpwindVel, geo, ip, StdVel[ip], nu);
                 number prod = 0;
                 for (int d = 0; d < dim; ++d) prod += StdVel[ip][d] * scvf.normal[d];
@@ -891,7 +1135,7 @@ struct Disc {
                 if (!bStokes) {
                     number UpwindVel[3];
                     if (pac) for (int d = 0; d < 3; ++d) UpwindVel[d] = stab.stabVel[ip][d];
-                    else convUpwind.upwind_vel(geo, ip, u, UpwindVel);
+                    else convUpwind.upwind_vel(geo, ip, u, StdVel, UpwindVel);
                     number w = 1.0;
                     if (bPecletBlend) w = peclet_blend(UpwindVel, geo, ip, StdVel[ip], nu);
                     number prod = 0;
@@ -919,6 +1163,9 @@ struct Disc {
                         }
                     } else {
                         number convFlux_vel = convUpwind.upShapeSh[ip][sh];
+                        // ip shapes: the ip velocities interpolated from the corners (:431-447)
+                        if (convUpwind.non_zero_shape_ip())
+                            for (int ip2 = 0; ip2 < geo.nscvf; ++ip2) convFlux_vel += geo.scvf[ip2].shape[sh] * convUpwind.upShapeIp[ip][ip2];
                         convFlux_vel *= prod * w;
                         for (int d1 = 0; d1 < dim; ++d1) { Jx(d1, from, d1, sh) += convFlux_vel; Jx(d1, to, d1, sh) -= convFlux_vel; }
                     }
@@ -1098,12 +1345,22 @@ static void build_coloring(Mesh& m) {
     for (int64_t e = 0; e < m.nElems; ++e) m.colorElems[f[m.color[e]]++] = (int32_t)e;
 }
 
+// one boundary face of an outflow side (NavierStokesNoNormalStressOutflowFV1): the
+// part of the side belonging to one of its corners
+struct OutflowBF {
+    int64_t elem;      // the element the side belongs to
+    int local;         // the corner's index in the element
+    number xi[3];      // local coordinates of the face's integration point
+    number n[3];       // outward area-weighted normal
+};
+
 struct Problem {
     Disc disc;
     Mesh mesh;
     std::vector<int32_t> dirRow;   // node * b + fct
     std::vector<number> dirVal;
     std::vector<number> bndFlux;   // continuity right-hand side of inflow boundaries, per node
+    std::vector<OutflowBF> outflow;
     std::string lastError;
     explicit Problem(int dim) : disc(dim) {}
 };
@@ -1244,6 +1501,83 @@ static void assemble(Problem& P, const number* U, const number* Uold, number dt,
             }
         }
     }
+    // outflow boundaries without normal stress (no_normal_stress_outflow_fv1.cpp:343-504),
+    // dt-scaled when transient like the other stiffness terms
+    const number sc = transient ? dt : 1.0;
+    for (const OutflowBF& bf : P.outflow) {
+        const int dim = m.dim, Pc = dim;
+        number corners[MAXCO * 3], uloc[4 * MAXCO];
+        gather_elem(m, bf.elem, U, corners, uloc, b);
+        number N[MAXCO], LG[MAXCO][3], J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, JtInv[3][3], G[MAXCO][3];
+        p1_shapes(m.roid, bf.xi, N);
+        p1_grads(m.roid, bf.xi, LG);
+        for (int k = 0; k < nsh; ++k)
+            for (int r = 0; r < dim; ++r)
+                for (int c = 0; c < dim; ++c) J[r][c] += corners[k * dim + r] * LG[k][c];
+        det_and_jtinv(dim, J, JtInv);
+        for (int k = 0; k < nsh; ++k)
+            for (int r = 0; r < 3; ++r) {
+                G[k][r] = 0;
+                if (r < dim) for (int c = 0; c < dim; ++c) G[k][r] += JtInv[r][c] * LG[k][c];
+            }
+        const number* nn = bf.n;
+        const number nu = P.disc.kinVisco, rho = P.disc.density;
+        const int64_t node = m.conn[bf.elem * nsh + bf.local];
+        number stdVel[3] = {0, 0, 0};
+        for (int d1 = 0; d1 < dim; ++d1)
+            for (int sh = 0; sh < nsh; ++sh) stdVel[d1] += uloc[d1 * nsh + sh] * N[sh];
+        number vn = 0;
+        for (int d = 0; d < dim; ++d) vn += stdVel[d] * nn[d];
+        if (D) {
+            // momentum: the tangential part of the viscous flux, the outgoing convective flux
+            number gradVel[3][3], df[3] = {0, 0, 0};
+            for (int d1 = 0; d1 < dim; ++d1)
+                for (int d2 = 0; d2 < dim; ++d2) {
+                    gradVel[d1][d2] = 0.0;
+                    for (int sh = 0; sh < nsh; ++sh) gradVel[d1][d2] += G[sh][d2] * uloc[d1 * nsh + sh];
+                }
+            for (int d1 = 0; d1 < dim; ++d1) for (int d2 = 0; d2 < dim; ++d2) df[d1] += gradVel[d1][d2] * nn[d2];
+            if (!P.disc.bLaplace)
+                for (int d1 = 0; d1 < dim; ++d1) for (int d2 = 0; d2 < dim; ++d2) df[d1] += gradVel[d2][d1] * nn[d2];
+            number dot = 0;
+            for (int d = 0; d < dim; ++d) dot += df[d] * nn[d];
+            for (int d = 0; d < dim; ++d) df[d] += -dot * nn[d];
+            for (int d = 0; d < dim; ++d) df[d] *= -nu * rho;
+            for (int d1 = 0; d1 < dim; ++d1) D[node * b + d1] += sc * df[d1];
+            if (!P.disc.bStokes) {
+                number flux = vn * rho;
+                if (flux < 0) flux = 0;
+                for (int d1 = 0; d1 < dim; ++d1) D[node * b + d1] += sc * (flux * stdVel[d1]);
+            }
+            D[node * b + Pc] += sc * (vn * rho);
+        }
+        if (JV) {
+            auto blk = [&](int sh) { return JV + m.elemBlk[(bf.elem * nsh + bf.local) * nsh + sh] * b * b; };
+            for (int sh = 0; sh < nsh; ++sh) {
+                number M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, ns[3] = {0, 0, 0}, gn = 0;
+                for (int d = 0; d < dim; ++d) gn += G[sh][d] * nn[d];
+                for (int d = 0; d < dim; ++d) M[d][d] = gn;
+                if (!P.disc.bLaplace)
+                    for (int d1 = 0; d1 < dim; ++d1) for (int d2 = 0; d2 < dim; ++d2) M[d1][d2] += G[sh][d1] * nn[d2];
+                for (int d2 = 0; d2 < dim; ++d2) for (int d1 = 0; d1 < dim; ++d1) ns[d2] += M[d1][d2] * nn[d1];
+                number* B = blk(sh);
+                for (int d1 = 0; d1 < dim; ++d1)
+                    for (int d2 = 0; d2 < dim; ++d2) B[d1 * b + d2] += sc * ((M[d1][d2] - nn[d1] * ns[d2]) * (-nu * rho));
+            }
+            if (!P.disc.bStokes) {
+                number old = vn * rho;
+                if (old < 0) old = 0;
+                for (int sh = 0; sh < nsh; ++sh) {
+                    number* B = blk(sh);
+                    for (int d1 = 0; d1 < dim; ++d1) B[d1 * b + d1] += sc * (old * N[sh]);
+                }
+            }
+            for (int sh = 0; sh < nsh; ++sh) {
+                number* B = blk(sh);
+                for (int d2 = 0; d2 < dim; ++d2) B[Pc * b + d2] += sc * (N[sh] * nn[d2] * rho);
+            }
+        }
+    }
     // inflow boundaries: the continuity rows' Neumann flux (a right-hand side: dt-scaled when transient)
     if (D && !P.bndFlux.empty())
         for (int64_t r = 0; r < m.nNodes; ++r) D[r * b + (b - 1)] += (transient ? dt : 1.0) * P.bndFlux[r];
@@ -1378,6 +1712,7 @@ int ora_upwind_id(const char* name) {
     if (n == "full") return UPW_FULL;
     if (n == "skewed") return UPW_SKEWED;
     if (n == "linearprofileskewed" || n == "lps") return UPW_LPS;
+    if (n == "positive" || n == "pos") return UPW_POS;
     return -1;
 }
 int ora_stab_id(const char* name) {
@@ -1498,6 +1833,271 @@ int ora_elem_batch(void* h, int roid, int64_t nelem, const double* corners, cons
             if (defM) { double* o = defM + e * n; std::fill(o, o + n, 0.0); P->disc.add_def_M_elem(o, geo, ue); }
             if (jacM) { double* o = jacM + e * n * n; std::fill(o, o + n * n, 0.0); P->disc.add_jac_M_elem(o, geo); }
             if (rhs) { double* o = rhs + e * n; std::fill(o, o + n, 0.0); P->disc.add_rhs_elem(o, geo); }
+        }
+        return 0;
+    } catch (std::exception& ex) { P->lastError = ex.what(); return 3; }
+}
+
+/* Data exports of the disc (navier_stokes_fv1.cpp:894-1491): per element the
+ * velocity, its gradient, the stabilised ip velocity, the pressure or its
+ * gradient at a set of local points, and optionally the derivatives w.r.t. the
+ * element's unknowns, with the reference's conventions:
+ *  - ipKind 0: the SCVF integration points (the FV1 branch of each export);
+ *    1: the SCV integration points (the corners: the nodal branch of the
+ *    pressure export, the general branch of the others); 2: nip given points;
+ *  - values[e][ip][vs], derivs[e][ip][fct][sh][vs] (vs = dim, dim*dim, dim, 1,
+ *    dim for which = 0..4), both zeroed first; entries an export leaves alone
+ *    stay zero. A number assigned to a vector derivative (the velocity
+ *    exports) sets all of its components, as MathVector's assignment does. The
+ *    general branch of the velocity gradient uses the local (reference)
+ *    gradients, as the reference does (:1062-1082); the pressure gradient's
+ *    general branch maps them with J^-T (:1473-1484). */
+int ora_export(void* h, int which, int roid, int64_t nelem, const double* corners, const double* u, const double* u_old, double dt,
+               int ipKind, int nipGiven, const double* lips, double* values, double* derivs) {
+    auto* P = static_cast<Problem*>(h);
+    try {
+        P->disc.check();
+        const RefElem& R = ref_elem(roid);
+        const int dim = R.dim;
+        if (dim != P->disc.dim) throw std::runtime_error("element dimension does not match the disc");
+        if (which < 0 || which > 4) throw std::runtime_error("unknown export");
+        const int nsh = R.nco, b = dim + 1, n = b * nsh, Pc = dim;
+        const int vs = (which == 1) ? dim * dim : (which == 3) ? 1 : dim;
+        FV1Geometry geo;
+        for (int64_t e = 0; e < nelem; ++e) {
+            const double* c = corners + e * nsh * dim;
+            const double* ue = u + e * n;
+            const double* uo = u_old ? u_old + e * n : nullptr;
+            geo.update(roid, c);
+            const int nip = ipKind == 0 ? geo.nscvf : ipKind == 1 ? nsh : nipGiven;
+            double* val = values + e * (int64_t)nip * vs;
+            std::fill(val, val + (int64_t)nip * vs, 0.0);
+            double* der = derivs ? derivs + e * (int64_t)nip * b * nsh * vs : nullptr;
+            if (der) std::fill(der, der + (int64_t)nip * b * nsh * vs, 0.0);
+            auto D = [&](int ip, int f, int sh) { return der + (((int64_t)ip * b + f) * nsh + sh) * vs; };
+            if (ipKind == 0 && which == 2) {
+                // ex_velocity_ip, FV1 branch (:1136-1232): the stabilisation's velocity and shapes
+                number StdVel[MAXSCVF][3];
+                P->disc.std_vel(geo, ue, StdVel);
+                P->disc.stab.update(geo, ue, StdVel, P->disc.bStokes, P->disc.kinVisco, P->disc.density,
+                                    P->disc.hasSource ? P->disc.source : nullptr, uo, dt);
+                const Stab& st = P->disc.stab;
+                for (int ip = 0; ip < nip; ++ip) {
+                    for (int d = 0; d < dim; ++d) val[ip * vs + d] = st.stabVel[ip][d];
+                    if (!der) continue;
+                    for (int sh = 0; sh < nsh; ++sh)
+                        for (int d1 = 0; d1 < dim; ++d1) {
+                            if (st.vel_comp_connected())
+                                for (int d2 = 0; d2 < dim; ++d2) D(ip, d2, sh)[d1] = st.stabShapeVel[ip][d1][d2][sh];
+                            else
+                                D(ip, d1, sh)[d1] = st.stabShapeVel[ip][d1][d1][sh];
+                            D(ip, Pc, sh)[d1] = st.stabShapeP[ip][d1][sh];
+                        }
+                }
+                continue;
+            }
+            if (ipKind == 1 && which == 3) {
+                // ex_nodal_pressure, SCV branch (:1336-1358): the corner's value
+                for (int ip = 0; ip < nip; ++ip) {
+                    const int co = geo.scv[ip].nodeId;
+                    val[ip] = ue[Pc * nsh + co];
+                    if (der) for (int sh = 0; sh < nsh; ++sh) D(ip, Pc, sh)[0] = (sh == co) ? 1.0 : 0.0;
+                }
+                continue;
+            }
+            for (int ip = 0; ip < nip; ++ip) {
+                // shapes, gradients (global at the SCVF ips, local elsewhere) and J^-T at the point
+                number N[MAXCO], G[MAXCO][3], JtInv[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                const bool fv1 = ipKind == 0;
+                if (fv1) {
+                    for (int sh = 0; sh < nsh; ++sh) {
+                        N[sh] = geo.scvf[ip].shape[sh];
+                        for (int d = 0; d < 3; ++d) G[sh][d] = geo.scvf[ip].globalGrad[sh][d];
+                    }
+                } else {
+                    number x[3] = {0, 0, 0};
+                    for (int d = 0; d < dim; ++d) x[d] = ipKind == 1 ? R.co[ip][d] : lips[ip * dim + d];
+                    p1_shapes(roid, x, N);
+                    p1_grads(roid, x, G);
+                    if (which == 4) {
+                        number J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                        for (int k = 0; k < nsh; ++k)
+                            for (int r = 0; r < dim; ++r)
+                                for (int cc = 0; cc < dim; ++cc) J[r][cc] += c[k * dim + r] * G[k][cc];
+                        det_and_jtinv(dim, J, JtInv);
+                    }
+                }
+                if (which == 0 || which == 2) {
+                    // ex_nodal_velocity (:919-990), ex_velocity_ip general branch (:1238-1275)
+                    for (int d = 0; d < dim; ++d)
+                        for (int sh = 0; sh < nsh; ++sh) {
+                            val[ip * vs + d] += ue[d * nsh + sh] * N[sh];
+                            if (der) for (int q = 0; q < vs; ++q) D(ip, d, sh)[q] = N[sh];
+                        }
+                } else if (which == 1) {
+                    // ex_velocity_grad (:1017-1098)
+                    for (int d1 = 0; d1 < dim; ++d1)
+                        for (int d2 = 0; d2 < dim; ++d2) {
+                            number v = 0.0;
+                            for (int sh = 0; sh < nsh; ++sh) {
+                                v += ue[d1 * nsh + sh] * G[sh][d2];
+                                if (der) D(ip, d1, sh)[d1 * dim + d2] = G[sh][d2];
+                            }
+                            val[ip * vs + d1 * dim + d2] = v;
+                        }
+                } else if (which == 3) {
+                    // ex_nodal_pressure, FV1 and general branches (:1307-1333, :1360-1390)
+                    number v = 0.0;
+                    for (int sh = 0; sh < nsh; ++sh) v += ue[Pc * nsh + sh] * N[sh];
+                    val[ip] = v;
+                    if (der) for (int sh = 0; sh < nsh; ++sh) D(ip, Pc, sh)[0] = N[sh];
+                } else {
+                    // ex_pressure_grad (:1421-1448 FV1, :1455-1490 general)
+                    if (fv1) {
+                        for (int sh = 0; sh < nsh; ++sh)
+                            for (int d = 0; d < dim; ++d) val[ip * vs + d] += ue[Pc * nsh + sh] * G[sh][d];
+                        if (der) for (int sh = 0; sh < nsh; ++sh) for (int d = 0; d < dim; ++d) D(ip, Pc, sh)[d] = G[sh][d];
+                    } else {
+                        number lg[3] = {0, 0, 0};
+                        for (int sh = 0; sh < nsh; ++sh)
+                            for (int d = 0; d < dim; ++d) lg[d] += ue[Pc * nsh + sh] * G[sh][d];
+                        for (int r = 0; r < dim; ++r) {
+                            number v = 0.0;
+                            for (int cc = 0; cc < dim; ++cc) v += JtInv[r][cc] * lg[cc];
+                            val[ip * vs + r] = v;
+                        }
+                        if (der)
+                            for (int sh = 0; sh < nsh; ++sh)
+                                for (int r = 0; r < dim; ++r) {
+                                    number v = 0.0;
+                                    for (int cc = 0; cc < dim; ++cc) v += JtInv[r][cc] * G[sh][cc];
+                                    D(ip, Pc, sh)[r] = v;
+                                }
+                    }
+                }
+            }
+        }
+        return 0;
+    } catch (std::exception& ex) { P->lastError = ex.what(); return 3; }
+}
+
+/* vorticityFV1 (incompressible/navier_stokes_tools.h:387-525): per element and
+ * corner, the curl (d u_y/dx - d u_x/dy) of the P1 velocity at the corner (the
+ * SCV's integration point) times the SCV volume is summed at the node with the
+ * SCV volume; the node value is the ratio (elements in mesh order). The formula
+ * takes the first two velocity components in 3D as well (the z-component). */
+int ora_vorticity(void* h, const double* U, double* vort) {
+    auto* P = static_cast<Problem*>(h);
+    try {
+        const Mesh& m = P->mesh;
+        if (m.nElems == 0) throw std::runtime_error("no mesh");
+        const RefElem& R = ref_elem(m.roid);
+        const int dim = m.dim, nsh = m.nsh, b = dim + 1;
+        std::vector<number> vol(m.nNodes, 0.0);
+        std::fill(vort, vort + m.nNodes, 0.0);
+        FV1Geometry geo;
+        number c[MAXCO * 3];
+        for (int64_t e = 0; e < m.nElems; ++e) {
+            const int32_t* nd = &m.conn[e * nsh];
+            for (int k = 0; k < nsh; ++k) for (int d = 0; d < dim; ++d) c[k * dim + d] = m.coords[(int64_t)nd[k] * dim + d];
+            geo.update(m.roid, c);
+            for (int co = 0; co < nsh; ++co) {
+                number x[3] = {0, 0, 0}, LG[MAXCO][3], J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, JtInv[3][3];
+                for (int d = 0; d < dim; ++d) x[d] = R.co[co][d];
+                p1_grads(m.roid, x, LG);
+                for (int k = 0; k < nsh; ++k)
+                    for (int r = 0; r < dim; ++r)
+                        for (int cc = 0; cc < dim; ++cc) J[r][cc] += c[k * dim + r] * LG[k][cc];
+                det_and_jtinv(dim, J, JtInv);
+                number lv = 0.0;
+                for (int sh = 0; sh < nsh; ++sh) {
+                    number g[3] = {0, 0, 0};
+                    for (int r = 0; r < dim; ++r) for (int cc = 0; cc < dim; ++cc) g[r] += JtInv[r][cc] * LG[sh][cc];
+                    lv += U[(int64_t)nd[sh] * b + 1] * g[0] - U[(int64_t)nd[sh] * b + 0] * g[1];
+                }
+                const number v = geo.scv[co].vol;
+                lv *= v;
+                vort[nd[co]] += lv;
+                vol[nd[co]] += v;
+            }
+        }
+        for (int64_t i = 0; i < m.nNodes; ++i) vort[i] /= vol[i];
+        return 0;
+    } catch (std::exception& ex) { P->lastError = ex.what(); return 3; }
+}
+
+/* Local coordinates of the global point x in element corners c (the inverse of the
+ * P1 / multilinear reference mapping: one solve on simplices, Newton steps from the
+ * element centre on quadrilaterals and hexahedra); true if x lies in the element
+ * (local coordinates within 1e-10 of the reference element). */
+static bool point_in_elem(int roid, int dim, int nsh, const number* c, const number* x, number* xi) {
+    const RefElem& R = ref_elem(roid);
+    for (int d = 0; d < 3; ++d) xi[d] = 0.0;
+    for (int d = 0; d < dim; ++d) { number s = 0; for (int k = 0; k < nsh; ++k) s += R.co[k][d]; xi[d] = s / nsh; }
+    for (int it = 0; it < 30; ++it) {
+        number N[MAXCO], LG[MAXCO][3], J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, JtInv[3][3], F[3] = {0, 0, 0};
+        p1_shapes(roid, xi, N);
+        p1_grads(roid, xi, LG);
+        for (int k = 0; k < nsh; ++k)
+            for (int r = 0; r < dim; ++r) {
+                F[r] += N[k] * c[k * dim + r];
+                for (int cc = 0; cc < dim; ++cc) J[r][cc] += c[k * dim + r] * LG[k][cc];
+            }
+        det_and_jtinv(dim, J, JtInv);
+        // xi -= J^-1 (F - x), J^-1 = (J^-T)^T
+        number dx[3] = {0, 0, 0}, step = 0.0;
+        for (int cc = 0; cc < dim; ++cc) {
+            number s = 0;
+            for (int r = 0; r < dim; ++r) s += JtInv[r][cc] * (F[r] - x[r]);
+            dx[cc] = s;
+        }
+        for (int cc = 0; cc < dim; ++cc) { xi[cc] -= dx[cc]; step = std::max(step, std::fabs(dx[cc])); }
+        if (!(step > 1e-15)) break;
+    }
+    const number tol = 1e-10;
+    if (roid == ROID_TRIANGLE) return xi[0] >= -tol && xi[1] >= -tol && 1.0 - xi[0] - xi[1] >= -tol;
+    if (roid == ROID_TETRAHEDRON) return xi[0] >= -tol && xi[1] >= -tol && xi[2] >= -tol && 1.0 - xi[0] - xi[1] - xi[2] >= -tol;
+    for (int d = 0; d < dim; ++d) if (!(xi[d] >= -tol && xi[d] <= 1.0 + tol)) return false;
+    return true;
+}
+
+/* The P1 solution's function fct at n global points (the point evaluation behind
+ * DrivenCavityEvalAtPoints, navier_stokes_tools.h:540-570): the first element in
+ * mesh order that contains the point, P1 shapes at its local coordinates; NaN
+ * where no element contains the point. */
+int ora_eval_points(void* h, const double* U, int64_t np, const double* pts, int fct, double* out) {
+    auto* P = static_cast<Problem*>(h);
+    try {
+        const Mesh& m = P->mesh;
+        if (m.nElems == 0) throw std::runtime_error("no mesh");
+        const int dim = m.dim, nsh = m.nsh, b = dim + 1;
+        if (fct < 0 || fct >= b) throw std::runtime_error("bad function index");
+        number c[MAXCO * 3];
+        for (int64_t p = 0; p < np; ++p) {
+            out[p] = std::numeric_limits<number>::quiet_NaN();
+            const number* x = pts + p * dim;
+            for (int64_t e = 0; e < m.nElems; ++e) {
+                const int32_t* nd = &m.conn[e * nsh];
+                bool out_of_box = false;
+                for (int d = 0; d < dim && !out_of_box; ++d) {
+                    number lo = 1e300, hi = -1e300;
+                    for (int k = 0; k < nsh; ++k) {
+                        c[k * dim + d] = m.coords[(int64_t)nd[k] * dim + d];
+                        lo = std::min(lo, c[k * dim + d]); hi = std::max(hi, c[k * dim + d]);
+                    }
+                    const number pad = 1e-10 * (hi - lo);
+                    out_of_box = x[d] < lo - pad || x[d] > hi + pad;
+                }
+                if (out_of_box) continue;
+                number xi[3];
+                if (!point_in_elem(m.roid, dim, nsh, c, x, xi)) continue;
+                number N[MAXCO];
+                p1_shapes(m.roid, xi, N);
+                number v = 0;
+                for (int k = 0; k < nsh; ++k) v += N[k] * U[(int64_t)nd[k] * b + fct];
+                out[p] = v;
+                break;
+            }
         }
         return 0;
     } catch (std::exception& ex) { P->lastError = ex.what(); return 3; }
@@ -1654,6 +2254,56 @@ int ora_add_inflow(void* h, int64_t nSides, int nco, const int32_t* sides, const
         }
     }
     merge_dirichlet(*P, rows, vals);
+    return 0;
+}
+
+/* NavierStokesNoNormalStressOutflowFV1::add(subsets) (no_normal_stress_outflow_fv1.cpp,
+ * no_normal_stress_outflow_base): sides[nSides][nco] of the outflow boundary; each
+ * corner of a side gets the boundary face {corner, side-edge midpoints, side centre}
+ * (2D: {corner, side midpoint}) with its integration point at the mean of those
+ * points (in local coordinates) and its outward area-weighted normal. */
+int ora_add_outflow(void* h, int64_t nSides, int nco, const int32_t* sides) {
+    auto* P = static_cast<Problem*>(h);
+    Mesh& m = P->mesh;
+    const int dim = m.dim, nsh = m.nsh;
+    const RefElem& R = ref_elem(m.roid);
+    for (int64_t s = 0; s < nSides; ++s) {
+        const int32_t* sn = sides + s * nco;
+        int64_t owner = -1;
+        int owners = 0;
+        for (int64_t e = 0; e < m.nElems; ++e) {
+            int found = 0;
+            for (int j = 0; j < nco; ++j)
+                for (int i = 0; i < nsh; ++i) found += (m.conn[e * nsh + i] == sn[j]);
+            if (found == nco) { owner = e; ++owners; }
+        }
+        if (owners != 1) { P->lastError = "outflow side is not a boundary side of exactly one element"; return 1; }
+        number x[4][3] = {{0}}, cen[3] = {0, 0, 0}, lx[4][3] = {{0}}, lsc[3] = {0, 0, 0};
+        int loc[4];
+        for (int j = 0; j < nco; ++j) {
+            for (int d = 0; d < dim; ++d) x[j][d] = m.coords[(int64_t)sn[j] * dim + d];
+            loc[j] = -1;
+            for (int i = 0; i < nsh; ++i) if (m.conn[owner * nsh + i] == sn[j]) loc[j] = i;
+            for (int d = 0; d < dim; ++d) { lx[j][d] = R.co[loc[j]][d]; lsc[d] += lx[j][d] / nco; }
+        }
+        for (int i = 0; i < nsh; ++i) for (int d = 0; d < dim; ++d) cen[d] += m.coords[(int64_t)m.conn[owner * nsh + i] * dim + d] / nsh;
+        for (int j = 0; j < nco; ++j) {
+            OutflowBF bf;
+            bf.elem = owner;
+            bf.local = loc[j];
+            boundary_face_normal(dim, nco, x, j, cen, bf.n);
+            for (int d = 0; d < 3; ++d) bf.xi[d] = 0.0;
+            if (dim == 2) {
+                const int o = 1 - j;
+                for (int d = 0; d < 2; ++d) bf.xi[d] = 0.5 * (lx[j][d] + 0.5 * (lx[j][d] + lx[o][d]));
+            } else {
+                const int nx = (j + 1) % nco, pv = (j + nco - 1) % nco;
+                for (int d = 0; d < 3; ++d)
+                    bf.xi[d] = 0.25 * (lx[j][d] + 0.5 * (lx[j][d] + lx[nx][d]) + lsc[d] + 0.5 * (lx[pv][d] + lx[j][d]));
+            }
+            P->outflow.push_back(bf);
+        }
+    }
     return 0;
 }
 

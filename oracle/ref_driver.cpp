@@ -172,6 +172,95 @@ void geometry(const double* corners, double* out) {
     for (size_t a = 0; a < geo.num_scv(); ++a) out[geo.num_scvf() * 40 + a] = geo.scv(a).volume();
 }
 
+// The reference's data exports (navier_stokes_fv1.cpp:894-1491) of n elements at the
+// SCVF ips (ipKind 0), the SCV ips (1) or nip given local points (2); layouts as
+// ora_export: values[e][ip][vs], derivs[e][ip][fct][sh][vs], zeroed before each call.
+template <int dim> void put(double* o, const MathVector<dim>& v) { for (int d = 0; d < dim; ++d) o[d] = v[d]; }
+template <int dim> void put(double* o, const MathMatrix<dim, dim>& m) {
+    for (int r = 0; r < dim; ++r) for (int c = 0; c < dim; ++c) o[r * dim + c] = m(r, c);
+}
+template <int dim> void put(double* o, const number& v) { o[0] = v; }
+template <class T> void zero(T& v) { v = 0.0; }
+
+template <int dim, class TElem>
+void run_export(const ref_config& c, int which, int64_t n, const double* corners, const double* u, const double* uold, double dt, int ipKind,
+                int nipGiven, const double* lips, double* values, double* derivs) {
+    typedef typename DomainOf<dim>::type TDomain;
+    typedef FV1Geometry<TElem, dim> TGeom;
+    typedef NavierStokesFV1<TDomain> TDisc;
+    static const int nsh = (int)TGeom::nsh, b = dim + 1, nloc = b * nsh;
+    const ReferenceObjectID roid = TGeom::ROID;
+    TDisc disc(dim == 2 ? "u,v,p" : "u,v,w,p", "Inner");
+    configure<dim>(disc, c);
+    LocalVectorTimeSeries ts;
+    LocalVector U(b, nsh), Uo(b, nsh);
+    if (uold) {
+        ts.set(&U, dt, &Uo, 0.0);
+        disc.set_time_series(&ts);
+    }
+    disc.template prep_elem_loop<TElem, TGeom>(roid, 0);
+    const TGeom& geo = GeomProvider<TGeom>::get();
+    MathVector<dim> co[nsh];
+    std::vector<MathVector<dim> > given(nipGiven > 0 ? nipGiven : 1);
+    for (int i = 0; i < nipGiven; ++i) for (int d = 0; d < dim; ++d) given[i][d] = lips[i * dim + d];
+    const int vs = (which == 1) ? dim * dim : (which == 3) ? 1 : dim;
+    for (int64_t e = 0; e < n; ++e) {
+        for (int k = 0; k < nsh; ++k)
+            for (int x = 0; x < dim; ++x) co[k][x] = corners[(e * nsh + k) * dim + x];
+        for (int q = 0; q < nloc; ++q) {
+            U.data()[q] = u[e * nloc + q];
+            Uo.data()[q] = uold ? uold[e * nloc + q] : 0.0;
+        }
+        disc.template prep_elem<TElem, TGeom>(U, nullptr, roid, co);
+        const MathVector<dim>* lip = ipKind == 0 ? geo.scvf_local_ips() : ipKind == 1 ? geo.scv_local_ips() : &given[0];
+        const size_t nip = ipKind == 0 ? geo.num_scvf() : ipKind == 1 ? geo.num_scv() : (size_t)nipGiven;
+        std::vector<MathVector<dim> > gip(nip);
+        double* val = values + e * (int64_t)nip * vs;
+        double* der = derivs ? derivs + e * (int64_t)nip * b * nsh * vs : nullptr;
+        auto run = [&](auto* proto, auto fn) {
+            typedef typename std::remove_pointer<decltype(proto)>::type T;
+            std::vector<T> v(nip);
+            for (auto& x : v) zero(x);
+            std::vector<std::vector<std::vector<T> > > dv(nip, std::vector<std::vector<T> >(b, std::vector<T>(nsh)));
+            for (auto& a : dv) for (auto& bb : a) for (auto& x : bb) zero(x);
+            fn(v.data(), gip.data(), lip, nip, der != nullptr, dv.data());
+            for (size_t ip = 0; ip < nip; ++ip) {
+                put<dim>(val + ip * vs, v[ip]);
+                if (der)
+                    for (int f = 0; f < b; ++f)
+                        for (int sh = 0; sh < nsh; ++sh) put<dim>(der + ((ip * b + f) * nsh + sh) * vs, dv[ip][f][sh]);
+            }
+        };
+        switch (which) {
+            case 0:
+                run((MathVector<dim>*)nullptr, [&](auto* v, auto* g, auto* l, size_t ni, bool bd, auto* dv) {
+                    disc.template ex_nodal_velocity<TElem, TGeom>(v, g, 0.0, 0, U, nullptr, co, l, ni, bd, dv);
+                });
+                break;
+            case 1:
+                run((MathMatrix<dim, dim>*)nullptr, [&](auto* v, auto* g, auto* l, size_t ni, bool bd, auto* dv) {
+                    disc.template ex_velocity_grad<TElem, TGeom>(v, g, 0.0, 0, U, nullptr, co, l, ni, bd, dv);
+                });
+                break;
+            case 2:
+                run((MathVector<dim>*)nullptr, [&](auto* v, auto* g, auto* l, size_t ni, bool bd, auto* dv) {
+                    disc.template ex_velocity_ip<TElem, TGeom>(v, g, 0.0, 0, U, nullptr, co, l, ni, bd, dv);
+                });
+                break;
+            case 3:
+                run((number*)nullptr, [&](auto* v, auto* g, auto* l, size_t ni, bool bd, auto* dv) {
+                    disc.template ex_nodal_pressure<TElem, TGeom>(v, g, 0.0, 0, U, nullptr, co, l, ni, bd, dv);
+                });
+                break;
+            default:
+                run((MathVector<dim>*)nullptr, [&](auto* v, auto* g, auto* l, size_t ni, bool bd, auto* dv) {
+                    disc.template ex_pressure_grad<TElem, TGeom>(v, g, 0.0, 0, U, nullptr, co, l, ni, bd, dv);
+                });
+        }
+    }
+    disc.template fsh_elem_loop<TElem, TGeom>();
+}
+
 thread_local std::string g_err;
 
 }  // namespace
@@ -189,6 +278,22 @@ int ref_elem_batch(int roid, int64_t n, const ref_config* c, const double* corne
             case ROID_QUADRILATERAL: run_batch<2, Quadrilateral>(*c, n, corners, u, u_old, dt, defA, jacA, defM, jacM, rhs); return 0;
             case ROID_TETRAHEDRON: run_batch<3, Tetrahedron>(*c, n, corners, u, u_old, dt, defA, jacA, defM, jacM, rhs); return 0;
             case ROID_HEXAHEDRON: run_batch<3, Hexahedron>(*c, n, corners, u, u_old, dt, defA, jacA, defM, jacM, rhs); return 0;
+        }
+        return 2;
+    } catch (std::exception& e) {
+        g_err = e.what();
+        return 1;
+    }
+}
+
+int ref_export(int which, int roid, int64_t n, const ref_config* c, const double* corners, const double* u, const double* u_old, double dt,
+               int ipKind, int nip, const double* lips, double* values, double* derivs) {
+    try {
+        switch (roid) {
+            case ROID_TRIANGLE: run_export<2, Triangle>(*c, which, n, corners, u, u_old, dt, ipKind, nip, lips, values, derivs); return 0;
+            case ROID_QUADRILATERAL: run_export<2, Quadrilateral>(*c, which, n, corners, u, u_old, dt, ipKind, nip, lips, values, derivs); return 0;
+            case ROID_TETRAHEDRON: run_export<3, Tetrahedron>(*c, which, n, corners, u, u_old, dt, ipKind, nip, lips, values, derivs); return 0;
+            case ROID_HEXAHEDRON: run_export<3, Hexahedron>(*c, which, n, corners, u, u_old, dt, ipKind, nip, lips, values, derivs); return 0;
         }
         return 2;
     } catch (std::exception& e) {

@@ -7,6 +7,8 @@ reference's NavierStokesFV1 interface.
 """
 from . import _capi, mesh
 from ._capi import NSFV1Error
-from .navier_stokes_fv1 import NavierStokesFV1, NavierStokesInflowFV1, NavierStokesWall, mesh_pattern
+from .navier_stokes_fv1 import (DataExport, NavierStokesFV1, NavierStokesInflowFV1, NavierStokesNoNormalStressOutflowFV1, NavierStokesWall,
+                                mesh_pattern)
 
-__all__ = ["NavierStokesFV1", "NavierStokesInflowFV1", "NavierStokesWall", "NSFV1Error", "mesh", "mesh_pattern", "_capi"]
+__all__ = ["DataExport", "NavierStokesFV1", "NavierStokesInflowFV1", "NavierStokesNoNormalStressOutflowFV1", "NavierStokesWall", "NSFV1Error",
+           "mesh", "mesh_pattern", "_capi"]

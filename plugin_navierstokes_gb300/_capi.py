@@ -111,6 +111,7 @@ _SIGS = {
     "nsfv1_add_wall": (c_int, [c_void_p, c_int64, c_void_p]),
     "nsfv1_add_inflow": (c_int, [c_void_p, c_int64, c_int, c_void_p, c_void_p]),
     "nsfv1_clear_boundary": (c_int, [c_void_p]),
+    "nsfv1_add_outflow": (c_int, [c_void_p, c_int64, c_int, c_void_p]),
     "nsfv1_assemble_defect": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p]),
     "nsfv1_assemble_jacobian": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_int, c_void_p]),
     "nsfv1_assemble_defect_jacobian": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p, c_int, c_void_p]),
@@ -118,6 +119,10 @@ _SIGS = {
                                  c_void_p, c_void_p, c_void_p, c_void_p]),
     "nsfv1_elem_batch_host": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p,
                                       c_void_p, c_void_p, c_void_p]),
+    "nsfv1_vorticity": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "nsfv1_eval_points": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int, c_void_p, c_void_p]),
+    "nsfv1_export": (c_int, [c_void_p, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_double, c_int, c_int, c_void_p,
+                             c_void_p, c_void_p, c_void_p]),
     "nsfv1_bsr_mv": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "nsfv1_block_jacobi": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "nsfv1_block_jacobi_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),

@@ -1214,7 +1214,9 @@ int nsfv1_set_instance_grids(nsfv1_disc* h, const int32_t* cells) {
         C.viscoSet = D->viscoSet; C.stabSet = D->stabSet; C.convUpwindSet = D->convUpwindSet; C.stabSharesConv = D->stabSharesConv;
         C.convUpwindType = D->convUpwindType; C.stabUpwindType = D->stabUpwindType; C.stabType = D->stabType; C.diffLen = D->diffLen;
         nsfv1_disc* ch = reinterpret_cast<nsfv1_disc*>(&C);
-        int st = nsfv1_set_mesh(ch, ROID_QUADRILATERAL, nn, coords.data(), (int64_t)conn.size() / 4, conn.data());
+        C.pac = D->pac;
+        int st = C.ensure_ipws() ? NSFV1_OK : C.status;
+        if (st == NSFV1_OK) st = nsfv1_set_mesh(ch, ROID_QUADRILATERAL, nn, coords.data(), (int64_t)conn.size() / 4, conn.data());
         if (st == NSFV1_OK) st = nsfv1_set_elem_viscosity(ch, nuE.data());
         if (st == NSFV1_OK) st = nsfv1_set_dirichlet(ch, (int64_t)dirRow.size(), dirRow.data(), dirVal.data());
         if (st != NSFV1_OK) { D->fail(st, "multigrid level " + std::to_string(l) + ": " + C.lastError); L.release(); return D->status; }

@@ -34,6 +34,7 @@ static int upwind_id(const char* name) {
     if (n == "full") return UPW_FULL;
     if (n == "skewed") return UPW_SKEWED;
     if (n == "linearprofileskewed" || n == "lps") return UPW_LPS;
+    if (n == "positive" || n == "pos") return UPW_POS;
     return -1;
 }
 // CreateNavierStokesStabilization (stabilization.cpp:46-57) + the "without" variant
@@ -76,7 +77,9 @@ template <class T> static cudaError_t dupload(T*& dst, const T* src, size_t n) {
 
 void Disc::free_mesh() {
     dfree(d_coords); dfree(d_conn); dfree(d_elemBlk); dfree(d_colorElems); dfree(d_rowPtr); dfree(d_colIdx);
-    dfree(d_dirRow); dfree(d_dirVal); dfree(d_diagPos); dfree(d_bjDinv); dfree(d_nuElem); dfree(d_bndFlux);
+    dfree(d_dirRow); dfree(d_dirVal); dfree(d_diagPos); dfree(d_bjDinv); dfree(d_nuElem); dfree(d_bndFlux); dfree(d_nodeVol);
+    free_outflow();
+    outflowHost.clear();
     bndFluxHost.clear();
     dfree(d_instNode0); dfree(d_elemInst); dfree(d_nodeInst); dfree(d_instActive);
     nInst = 0; instNode0.clear(); instSkip = false;
@@ -84,11 +87,44 @@ void Disc::free_mesh() {
     if (batch) { batch_free(batch); batch = nullptr; }
 }
 
+void Disc::free_outflow() {
+    dfree(d_ofSeg); dfree(d_ofElem); dfree(d_ofLocal); dfree(d_ofXi); dfree(d_ofN);
+    nOfSeg = 0;
+}
+
+// the outflow faces' terms (after the element loop, before the Dirichlet rows)
+bool Disc::outflow_terms(const DiscParams& P, const double* u, double* d, void* vals, int prec, cudaStream_t s) {
+    if (nOfSeg <= 0) return true;
+    AsmArgs a{d_coords, d_conn, d_elemBlk, nullptr, 0, d_err, u, nullptr, d, vals, d_nuElem, nullptr, nullptr, nNodes, (int64_t)colIdx.size()};
+    OutflowArgs o{nOfSeg, d_ofSeg, d_ofElem, d_ofLocal, d_ofXi, d_ofN};
+    return cuda_ok(launch_outflow(roid, P, a, o, prec, s), "outflow boundary");
+}
+
 Disc::~Disc() {
     free_mesh();
     free_workspace();
     if (batch) { batch_free(batch); batch = nullptr; }
     dfree(d_err);
+    dfree(d_ipws);
+}
+
+// The positive upwind's element path keeps the state of every SCVF of an element
+// in a per-thread workspace: one slice per thread of a fixed launch width (one
+// 64-thread CTA per SM), sized for the largest element type of the dimension.
+// Allocated when such an upwind is set, so that no assembly call allocates.
+bool Disc::ensure_ipws(bool force) {
+    const bool need = force || convUpwindType == UPW_POS || stabUpwindType == UPW_POS;
+    if (!need || d_ipws) return true;
+    int dev = 0, sms = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "device")) return false;
+    if (!cuda_ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count")) return false;
+    const int64_t threads = (int64_t)sms * kIpwsCtaThreads;
+    if (!cuda_ok(cudaMalloc(&d_ipws, sizeof(double) * (size_t)threads * ipws_doubles_host(dim)), "positive-upwind workspace")) {
+        d_ipws = nullptr;
+        return false;
+    }
+    ipwsThreads = threads;
+    return true;
 }
 
 // Disc parameters for a launch; validates like prep_elem_loop (navier_stokes_fv1.cpp:136-199)
@@ -106,6 +142,17 @@ bool Disc::params(DiscParams& P, bool transient, double dt) {
     P.stab = stabType; P.diffLen = diffLen;
     P.stokes = stokes; P.laplace = laplace; P.peclet = peclet; P.hasSource = hasSource; P.transient = transient ? 1 : 0;
     P.pac = pac ? 1 : 0;
+    P.ipws = d_ipws;
+    P.ipwsStride = ipwsThreads;
+    return true;
+}
+
+// the positive-upwind workspace of a launch (allocated here at the latest)
+bool Disc::bind_ipws(DiscParams& P) {
+    if (!uses_ipshape(P) || P.ipws) return true;
+    if (!ensure_ipws()) return false;
+    P.ipws = d_ipws;
+    P.ipwsStride = ipwsThreads;
     return true;
 }
 
@@ -131,6 +178,11 @@ bool Disc::check_err_word(cudaStream_t s) {
     if (err & 1) {
         cudaMemsetAsync(d_err, 0, sizeof(int), s);
         return fail(NSFV1_ERR_GEOMETRY, "GetLinearProfileSkewedUpwindShapes: Cannot find cut side.");
+    }
+    if (err & 8) {
+        // the non-diagonal stabilisation's ip-ip system (stabilization.cpp:299, 641)
+        cudaMemsetAsync(d_err, 0, sizeof(int), s);
+        return fail(NSFV1_ERR_BREAKDOWN, "Could not compute inverse.");
     }
     return true;
 }
@@ -269,7 +321,7 @@ int nsfv1_set_upwind(nsfv1_disc* h, const char* name) {
     const int t = upwind_id(name);
     if (t < 0) {
         D->fail(NSFV1_ERR_ARGUMENT, std::string("NavierStokes: upwind type '") + (name ? name : "") +
-                "' not found. Options are: no, full, skewed, LinearProfileSkewed (lps)");
+                "' not found. Options are: no, full, skewed, LinearProfileSkewed (lps), positive (pos)");
         return D->status;
     }
     D->pac = false;   // set_upwind(name) clears the stabilisation-as-upwind (m_spConvStab = SPNULL)
@@ -279,6 +331,7 @@ int nsfv1_set_upwind(nsfv1_disc* h, const char* name) {
     D->convUpwindType = t; D->convUpwindSet = true;
     if (D->stabSet && D->stabUpwindType < 0) { D->stabUpwindType = t; D->stabSharesConv = true; }
     else D->stabSharesConv = false;
+    if (D->d_err && !D->ensure_ipws()) return D->status;   // the device is in use: allocate now
     return NSFV1_OK;
 }
 
@@ -321,6 +374,7 @@ int nsfv1_set_stabilization_upwind(nsfv1_disc* h, const char* name) {
     if (t < 0) { D->fail(NSFV1_ERR_ARGUMENT, std::string("NavierStokes: upwind type '") + (name ? name : "") + "' not found."); return D->status; }
     if (!D->stabSet) { D->fail(NSFV1_ERR_STATE, "Stabilization has not been set."); return D->status; }
     D->stabUpwindType = t; D->stabSharesConv = false;
+    if (D->d_err && !D->ensure_ipws()) return D->status;   // the device is in use: allocate now
     return NSFV1_OK;
 }
 
@@ -371,6 +425,7 @@ int nsfv1_set_mesh(nsfv1_disc* h, int elem_type, int64_t n_nodes, const double* 
             if (!D->cuda_ok(cudaMalloc((void**)&D->d_err, sizeof(int)), "alloc err")) return D->status;
         }
         if (!D->cuda_ok(cudaMemset(D->d_err, 0, sizeof(int)), "memset err")) return D->status;
+        if (!D->ensure_ipws()) return D->status;
         D->nDir = 0;
         D->free_workspace();
         D->hasMesh = true;
@@ -504,9 +559,123 @@ bool side_bf_normals(int dim, int nco, const double (*x)[3], const double* elemC
     return true;
 }
 
+// The element of every boundary side (the one element that has all of its nodes);
+// false (with the disc's error set) for a bad side.
+bool side_owners(Disc* D, int64_t n_sides, int side_nco, const int32_t* side_nodes, const std::string& who, std::vector<int64_t>& owner) {
+    const int dim = D->dim, nsh = D->nsh;
+    if (n_sides < 0 || (n_sides > 0 && !side_nodes) || (dim == 2 && side_nco != 2) || (dim == 3 && side_nco != 3 && side_nco != 4))
+        return D->fail(NSFV1_ERR_ARGUMENT, who + ": sides of 2 (2D) or 3 / 4 (3D) nodes");
+    for (int64_t k = 0; k < n_sides * side_nco; ++k)
+        if (side_nodes[k] < 0 || side_nodes[k] >= D->nNodes) return D->fail(NSFV1_ERR_ARGUMENT, who + ": node out of range");
+    std::vector<int64_t> nptr(D->nNodes + 1, 0);
+    for (int64_t k = 0; k < D->nElems * nsh; ++k) nptr[D->connHost[k] + 1]++;
+    for (int64_t r = 0; r < D->nNodes; ++r) nptr[r + 1] += nptr[r];
+    std::vector<int32_t> nel(nptr[D->nNodes]);
+    {
+        std::vector<int64_t> fill(nptr.begin(), nptr.end() - 1);
+        for (int64_t e = 0; e < D->nElems; ++e)
+            for (int i = 0; i < nsh; ++i) nel[fill[D->connHost[e * nsh + i]]++] = (int32_t)e;
+    }
+    owner.assign(n_sides, -1);
+    for (int64_t sIdx = 0; sIdx < n_sides; ++sIdx) {
+        const int32_t* sn = side_nodes + sIdx * side_nco;
+        int owners = 0;
+        for (int64_t q = nptr[sn[0]]; q < nptr[sn[0] + 1]; ++q) {
+            const int64_t e = nel[q];
+            bool all = true;
+            for (int j = 1; j < side_nco && all; ++j) {
+                bool has = false;
+                for (int i = 0; i < nsh; ++i) has |= D->connHost[e * nsh + i] == sn[j];
+                all = has;
+            }
+            if (all) { owner[sIdx] = e; ++owners; }
+        }
+        if (owners != 1)
+            return D->fail(NSFV1_ERR_ARGUMENT, who + ": side " + std::to_string(sIdx) + " is not a boundary side of exactly one element");
+    }
+    return true;
+}
+
+double ref_co(int roid, int c, int d) {
+    switch (roid) {
+        case ROID_TRIANGLE: return Ref<ROID_TRIANGLE>::co(c, d);
+        case ROID_QUADRILATERAL: return Ref<ROID_QUADRILATERAL>::co(c, d);
+        case ROID_TETRAHEDRON: return Ref<ROID_TETRAHEDRON>::co(c, d);
+        case ROID_HEXAHEDRON: return Ref<ROID_HEXAHEDRON>::co(c, d);
+    }
+    return 0.0;
+}
+
 }  // namespace
 
 extern "C" {
+
+int nsfv1_add_outflow(nsfv1_disc* h, int64_t n_sides, int side_nco, const int32_t* side_nodes) {
+    NSFV1_H;
+    const int dim = D->dim, nsh = D->nsh;
+    const std::string who = "NavierStokesNoNormalStressOutflow::add";
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, who + ": no mesh"); return D->status; }
+    std::vector<int64_t> owner;
+    if (!side_owners(D, n_sides, side_nco, side_nodes, who, owner)) return D->status;
+    for (int64_t sIdx = 0; sIdx < n_sides; ++sIdx) {
+        const int32_t* sn = side_nodes + sIdx * side_nco;
+        const int64_t e = owner[sIdx];
+        double x[4][3] = {{0}}, cen[3] = {0, 0, 0}, nrm[4][3], lx[4][3] = {{0}}, lsc[3] = {0, 0, 0};
+        int loc[4] = {0, 0, 0, 0};
+        for (int j = 0; j < side_nco; ++j) {
+            for (int d = 0; d < dim; ++d) x[j][d] = D->coordsHost[(size_t)sn[j] * dim + d];
+            for (int i = 0; i < nsh; ++i)
+                if (D->connHost[e * nsh + i] == sn[j]) loc[j] = i;
+            for (int d = 0; d < dim; ++d) {
+                lx[j][d] = ref_co(D->roid, loc[j], d);
+                lsc[d] += lx[j][d] / side_nco;
+            }
+        }
+        for (int i = 0; i < nsh; ++i)
+            for (int d = 0; d < dim; ++d) cen[d] += D->coordsHost[(size_t)D->connHost[e * nsh + i] * dim + d] / nsh;
+        if (!side_bf_normals(dim, side_nco, x, cen, nrm)) {
+            D->fail(NSFV1_ERR_GEOMETRY, who + ": degenerate side " + std::to_string(sIdx));
+            return D->status;
+        }
+        for (int j = 0; j < side_nco; ++j) {
+            // the face {corner, side-edge midpoints, side centre}: its integration point is the
+            // mean of those points in local coordinates (2D: {corner, side midpoint})
+            Disc::OutflowFace f;
+            f.node = sn[j];
+            f.elem = (int32_t)e;
+            f.local = loc[j];
+            for (int d = 0; d < 3; ++d) { f.n[d] = nrm[j][d]; f.xi[d] = 0.0; }
+            if (dim == 2) {
+                const int o = 1 - j;
+                for (int d = 0; d < 2; ++d) f.xi[d] = 0.5 * (lx[j][d] + 0.5 * (lx[j][d] + lx[o][d]));
+            } else {
+                const int nx = (j + 1) % side_nco, pv = (j + side_nco - 1) % side_nco;
+                for (int d = 0; d < 3; ++d)
+                    f.xi[d] = 0.25 * (lx[j][d] + 0.5 * (lx[j][d] + lx[nx][d]) + lsc[d] + 0.5 * (lx[pv][d] + lx[j][d]));
+            }
+            D->outflowHost.push_back(f);
+        }
+    }
+    // faces grouped by node (stable: a node's faces keep the order they were added in)
+    std::vector<Disc::OutflowFace> fs = D->outflowHost;
+    std::stable_sort(fs.begin(), fs.end(), [](const Disc::OutflowFace& a, const Disc::OutflowFace& c) { return a.node < c.node; });
+    std::vector<int32_t> seg, el, lo;
+    std::vector<double> xi, nr;
+    for (size_t k = 0; k < fs.size(); ++k) {
+        if (k == 0 || fs[k].node != fs[k - 1].node) seg.push_back((int32_t)k);
+        el.push_back(fs[k].elem);
+        lo.push_back(fs[k].local);
+        for (int d = 0; d < 3; ++d) { xi.push_back(fs[k].xi[d]); nr.push_back(fs[k].n[d]); }
+    }
+    seg.push_back((int32_t)fs.size());
+    D->free_outflow();
+    if (!D->cuda_ok(dupload(D->d_ofSeg, seg.data(), seg.size()), "outflow") || !D->cuda_ok(dupload(D->d_ofElem, el.data(), el.size()), "outflow") ||
+        !D->cuda_ok(dupload(D->d_ofLocal, lo.data(), lo.size()), "outflow") || !D->cuda_ok(dupload(D->d_ofXi, xi.data(), xi.size()), "outflow") ||
+        !D->cuda_ok(dupload(D->d_ofN, nr.data(), nr.size()), "outflow"))
+        return D->status;
+    D->nOfSeg = (int32_t)seg.size() - 1;
+    return NSFV1_OK;
+}
 
 int nsfv1_add_dirichlet(nsfv1_disc* h, int64_t n, const int32_t* dofs, const double* values) {
     NSFV1_H;
@@ -536,45 +705,16 @@ int nsfv1_add_inflow(nsfv1_disc* h, int64_t n_sides, int side_nco, const int32_t
     NSFV1_H;
     const int dim = D->dim, b = dim + 1, nsh = D->nsh;
     if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "NavierStokesInflow::add: no mesh"); return D->status; }
-    if (n_sides < 0 || (n_sides > 0 && (!side_nodes || !vel)) || (dim == 2 && side_nco != 2) || (dim == 3 && side_nco != 3 && side_nco != 4)) {
-        D->fail(NSFV1_ERR_ARGUMENT, "NavierStokesInflow::add: sides of 2 (2D) or 3 / 4 (3D) nodes and a velocity of dim components");
-        return D->status;
-    }
-    for (int64_t k = 0; k < n_sides * side_nco; ++k)
-        if (side_nodes[k] < 0 || side_nodes[k] >= D->nNodes) { D->fail(NSFV1_ERR_ARGUMENT, "NavierStokesInflow::add: node out of range"); return D->status; }
-    // node -> incident elements
-    std::vector<int64_t> nptr(D->nNodes + 1, 0);
-    for (int64_t k = 0; k < D->nElems * nsh; ++k) nptr[D->connHost[k] + 1]++;
-    for (int64_t r = 0; r < D->nNodes; ++r) nptr[r + 1] += nptr[r];
-    std::vector<int32_t> nel(nptr[D->nNodes]);
-    {
-        std::vector<int64_t> fill(nptr.begin(), nptr.end() - 1);
-        for (int64_t e = 0; e < D->nElems; ++e)
-            for (int i = 0; i < nsh; ++i) nel[fill[D->connHost[e * nsh + i]]++] = (int32_t)e;
-    }
+    if (n_sides > 0 && !vel) { D->fail(NSFV1_ERR_ARGUMENT, "NavierStokesInflow::add: a velocity of dim components is needed"); return D->status; }
+    std::vector<int64_t> owners;
+    if (!side_owners(D, n_sides, side_nco, side_nodes, "NavierStokesInflow::add", owners)) return D->status;
     std::vector<double> flux = D->bndFluxHost;
     flux.resize(D->nNodes, 0.0);
     std::vector<int32_t> dofs;
     std::vector<double> vals;
     for (int64_t sIdx = 0; sIdx < n_sides; ++sIdx) {
         const int32_t* sn = side_nodes + sIdx * side_nco;
-        // the one element that has every node of the side
-        int64_t owner = -1;
-        int owners = 0;
-        for (int64_t q = nptr[sn[0]]; q < nptr[sn[0] + 1]; ++q) {
-            const int64_t e = nel[q];
-            bool all = true;
-            for (int j = 1; j < side_nco && all; ++j) {
-                bool has = false;
-                for (int i = 0; i < nsh; ++i) has |= D->connHost[e * nsh + i] == sn[j];
-                all = has;
-            }
-            if (all) { owner = e; ++owners; }
-        }
-        if (owners != 1) {
-            D->fail(NSFV1_ERR_ARGUMENT, "NavierStokesInflow::add: side " + std::to_string(sIdx) + " is not a boundary side of exactly one element");
-            return D->status;
-        }
+        const int64_t owner = owners[sIdx];
         double x[4][3] = {{0}}, cen[3] = {0, 0, 0}, nrm[4][3];
         for (int j = 0; j < side_nco; ++j)
             for (int d = 0; d < dim; ++d) x[j][d] = D->coordsHost[(size_t)sn[j] * dim + d];
@@ -598,6 +738,8 @@ int nsfv1_add_inflow(nsfv1_disc* h, int64_t n_sides, int side_nco, const int32_t
 
 int nsfv1_clear_boundary(nsfv1_disc* h) {
     NSFV1_H;
+    D->free_outflow();
+    D->outflowHost.clear();
     dfree(D->d_bndFlux);
     D->bndFluxHost.clear();
     dfree(D->d_dirRow);
@@ -635,10 +777,76 @@ int nsfv1_elem_batch(nsfv1_disc* h, int elem_type, int64_t n, const double* corn
         if (!D->cuda_ok(cudaMalloc((void**)&D->d_err, sizeof(int)), "alloc err")) return D->status;
         cudaMemset(D->d_err, 0, sizeof(int));
     }
+    if (n > 0 && !D->bind_ipws(P)) return D->status;
     ElemBatchArgs a{n, corners, u, u_old, defA, jacA, defM, jacM, rhs, D->d_err};
     cudaStream_t s = (cudaStream_t)stream;
     if (!D->cuda_ok(launch_elem_batch(elem_type, P, a, s), "elem_batch")) return D->status;
     return D->check_err_word(s) ? NSFV1_OK : D->status;
+}
+
+int nsfv1_export(nsfv1_disc* h, int which, int elem_type, int64_t n, const double* corners, const double* u, const double* u_old, double dt,
+                 int ip_kind, int nip, const double* local_ips, double* values, double* derivs, void* stream) {
+    NSFV1_H;
+    const int dim = ref_dim(elem_type);
+    if (dim != D->dim) { D->fail(NSFV1_ERR_ARGUMENT, "element dimension does not match the disc"); return D->status; }
+    if (which < NSFV1_EX_VELOCITY || which > NSFV1_EX_PRESSURE_GRAD) { D->fail(NSFV1_ERR_ARGUMENT, "export: unknown export id"); return D->status; }
+    if (ip_kind < NSFV1_IPS_SCVF || ip_kind > NSFV1_IPS_GIVEN) { D->fail(NSFV1_ERR_ARGUMENT, "export: unknown kind of points"); return D->status; }
+    if (ip_kind == NSFV1_IPS_GIVEN && (nip < 1 || nip > kMaxExportPoints || !local_ips)) {
+        D->fail(NSFV1_ERR_ARGUMENT, "export: 1 to " + std::to_string(kMaxExportPoints) + " given local points needed");
+        return D->status;
+    }
+    if (n < 0 || (n > 0 && (!corners || !u || !values))) { D->fail(NSFV1_ERR_ARGUMENT, "export: bad arguments"); return D->status; }
+    DiscParams P;
+    if (!D->params(P, u_old != nullptr, dt)) return D->status;
+    if (n == 0) return NSFV1_OK;
+    if (!D->d_err) {
+        if (!D->cuda_ok(cudaMalloc((void**)&D->d_err, sizeof(int)), "alloc err")) return D->status;
+        cudaMemset(D->d_err, 0, sizeof(int));
+    }
+    // the per-SCVF state of the stabilised ip velocity lives in the element path's workspace
+    if (!D->ensure_ipws(true)) return D->status;
+    P.ipws = D->d_ipws;
+    P.ipwsStride = D->ipwsThreads;
+    ExportArgs a{};
+    a.which = which; a.ipKind = ip_kind; a.nip = ip_kind == NSFV1_IPS_GIVEN ? nip : 0; a.n = n;
+    a.corners = corners; a.u = u; a.uold = u_old; a.values = values; a.derivs = derivs; a.err = D->d_err;
+    if (ip_kind == NSFV1_IPS_GIVEN)
+        for (int i = 0; i < nip; ++i)
+            for (int d = 0; d < 3; ++d) a.lips[i][d] = d < dim ? local_ips[i * dim + d] : 0.0;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!D->cuda_ok(launch_export(elem_type, P, a, s), "export")) return D->status;
+    return D->check_err_word(s) ? NSFV1_OK : D->status;
+}
+
+int nsfv1_vorticity(nsfv1_disc* h, const double* u, double* vort, void* stream) {
+    NSFV1_H;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "vorticity: no mesh set"); return D->status; }
+    if (!u || !vort) { D->fail(NSFV1_ERR_ARGUMENT, "vorticity: null vector"); return D->status; }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!D->d_nodeVol && !D->cuda_ok(cudaMalloc((void**)&D->d_nodeVol, sizeof(double) * D->nNodes), "vorticity scratch")) return D->status;
+    if (!D->cuda_ok(cudaMemsetAsync(vort, 0, sizeof(double) * D->nNodes, s), "memset") ||
+        !D->cuda_ok(cudaMemsetAsync(D->d_nodeVol, 0, sizeof(double) * D->nNodes, s), "memset"))
+        return D->status;
+    for (int c = 0; c < D->nColors; ++c) {
+        AsmArgs a{D->d_coords, D->d_conn, D->d_elemBlk, D->d_colorElems + D->colorPtr[c], D->colorPtr[c + 1] - D->colorPtr[c], D->d_err,
+                  u, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, D->nNodes, (int64_t)D->colIdx.size()};
+        if (!D->cuda_ok(launch_vorticity(D->roid, a, vort, D->d_nodeVol, s), "vorticity")) return D->status;
+    }
+    if (!D->cuda_ok(launch_divide(D->nNodes, vort, D->d_nodeVol, s), "vorticity")) return D->status;
+    return D->check_err_word(s) ? NSFV1_OK : D->status;
+}
+
+int nsfv1_eval_points(nsfv1_disc* h, const double* u, int64_t n, const double* points, int fct, double* values, void* stream) {
+    NSFV1_H;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "eval_points: no mesh set"); return D->status; }
+    if (n < 0 || (n > 0 && (!u || !points || !values)) || fct < 0 || fct > D->dim) {
+        D->fail(NSFV1_ERR_ARGUMENT, "eval_points: bad arguments");
+        return D->status;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!D->cuda_ok(launch_eval_points(D->roid, D->nElems, D->nNodes, D->d_coords, D->d_conn, u, n, points, fct, values, s), "eval_points"))
+        return D->status;
+    return D->cuda_ok(cudaStreamSynchronize(s), "eval_points") ? NSFV1_OK : D->status;
 }
 
 int nsfv1_elem_batch_host(nsfv1_disc* h, int elem_type, int64_t n, const double* corners, const double* u, const double* u_old,
@@ -778,7 +986,7 @@ bool Disc::assemble_defect(const double* u, const double* u_old, double dt, doub
     if (!hasMesh) return fail(NSFV1_ERR_STATE, "assemble_defect: no mesh set");
     if (!u || !d) return fail(NSFV1_ERR_ARGUMENT, "assemble_defect: null vector");
     DiscParams P;
-    if (!params(P, u_old != nullptr, dt)) return false;
+    if (!params(P, u_old != nullptr, dt) || !bind_ipws(P)) return false;
     const int b = dim + 1;
     if (!cuda_ok(cudaMemsetAsync(d, 0, sizeof(double) * nNodes * b, s), "memset defect")) return false;
     for (int c = 0; c < nColors; ++c) {
@@ -786,6 +994,7 @@ bool Disc::assemble_defect(const double* u, const double* u_old, double dt, doub
                   d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive, nNodes, (int64_t)colIdx.size()};
         if (!cuda_ok(launch_defect(roid, P, a, s, asmThreads), "defect kernel")) return false;
     }
+    if (!outflow_terms(P, u, d, nullptr, 0, s)) return false;
     if (!cuda_ok(launch_bnd_flux(b, nNodes, u_old ? dt : 1.0, d_bndFlux, d, s), "inflow flux")) return false;
     if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, d, nullptr, 0, s), "dirichlet")) return false;
     return check_err_word(s);
@@ -798,7 +1007,7 @@ bool Disc::assemble_defect_jacobian(const double* u, const double* u_old, double
     if (prec == NSFV1_F32 && dim == 3 && (reinterpret_cast<uintptr_t>(vals) & 15))
         return fail(NSFV1_ERR_ARGUMENT, "assemble_defect_jacobian: FP32 values of a 3D mesh must be 16-byte aligned");
     DiscParams P;
-    if (!params(P, u_old != nullptr, dt)) return false;
+    if (!params(P, u_old != nullptr, dt) || !bind_ipws(P)) return false;
     const int b = dim + 1;
     if (!cuda_ok(cudaMemsetAsync(d, 0, sizeof(double) * nNodes * b, s), "memset defect")) return false;
     const size_t vsize = prec == NSFV1_F64 ? sizeof(double) : sizeof(float);
@@ -808,6 +1017,7 @@ bool Disc::assemble_defect_jacobian(const double* u, const double* u_old, double
                   d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive, nNodes, (int64_t)colIdx.size()};
         if (!cuda_ok(launch_defect_jacobian(roid, P, a, prec, s, asmThreads), "defect+jacobian kernel")) return false;
     }
+    if (!outflow_terms(P, u, d, vals, prec, s)) return false;
     if (!cuda_ok(launch_bnd_flux(b, nNodes, u_old ? dt : 1.0, d_bndFlux, d, s), "inflow flux")) return false;
     if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, d, vals, prec, s), "dirichlet")) return false;
     return check_err_word(s);
@@ -820,7 +1030,7 @@ bool Disc::assemble_jacobian(const double* u, const double* u_old, double dt, vo
     if (prec == NSFV1_F32 && dim == 3 && (reinterpret_cast<uintptr_t>(vals) & 15))
         return fail(NSFV1_ERR_ARGUMENT, "assemble_jacobian: FP32 values of a 3D mesh must be 16-byte aligned");
     DiscParams P;
-    if (!params(P, u_old != nullptr, dt)) return false;
+    if (!params(P, u_old != nullptr, dt) || !bind_ipws(P)) return false;
     const int b = dim + 1;
     const size_t bytes = colIdx.size() * b * b * (prec == NSFV1_F64 ? sizeof(double) : sizeof(float));
     if (!cuda_ok(cudaMemsetAsync(vals, 0, bytes, s), "memset jacobian")) return false;
@@ -829,6 +1039,7 @@ bool Disc::assemble_jacobian(const double* u, const double* u_old, double dt, vo
                   d_nuElem, instSkip ? d_elemInst : nullptr, d_instActive, nNodes, (int64_t)colIdx.size()};
         if (!cuda_ok(launch_jacobian(roid, P, a, prec, s, asmThreads), "jacobian kernel")) return false;
     }
+    if (!outflow_terms(P, u, nullptr, vals, prec, s)) return false;
     if (!cuda_ok(launch_dirichlet(b, nDir, d_dirRow, d_dirVal, d_rowPtr, d_colIdx, u, nullptr, vals, prec, s), "dirichlet")) return false;
     return sync ? check_err_word(s) : true;
 }

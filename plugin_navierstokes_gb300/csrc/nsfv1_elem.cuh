@@ -126,6 +126,14 @@ struct Elem {
     T JtInv[3][3];      // constant J^-T of an affine element
 };
 
+// -v by flipping the sign bit with an integer XOR: exact like the negation
+// itself, and it keeps the negated copies of the fluxes and Jacobian entries
+// (one per entry of every 'to' row) off the FP64 / FP32 arithmetic pipes
+__device__ __forceinline__ double flip_sign(const double v) {
+    return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ULL);
+}
+__device__ __forceinline__ float flip_sign(const float v) { return __int_as_float(__float_as_int(v) ^ (int)0x80000000u); }
+
 // Affine test: simplices always; a quadrilateral / hexahedron when every corner
 // equals x0 + the sum of its edge vectors to within rtol of the element size.
 // On such elements the mapping Jacobian is one constant matrix and the FV1
@@ -345,6 +353,39 @@ __device__ __forceinline__ void ip_geom(const Elem<ROID, T>& E, const int ip, Ip
             J[r][c] = s;
         }
     jt_inverse<dim, T>(J, G.JtInv);
+}
+
+// P1 shapes and local gradients at the local point x (the element's trial space:
+// linear on simplices, multilinear on quadrilaterals / hexahedra, ugcore corner order)
+template <int ROID>
+__device__ __forceinline__ void p1_eval(const double* x, double (&N)[Ref<ROID>::nsh], double (&G)[Ref<ROID>::nsh][3]) {
+    const double a = x[0], b = x[1], c = x[2];
+    if constexpr (ROID == ROID_TRIANGLE) {
+        N[0] = 1.0 - a - b; N[1] = a; N[2] = b;
+        G[0][0] = -1.0; G[0][1] = -1.0; G[1][0] = 1.0; G[1][1] = 0.0; G[2][0] = 0.0; G[2][1] = 1.0;
+    } else if constexpr (ROID == ROID_QUADRILATERAL) {
+        N[0] = (1.0 - a) * (1.0 - b); N[1] = a * (1.0 - b); N[2] = a * b; N[3] = (1.0 - a) * b;
+        G[0][0] = -(1.0 - b); G[0][1] = -(1.0 - a); G[1][0] = 1.0 - b; G[1][1] = -a;
+        G[2][0] = b;          G[2][1] = a;          G[3][0] = -b;      G[3][1] = 1.0 - a;
+    } else if constexpr (ROID == ROID_TETRAHEDRON) {
+        N[0] = 1.0 - a - b - c; N[1] = a; N[2] = b; N[3] = c;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) G[k][d] = (k == 0) ? -1.0 : (k == d + 1 ? 1.0 : 0.0);
+    } else {
+        const double ma = 1.0 - a, mb = 1.0 - b, mc = 1.0 - c;
+        N[0] = ma * mb * mc; N[1] = a * mb * mc; N[2] = a * b * mc; N[3] = ma * b * mc;
+        N[4] = ma * mb * c;  N[5] = a * mb * c;  N[6] = a * b * c;  N[7] = ma * b * c;
+        G[0][0] = -mb * mc; G[0][1] = -ma * mc; G[0][2] = -ma * mb;
+        G[1][0] = mb * mc;  G[1][1] = -a * mc;  G[1][2] = -a * mb;
+        G[2][0] = b * mc;   G[2][1] = a * mc;   G[2][2] = -a * b;
+        G[3][0] = -b * mc;  G[3][1] = ma * mc;  G[3][2] = -ma * b;
+        G[4][0] = -mb * c;  G[4][1] = -ma * c;  G[4][2] = ma * mb;
+        G[5][0] = mb * c;   G[5][1] = -a * c;   G[5][2] = a * mb;
+        G[6][0] = b * c;    G[6][1] = a * c;    G[6][2] = a * b;
+        G[7][0] = -b * c;   G[7][1] = ma * c;   G[7][2] = ma * b;
+    }
 }
 
 // global gradient of shape k at the SCVF ip
@@ -926,9 +967,9 @@ __device__ __forceinline__ void scvf_def_A(const DiscParams& P, const Elem<ROID,
     for (int d = 0; d < dim; ++d) contFlux += stabVel[d] * G.n[d];
     contFlux *= rho;
 #pragma unroll
-    for (int d1 = 0; d1 < dim; ++d1) { sink.add(G.from, d1, flux[d1]); sink.add(G.to, d1, -flux[d1]); }
+    for (int d1 = 0; d1 < dim; ++d1) { sink.add(G.from, d1, flux[d1]); sink.add(G.to, d1, flip_sign(flux[d1])); }
     sink.add(G.from, Pc, contFlux);
-    sink.add(G.to, Pc, -contFlux);
+    sink.add(G.to, Pc, flip_sign(contFlux));
 }
 
 template <int ROID, typename T, class DSink>

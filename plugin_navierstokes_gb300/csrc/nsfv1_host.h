@@ -60,11 +60,24 @@ struct Disc {
     // continuity-row flux of inflow boundaries (nsfv1_add_inflow), per node; added to the defect
     std::vector<double> bndFluxHost;
     double* d_bndFlux = nullptr;
+    double* d_nodeVol = nullptr;    // nsfv1_vorticity scratch: SCV volume per node
+    // outflow boundary faces without normal stress (nsfv1_add_outflow), grouped by node
+    struct OutflowFace {
+        int32_t node, elem, local;
+        double xi[3], n[3];
+    };
+    std::vector<OutflowFace> outflowHost;
+    int32_t *d_ofSeg = nullptr, *d_ofElem = nullptr, *d_ofLocal = nullptr;
+    double *d_ofXi = nullptr, *d_ofN = nullptr;
+    int32_t nOfSeg = 0;
     double* d_bjDinv = nullptr;     // nsfv1_block_jacobi scratch: inverted diagonal blocks
     int32_t* d_dirRow = nullptr;
     double* d_dirVal = nullptr;
     int64_t nDir = 0;
     int* d_err = nullptr;
+    // workspace of the positive-upwind element path (allocated when such an upwind is set)
+    double* d_ipws = nullptr;
+    int64_t ipwsThreads = 0;
     int asmThreads = 32;            // CTA size of the assembly colour launches
 
     Workspace ws;
@@ -75,11 +88,15 @@ struct Disc {
 
     ~Disc();
     void free_mesh();
+    void free_outflow();
+    bool outflow_terms(const DiscParams& P, const double* u, double* d, void* vals, int prec, cudaStream_t s);
     void free_workspace();
     bool fail(int code, const std::string& msg);
     bool cuda_ok(cudaError_t e, const char* where);
     bool check_err_word(cudaStream_t s);
     bool params(DiscParams& P, bool transient, double dt);
+    bool ensure_ipws(bool force = false);   // allocates d_ipws if a positive upwind is configured (or force)
+    bool bind_ipws(DiscParams& P);   // P.ipws for a launch that needs it
     bool assemble_defect(const double* u, const double* u_old, double dt, double* d, cudaStream_t s);
     bool assemble_jacobian(const double* u, const double* u_old, double dt, void* vals, int prec, cudaStream_t s, bool sync = true);
     bool assemble_defect_jacobian(const double* u, const double* u_old, double dt, double* d, void* vals, int prec, cudaStream_t s);

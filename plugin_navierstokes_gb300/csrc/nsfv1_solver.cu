@@ -452,15 +452,22 @@ __global__ void k_multi_axpy_add(int64_t n, int m, const double* __restrict__ y,
 
 static inline int grid_for(int64_t n, int t = 256) { return (int)((n + t - 1) / t); }
 
+// Lanes per block row: a row of the FV1 patterns holds 7 (triangles) to 27
+// (hexahedra) blocks. With 4 lanes per 3x3-block row each lane takes about two
+// blocks and the butterfly over the lanes has two levels instead of three; on a
+// 1025^2-row, 7-blocks-per-row FP32 matrix the double-float SpMV went from 112.8
+// to 88.2 us (8 -> 4 lanes; 2 lanes: 87.9 us, 1 lane: 105.0 us, loads uncoalesced).
+template <int b> constexpr int spmv_lanes() { return b == 4 ? 8 : 4; }
+
 template <typename MT, typename VT>
 static cudaError_t spmv(const Disc& D, const MT* vals, const VT* x, VT* y, cudaStream_t s) {
     const int64_t nR = D.nNodes;
     const int b = D.dim + 1;
     if (b == 4) {
-        constexpr int G = 16;
+        constexpr int G = spmv_lanes<4>();
         k_bsr_mv<MT, VT, 4, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y);
     } else {
-        constexpr int G = 8;
+        constexpr int G = spmv_lanes<3>();
         k_bsr_mv<MT, VT, 3, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y);
     }
     return cudaGetLastError();
@@ -809,13 +816,10 @@ int nsfv1_bsr_mv(nsfv1_disc* h, const void* vals, int prec, const double* x, dou
     D->status = NSFV1_OK;
     if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "bsr_mv: no mesh"); return D->status; }
     cudaStream_t s = (cudaStream_t)stream;
-    const int64_t nR = D->nNodes;
     if (prec == NSFV1_F64) {
-        if (D->dim == 3) k_bsr_mv<double, double, 4, 16><<<grid_for(nR * 16), 256, 0, s>>>(nR, D->d_rowPtr, D->d_colIdx, (const double*)vals, x, y);
-        else k_bsr_mv<double, double, 3, 8><<<grid_for(nR * 8), 256, 0, s>>>(nR, D->d_rowPtr, D->d_colIdx, (const double*)vals, x, y);
+        if (!D->cuda_ok(spmv<double, double>(*D, (const double*)vals, x, y, s), "bsr_mv")) return D->status;
     } else if (prec == NSFV1_F32) {
-        if (D->dim == 3) k_bsr_mv<float, double, 4, 16><<<grid_for(nR * 16), 256, 0, s>>>(nR, D->d_rowPtr, D->d_colIdx, (const float*)vals, x, y);
-        else k_bsr_mv<float, double, 3, 8><<<grid_for(nR * 8), 256, 0, s>>>(nR, D->d_rowPtr, D->d_colIdx, (const float*)vals, x, y);
+        if (!D->cuda_ok(spmv<float, double>(*D, (const float*)vals, x, y, s), "bsr_mv")) return D->status;
     } else {
         D->fail(NSFV1_ERR_ARGUMENT, "bsr_mv: bad precision");
         return D->status;

@@ -175,6 +175,52 @@ class NavierStokesFV1:
         self._c(self._lib.nsfv1_elem_batch(self._h, int(elem_type), n, _ptr(corners), _ptr(u), _ptr(u_old), float(dt),
                                            _ptr(defA), _ptr(jacA), _ptr(defM), _ptr(jacM), _ptr(rhs), _stream_ptr(stream)))
 
+    # ---- post-processing (navier_stokes_tools.h) ----
+    def vorticity(self, u, vort, stream=None) -> None:
+        """vorticityFV1: the SCV-averaged corner curl of the P1 velocity, one value per node."""
+        self._c(self._lib.nsfv1_vorticity(self._h, _ptr(u), _ptr(vort), _stream_ptr(stream)))
+
+    def eval_points(self, u, points, fct: int, stream=None):
+        """Function fct (0..dim) of the P1 solution u at global points [n][dim] (device tensor);
+        returns a device tensor of n values, NaN outside the mesh."""
+        import torch
+
+        pts = points.contiguous()
+        out = torch.empty(pts.shape[0], dtype=torch.float64, device=pts.device)
+        self._c(self._lib.nsfv1_eval_points(self._h, _ptr(u), pts.shape[0], _ptr(pts), int(fct), _ptr(out), _stream_ptr(stream)))
+        return out
+
+    # ---- data exports (navier_stokes_fv1.cpp:894-1491; the accessors of
+    # incompressible_navier_stokes_base.h:237-249) ----
+    def velocity(self) -> "DataExport":
+        return DataExport(self, EX_VELOCITY)
+
+    def velocity_grad(self) -> "DataExport":
+        return DataExport(self, EX_VELOCITY_GRAD)
+
+    def velocity_ip(self) -> "DataExport":
+        return DataExport(self, EX_VELOCITY_IP)
+
+    def pressure(self) -> "DataExport":
+        return DataExport(self, EX_PRESSURE)
+
+    def pressure_grad(self) -> "DataExport":
+        return DataExport(self, EX_PRESSURE_GRAD)
+
+    def export(self, which: int, elem_type: int, corners, u, values, u_old=None, dt: float = 0.0, points="scvf", derivs=None,
+               stream=None) -> None:
+        """Export `which` of n elements into device arrays values [n][nip][vs] and, if given,
+        derivs [n][nip][dim+1][corners][vs]; points "scvf", "scv" or a local-point array [nip][dim]."""
+        if isinstance(points, str):
+            kind, nip, lips = {"scvf": 0, "scv": 1}[points], 0, None
+        else:
+            lips = np.ascontiguousarray(points, np.float64)
+            kind, nip = 2, int(lips.shape[0])
+        n = corners.shape[0]
+        self._c(self._lib.nsfv1_export(self._h, int(which), int(elem_type), n, _ptr(corners), _ptr(u), _ptr(u_old), float(dt), kind,
+                                       nip, None if lips is None else lips.ctypes.data, _ptr(values), _ptr(derivs),
+                                       _stream_ptr(stream)))
+
     def bsr_mv(self, vals, x, y, stream=None) -> None:
         import torch
 
@@ -311,6 +357,39 @@ def mesh_pattern(elem_type: int, n_nodes: int, conn: np.ndarray):
     return rp, ci, col, nc.value
 
 
+EX_VELOCITY, EX_VELOCITY_GRAD, EX_VELOCITY_IP, EX_PRESSURE, EX_PRESSURE_GRAD = range(5)
+_NSCVF = {2: 3, 3: 4, 4: 6, 8: 12}
+_NSH = {2: 3, 3: 4, 4: 4, 8: 8}
+
+
+class DataExport:
+    """One of the disc's data exports (the reference's velocity(), velocity_grad(),
+    velocity_ip(), pressure(), pressure_grad() return a CplUserData that ugcore
+    evaluates per element at integration points): evaluate() runs it on the GPU for
+    a batch of elements and returns torch tensors (values, derivatives or None)."""
+
+    def __init__(self, disc: NavierStokesFV1, which: int):
+        self.disc, self.which = disc, which
+
+    def value_size(self) -> int:
+        dim = self.disc.dim
+        return {EX_VELOCITY: dim, EX_VELOCITY_GRAD: dim * dim, EX_VELOCITY_IP: dim, EX_PRESSURE: 1, EX_PRESSURE_GRAD: dim}[self.which]
+
+    def evaluate(self, elem_type: int, corners, u, u_old=None, dt: float = 0.0, points="scvf", derivs: bool = False, stream=None):
+        import torch
+
+        n = corners.shape[0]
+        if isinstance(points, str):
+            nip = {"scvf": _NSCVF[elem_type], "scv": _NSH[elem_type]}[points]
+        else:
+            nip = int(np.asarray(points).shape[0])
+        vs = self.value_size()
+        vals = torch.empty((n, nip, vs), dtype=torch.float64, device=corners.device)
+        der = torch.empty((n, nip, self.disc.dim + 1, _NSH[elem_type], vs), dtype=torch.float64, device=corners.device) if derivs else None
+        self.disc.export(self.which, elem_type, corners, u, vals, u_old, dt, points, der, stream)
+        return vals, der
+
+
 class NavierStokesWall:
     """``NavierStokesWall(master)`` (incompressible/bnd/wall.h, wall_impl.h:44-69):
     ``add(nodes)`` makes every velocity component of the nodes a zero Dirichlet row.
@@ -342,3 +421,20 @@ class NavierStokesInflowFV1:
         if v.size != self.master.dim:
             raise NSFV1Error(_capi.ERR_ARGUMENT, "NavierStokesInflow::add: the velocity needs dim components")
         self.master._c(self.master._lib.nsfv1_add_inflow(self.master._h, sd.shape[0], sd.shape[1], sd.ctypes.data, v.ctypes.data))
+
+
+class NavierStokesNoNormalStressOutflowFV1:
+    """``NavierStokesNoNormalStressOutflowFV1(master)`` (incompressible/fv1/bnd/
+    no_normal_stress_outflow_fv1.cpp:343-504): ``add(sides)`` makes the given
+    boundary sides an outflow boundary without normal stress -- the tangential
+    viscous flux, the outgoing convective flux and the continuity flux of each
+    corner's boundary face enter the defect and the Jacobian (nsfv1_add_outflow).
+    ``sides`` is an (n_sides, nodes per side) array of node ids standing for the
+    reference's boundary subset names."""
+
+    def __init__(self, master: NavierStokesFV1):
+        self.master = master
+
+    def add(self, sides) -> None:
+        sd = np.ascontiguousarray(np.atleast_2d(np.asarray(sides, dtype=np.int32)))
+        self.master._c(self.master._lib.nsfv1_add_outflow(self.master._h, sd.shape[0], sd.shape[1], sd.ctypes.data))

@@ -27,6 +27,15 @@ DISC_CASES = [
     ("full", "flow", "raw", False, 0.0, False, False, True, False),
 ]
 
+# the positive upwind (ip shapes: the non-diagonal FIELDS / FLOW branches)
+POS_CASES = [
+    ("pos", "fields", "raw", False, 0.0, False, False, False, False),
+    ("pos", "flow", "raw", True, 1.0, False, False, False, True),
+    ("pos", "fields", "cor", True, 1.0, True, False, False, False),
+    ("pos", "flow", "fivepoint", False, 0.0, False, True, False, False),
+    ("pos", "without", "raw", False, 1.0, False, False, False, False),
+]
+
 
 def random_elements(roid: int, n: int, seed: int, h: float = 0.1, jitter: float = 0.15, affine: bool = False) -> np.ndarray:
     """n distorted copies of the reference element scaled by h (corner jitter

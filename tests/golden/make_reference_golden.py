@@ -20,7 +20,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 import oracle  # noqa: E402
-from _cases import DISC_CASES, DIM, ROIDS, random_elements, random_local_u, ref_config  # noqa: E402
+from _cases import DISC_CASES, DIM, POS_CASES, ROIDS, random_elements, random_local_u, ref_config  # noqa: E402
 
 DT = 0.01
 
@@ -48,6 +48,21 @@ def fixtures():
                 r = oracle.ref_elem_batch(roid, dict(ref_config(dim, cfg), pac=True), corners, u, uo, DT)
                 for k, v in r.items():
                     out[key + "_pac_" + k] = v
+        # the positive upwind (non-diagonal stabilisation), with and without PAC
+        for ci, cfg in enumerate(POS_CASES):
+            seed = 9000 + 1000 * roid + ci
+            corners = np.concatenate([random_elements(roid, n, seed), random_elements(roid, 2, seed + 7, affine=True)])
+            u = random_local_u(roid, n + 2, seed + 1, zero_frac=0.2)
+            uo = random_local_u(roid, n + 2, seed + 2) if cfg[3] else None
+            key = f"{tname}_pos{ci}"
+            out[key + "_corners"] = corners
+            out[key + "_u"] = u
+            if uo is not None:
+                out[key + "_uold"] = uo
+            for pac in (False, True):
+                r = oracle.ref_elem_batch(roid, dict(ref_config(dim, cfg), pac=pac), corners, u, uo, DT)
+                for k, v in r.items():
+                    out[key + ("_pac_" if pac else "_") + k] = v
     return out
 
 

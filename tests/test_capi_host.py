@@ -19,11 +19,14 @@ def test_library_exports_every_declared_symbol():
 def test_setters_string_ids_and_errors():
     d = NavierStokesFV1("u,v,p", "Inner")
     assert d.dim == 2 and d.disc_type() == "fv1"
-    for name in ["no", "FULL", " lps ", "LinearProfileSkewed", "skewed"]:
+    for name in ["no", "FULL", " lps ", "LinearProfileSkewed", "skewed", "positive", " POS"]:
         d.set_upwind(name)
     with pytest.raises(NSFV1Error) as ex:
         d.set_upwind("weighted")
     assert ex.value.status == _capi.ERR_ARGUMENT and "not found" in str(ex.value)
+    # the positive upwind's workspace comes with the first device use, not with the setter
+    d.set_stabilization("flow")
+    d.set_stabilization_upwind("pos")
     for name in ["fields", "Flow", "without"]:
         d.set_stabilization(name)
     d.set_stabilization("fields", "FivePoint")

@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 import oracle
-from _cases import DISC_CASES, DIM, NSH, ROIDS, cfg_name, configure, random_elements, random_local_u, ref_config, rel_err
+from _cases import DISC_CASES, DIM, NSH, POS_CASES, ROIDS, cfg_name, configure, random_elements, random_local_u, ref_config, rel_err
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_elements.npz")
 TOL = 1e-12
@@ -54,6 +54,69 @@ def test_oracle_pac_reproduces_the_reference_fixtures(tname, ci):
     r = o.elem_batch(roid, g[key + "_corners"], g[key + "_u"], uo, 0.01)
     for k in ("defA", "jacA", "defM", "jacM", "rhs"):
         assert rel_err(r[k], g[key + "_pac_" + k]) <= TOL, (key, "pac", k, rel_err(r[k], g[key + "_pac_" + k]))
+
+
+@pytest.mark.parametrize("tname", list(ROIDS))
+@pytest.mark.parametrize("ci", range(len(POS_CASES)))
+@pytest.mark.parametrize("pac", [False, True])
+def test_oracle_positive_upwind_reproduces_the_reference_fixtures(tname, ci, pac):
+    """The positive upwind (ip shapes) and the non-diagonal FIELDS / FLOW branches."""
+    g = np.load(GOLDEN)
+    roid = ROIDS[tname]
+    dim = DIM[roid]
+    key = f"{tname}_pos{ci}"
+    uo = g[key + "_uold"] if (key + "_uold") in g else None
+    o = oracle.Oracle(dim)
+    configure(o, dim, POS_CASES[ci])
+    if pac:
+        o.set_pac_upwind(True)
+    r = o.elem_batch(roid, g[key + "_corners"], g[key + "_u"], uo, 0.01)
+    tag = "_pac_" if pac else "_"
+    for k in ("defA", "jacA", "defM", "jacM", "rhs"):
+        assert rel_err(r[k], g[key + tag + k]) <= TOL, (key, pac, k, rel_err(r[k], g[key + tag + k]))
+
+
+@pytest.mark.skipif(not has_ref, reason="reference checkout not present")
+@pytest.mark.parametrize("tname", list(ROIDS))
+@pytest.mark.parametrize("ci", range(len(POS_CASES)))
+def test_oracle_positive_upwind_matches_the_reference_live(tname, ci):
+    roid = ROIDS[tname]
+    dim = DIM[roid]
+    cfg = POS_CASES[ci]
+    n = 40
+    corners = np.concatenate([random_elements(roid, n, 700 + 11 * ci + roid), random_elements(roid, 8, 800 + ci, affine=True)])
+    u = random_local_u(roid, n + 8, 900 + ci, zero_frac=0.1)
+    uo = random_local_u(roid, n + 8, 950 + ci) if cfg[3] else None
+    for pac in (False, True):
+        o = oracle.Oracle(dim)
+        configure(o, dim, cfg)
+        if pac:
+            o.set_pac_upwind(True)
+        mine = o.elem_batch(roid, corners, u, uo, 0.01)
+        ref = oracle.ref_elem_batch(roid, dict(ref_config(dim, cfg), pac=pac), corners, u, uo, 0.01)
+        for k in ref:
+            assert rel_err(mine[k], ref[k]) <= TOL, (tname, cfg_name(cfg), pac, k, rel_err(mine[k], ref[k]))
+
+
+@pytest.mark.skipif(not has_ref, reason="reference checkout not present")
+@pytest.mark.parametrize("tname", list(ROIDS))
+@pytest.mark.parametrize("conv,stab_up,stab", [("pos", "lps", "flow"), ("full", "pos", "fields"), ("lps", "pos", "flow")])
+def test_oracle_mixed_upwind_objects_match_the_reference_live(tname, conv, stab_up, stab):
+    """Convection and stabilisation with upwind objects of different kinds (one of them positive)."""
+    roid = ROIDS[tname]
+    dim = DIM[roid]
+    cfg = (conv, stab, "raw", True, 1.0, False, False, False, False)
+    n = 24
+    corners = random_elements(roid, n, 1200 + roid)
+    u = random_local_u(roid, n, 1300 + roid)
+    uo = random_local_u(roid, n, 1400 + roid)
+    o = oracle.Oracle(dim)
+    configure(o, dim, cfg)
+    o.set_stabilization_upwind(stab_up)
+    mine = o.elem_batch(roid, corners, u, uo, 0.01)
+    ref = oracle.ref_elem_batch(roid, dict(ref_config(dim, cfg), stab_upwind=stab_up), corners, u, uo, 0.01)
+    for k in ref:
+        assert rel_err(mine[k], ref[k]) <= TOL, (tname, conv, stab_up, k, rel_err(mine[k], ref[k]))
 
 
 @pytest.mark.skipif(not has_ref, reason="reference checkout not present")
@@ -168,3 +231,27 @@ def test_64_cavity_full_upwind_fields_stalls_with_the_reference_code():
     assert max(fields[-10:]) > 2 * min(fields[-10:])   # no monotone progress: a cycle
     flow = _ref_cavity_newton(64, "flow", 20)
     assert flow[-1] < 1e-8 and len(flow) <= 15, flow
+
+
+@pytest.mark.skipif(not has_ref, reason="reference checkout not present")
+@pytest.mark.parametrize("tname", list(ROIDS))
+@pytest.mark.parametrize("which", range(5))
+def test_oracle_exports_match_the_reference_live(tname, which):
+    """The data exports (navier_stokes_fv1.cpp:894-1491): values and derivatives at
+    the SCVF ips, the SCV ips and given local points, for both stabilisations with
+    and without the positive upwind (diagonal and non-diagonal branches)."""
+    roid = ROIDS[tname]
+    dim = DIM[roid]
+    rng = np.random.default_rng(which + 10 * roid)
+    lips = rng.random((5, dim)) * (0.3 if roid in (2, 4) else 1.0)
+    cases = [DISC_CASES[i] for i in (0, 1, 2, 3, 5)] + [POS_CASES[i] for i in (0, 1, 4)]
+    for ci, cfg in enumerate(cases):
+        corners = np.concatenate([random_elements(roid, 6, 2000 + ci + roid), random_elements(roid, 2, 2100 + ci, affine=True)])
+        u = random_local_u(roid, 8, 2200 + ci)
+        uo = random_local_u(roid, 8, 2300 + ci) if cfg[3] else None
+        for kind in (0, 1, 2):
+            o = oracle.Oracle(dim)
+            configure(o, dim, cfg)
+            v, d = o.export(which, roid, corners, u, uo, 0.01, kind, lips if kind == 2 else None)
+            rv, rd = oracle.ref_export(which, roid, ref_config(dim, cfg), corners, u, uo, 0.01, kind, lips if kind == 2 else None)
+            assert rel_err(v, rv) <= TOL and rel_err(d, rd) <= TOL, (tname, oracle.EXPORTS[which], cfg_name(cfg), kind)
