@@ -44,6 +44,7 @@ extern "C" {
 #define NSFV1_TRIANGLE       2
 #define NSFV1_QUADRILATERAL  3
 #define NSFV1_TETRAHEDRON    4
+#define NSFV1_PRISM          6
 #define NSFV1_HEXAHEDRON     8
 
 /* Jacobian value precision */

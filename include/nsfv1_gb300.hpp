@@ -51,6 +51,7 @@ inline int num_corners(int roid) {
         case NSFV1_TRIANGLE: return 3;
         case NSFV1_QUADRILATERAL: return 4;
         case NSFV1_TETRAHEDRON: return 4;
+        case NSFV1_PRISM: return 6;
         case NSFV1_HEXAHEDRON: return 8;
     }
     return 0;

@@ -60,6 +60,7 @@ def load():
             "ora_add_inflow": (c_int, [c_void_p, c_int64, c_int, c_void_p, c_void_p]),
             "ora_vorticity": (c_int, [c_void_p, c_void_p, c_void_p]),
             "ora_add_outflow": (c_int, [c_void_p, c_int64, c_int, c_void_p]),
+            "ora_outflow_elem": (c_int, [c_void_p, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
             "ora_eval_points": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int, c_void_p]),
             "ora_export": (c_int, [c_void_p, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_double, c_int, c_int, c_void_p,
                                    c_void_p, c_void_p]),
@@ -76,8 +77,8 @@ def _p(a):
     return None if a is None else a.ctypes.data
 
 
-NSH = {2: 3, 3: 4, 4: 4, 8: 8}
-DIM = {2: 2, 3: 2, 4: 3, 8: 3}
+NSH = {2: 3, 3: 4, 4: 4, 6: 6, 8: 8}
+DIM = {2: 2, 3: 2, 4: 3, 6: 3, 8: 3}
 
 
 class Oracle:
@@ -134,6 +135,17 @@ class Oracle:
         """NavierStokesNoNormalStressOutflowFV1 on the given boundary sides [n][nco]."""
         sides = np.ascontiguousarray(sides, np.int32)
         self._c(self.lib.ora_add_outflow(self.h, sides.shape[0], sides.shape[1], sides.ctypes.data))
+
+    def outflow_elem(self, roid, corners, u, side_mask):
+        """The outflow disc's local defect and Jacobian of n elements whose sides side_mask[e]
+        (bit s = reference side s) lie on the outflow boundary."""
+        corners = np.ascontiguousarray(corners, np.float64)
+        u = np.ascontiguousarray(u, np.float64)
+        m = np.ascontiguousarray(side_mask, np.uint32)
+        ne, nl = corners.shape[0], (DIM[roid] + 1) * NSH[roid]
+        d, J = np.zeros((ne, nl)), np.zeros((ne, nl * nl))
+        self._c(self.lib.ora_outflow_elem(self.h, roid, ne, corners.ctypes.data, u.ctypes.data, m.ctypes.data, d.ctypes.data, J.ctypes.data))
+        return d, J
 
     def vorticity(self, U):
         """vorticityFV1 of the nodal state U[n_nodes * b] on the mesh: one value per node."""
@@ -229,7 +241,7 @@ class Oracle:
 def geometry(roid, corners):
     """FV1 geometry dump of one element: list of SCVF dicts + SCV volumes."""
     lib = load()
-    nscvf = {2: 3, 3: 4, 4: 6, 8: 12}[roid]
+    nscvf = {2: 3, 3: 4, 4: 6, 6: 9, 8: 12}[roid]
     nsh = NSH[roid]
     out = np.zeros(nscvf * 40 + nsh)
     c = np.ascontiguousarray(corners, np.float64)
@@ -296,6 +308,8 @@ def load_ref():
                                        c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
         lib.ref_geometry.restype = c_int
         lib.ref_geometry.argtypes = [c_int, c_void_p, c_void_p]
+        lib.ref_outflow_batch.restype = c_int
+        lib.ref_outflow_batch.argtypes = [c_int, c_int64, ctypes.POINTER(RefConfig), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
         lib.ref_export.restype = c_int
         lib.ref_export.argtypes = [c_int, c_int, c_int64, ctypes.POINTER(RefConfig), c_void_p, c_void_p, c_void_p, c_double, c_int, c_int,
                                    c_void_p, c_void_p, c_void_p]
@@ -339,7 +353,7 @@ def ref_elem_batch(roid, cfg: dict, corners, u, u_old=None, dt=0.0, want=("defA"
 
 # data exports of the disc (navier_stokes_fv1.cpp:894-1491), in the index order of ora_export / ref_export
 EXPORTS = ("velocity", "velocity_grad", "velocity_ip", "pressure", "pressure_grad")
-NSCVF = {2: 3, 3: 4, 4: 6, 8: 12}
+NSCVF = {2: 3, 3: 4, 4: 6, 6: 9, 8: 12}
 
 
 def export_size(which, roid):
@@ -349,6 +363,22 @@ def export_size(which, roid):
 
 def export_nip(roid, ip_kind, local_ips=None):
     return NSCVF[roid] if ip_kind == 0 else NSH[roid] if ip_kind == 1 else int(np.asarray(local_ips).shape[0])
+
+
+def ref_outflow(roid, cfg: dict, corners, u, side_mask):
+    """The reference's NavierStokesNoNormalStressOutflowFV1 on n elements (layouts as
+    Oracle.outflow_elem); side_mask[e] bit s marks reference side s as outflow boundary."""
+    lib = load_ref()
+    corners = np.ascontiguousarray(corners, np.float64)
+    u = np.ascontiguousarray(u, np.float64)
+    m = np.ascontiguousarray(side_mask, np.uint32)
+    ne, nl = corners.shape[0], (DIM[roid] + 1) * NSH[roid]
+    d, J = np.zeros((ne, nl)), np.zeros((ne, nl * nl))
+    c = _ref_cfg(cfg)
+    st = lib.ref_outflow_batch(roid, ne, ctypes.byref(c), corners.ctypes.data, u.ctypes.data, m.ctypes.data, d.ctypes.data, J.ctypes.data)
+    if st != 0:
+        raise RuntimeError(f"reference error {st}: {lib.ref_last_error().decode()}")
+    return d, J
 
 
 def ref_export(which, roid, cfg: dict, corners, u, u_old=None, dt=0.0, ip_kind=0, local_ips=None, derivs=True):
@@ -372,7 +402,7 @@ def ref_export(which, roid, cfg: dict, corners, u, u_old=None, dt=0.0, ip_kind=0
 def ref_geometry(roid, corners):
     """The ugcore stand-in's FV1 geometry of one element (same layout as geometry())."""
     lib = load_ref()
-    nscvf = {2: 3, 3: 4, 4: 6, 8: 12}[roid]
+    nscvf = {2: 3, 3: 4, 4: 6, 6: 9, 8: 12}[roid]
     nsh = NSH[roid]
     out = np.zeros(nscvf * 40 + nsh)
     c = np.ascontiguousarray(corners, np.float64)

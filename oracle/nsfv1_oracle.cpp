@@ -51,7 +51,7 @@ typedef double number;
 enum { MAXCO = 8, MAXEDGE = 12, MAXSIDE = 6, MAXSCVF = 12 };
 
 // ReferenceObjectID numbering of ugcore (elements of this path only).
-enum { ROID_TRIANGLE = 2, ROID_QUADRILATERAL = 3, ROID_TETRAHEDRON = 4, ROID_HEXAHEDRON = 8 };
+enum { ROID_TRIANGLE = 2, ROID_QUADRILATERAL = 3, ROID_TETRAHEDRON = 4, ROID_PRISM = 6, ROID_HEXAHEDRON = 8 };
 
 // upwind / stabilisation / diffusion-length ids
 enum { UPW_NONE = -1, UPW_NO = 0, UPW_FULL = 1, UPW_SKEWED = 2, UPW_LPS = 3, UPW_POS = 4 };
@@ -102,6 +102,15 @@ static RefElem make_ref(int roid) {
         int f[4][3] = {{0, 2, 1}, {0, 1, 3}, {1, 2, 3}, {0, 3, 2}};
         for (int i = 0; i < 6; ++i) { r.edge[i][0] = e[i][0]; r.edge[i][1] = e[i][1]; }
         for (int i = 0; i < 4; ++i) { r.side_nco[i] = 3; for (int j = 0; j < 3; ++j) r.side[i][j] = f[i][j]; }
+    } else if (roid == ROID_PRISM) {
+        // the triangle (0, 1, 2) at z = 0 extruded to (3, 4, 5); sides 0 and 4 triangles
+        r.dim = 3; r.nco = 6; r.nedge = 9; r.nside = 5;
+        set_co(r, 0, 0, 0, 0); set_co(r, 1, 1, 0, 0); set_co(r, 2, 0, 1, 0);
+        set_co(r, 3, 0, 0, 1); set_co(r, 4, 1, 0, 1); set_co(r, 5, 0, 1, 1);
+        int e[9][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 4}, {2, 5}, {3, 4}, {4, 5}, {5, 3}};
+        int f[5][4] = {{0, 2, 1, -1}, {0, 1, 4, 3}, {1, 2, 5, 4}, {2, 0, 3, 5}, {3, 4, 5, -1}};
+        for (int i = 0; i < 9; ++i) { r.edge[i][0] = e[i][0]; r.edge[i][1] = e[i][1]; }
+        for (int i = 0; i < 5; ++i) { r.side_nco[i] = (i == 0 || i == 4) ? 3 : 4; for (int j = 0; j < r.side_nco[i]; ++j) r.side[i][j] = f[i][j]; }
     } else if (roid == ROID_HEXAHEDRON) {
         r.dim = 3; r.nco = 8; r.nedge = 12; r.nside = 6;
         set_co(r, 0, 0, 0, 0); set_co(r, 1, 1, 0, 0); set_co(r, 2, 1, 1, 0); set_co(r, 3, 0, 1, 0);
@@ -149,11 +158,13 @@ static const RefElem& ref_elem(int roid) {
     static const RefElem tri = make_ref(ROID_TRIANGLE);
     static const RefElem quad = make_ref(ROID_QUADRILATERAL);
     static const RefElem tet = make_ref(ROID_TETRAHEDRON);
+    static const RefElem prism = make_ref(ROID_PRISM);
     static const RefElem hex = make_ref(ROID_HEXAHEDRON);
     switch (roid) {
         case ROID_TRIANGLE: return tri;
         case ROID_QUADRILATERAL: return quad;
         case ROID_TETRAHEDRON: return tet;
+        case ROID_PRISM: return prism;
         case ROID_HEXAHEDRON: return hex;
     }
     throw std::runtime_error("unsupported element type");
@@ -167,6 +178,11 @@ static void p1_shapes(int roid, const number* x, number* N) {
             N[0] = (1.0 - x[0]) * (1.0 - x[1]); N[1] = x[0] * (1.0 - x[1]);
             N[2] = x[0] * x[1]; N[3] = (1.0 - x[0]) * x[1]; return;
         case ROID_TETRAHEDRON: N[0] = 1.0 - x[0] - x[1] - x[2]; N[1] = x[0]; N[2] = x[1]; N[3] = x[2]; return;
+        case ROID_PRISM: {
+            const number t[3] = {1.0 - x[0] - x[1], x[0], x[1]};
+            for (int k = 0; k < 6; ++k) N[k] = t[k % 3] * (k >= 3 ? x[2] : 1.0 - x[2]);
+            return;
+        }
         case ROID_HEXAHEDRON: {
             const number a = x[0], b = x[1], c = x[2];
             N[0] = (1.0 - a) * (1.0 - b) * (1.0 - c); N[1] = a * (1.0 - b) * (1.0 - c);
@@ -191,6 +207,15 @@ static void p1_grads(int roid, const number* x, number G[][3]) {
             G[1][0] = 1; G[1][1] = 0; G[1][2] = 0;
             G[2][0] = 0; G[2][1] = 1; G[2][2] = 0;
             G[3][0] = 0; G[3][1] = 0; G[3][2] = 1; return;
+        case ROID_PRISM: {
+            const number t[3] = {1.0 - x[0] - x[1], x[0], x[1]};
+            const number dt[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
+            for (int k = 0; k < 6; ++k) {
+                const number z = k >= 3 ? x[2] : 1.0 - x[2], dz = k >= 3 ? 1.0 : -1.0;
+                G[k][0] = dt[k % 3][0] * z; G[k][1] = dt[k % 3][1] * z; G[k][2] = t[k % 3] * dz;
+            }
+            return;
+        }
         case ROID_HEXAHEDRON: {
             const number a = x[0], b = x[1], c = x[2];
             G[0][0] = -(1.0 - b) * (1.0 - c); G[0][1] = -(1.0 - a) * (1.0 - c); G[0][2] = -(1.0 - a) * (1.0 - b);
@@ -1457,6 +1482,112 @@ static void elem_local(Disc& disc, FV1Geometry& geo, const number* corners, int 
     }
 }
 
+/* NavierStokesNoNormalStressOutflowFV1 (no_normal_stress_outflow_fv1.cpp:343-504) on one
+ * boundary face, into the element-local defect / Jacobian (row bf.local), scaled by sc:
+ * momentum: the viscous flux -nu rho ((grad u + grad u^T) n) minus its part along the
+ * area-weighted n (v + (-(v.n)) n, as the reference writes it), the outgoing convective
+ * flux max(rho u.n, 0) u; continuity rho u.n; the Jacobian of the viscous and continuity
+ * terms and of the convective one with the flux frozen. */
+static void outflow_face_terms(const Disc& disc, int roid, const number* corners, const number* uloc, const OutflowBF& bf, number sc,
+                               number* dloc, number* Jloc) {
+    const RefElem& R = ref_elem(roid);
+    const int dim = R.dim, nsh = R.nco, b = dim + 1, Pc = dim, node = bf.local;
+    number N[MAXCO], LG[MAXCO][3], J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, JtInv[3][3], G[MAXCO][3];
+    p1_shapes(roid, bf.xi, N);
+    p1_grads(roid, bf.xi, LG);
+    for (int k = 0; k < nsh; ++k)
+        for (int r = 0; r < dim; ++r)
+            for (int c = 0; c < dim; ++c) J[r][c] += corners[k * dim + r] * LG[k][c];
+    det_and_jtinv(dim, J, JtInv);
+    for (int k = 0; k < nsh; ++k)
+        for (int r = 0; r < 3; ++r) {
+            G[k][r] = 0;
+            if (r < dim) for (int c = 0; c < dim; ++c) G[k][r] += JtInv[r][c] * LG[k][c];
+        }
+    const number* nn = bf.n;
+    const number nu = disc.kinVisco, rho = disc.density;
+    number stdVel[3] = {0, 0, 0};
+    for (int d1 = 0; d1 < dim; ++d1)
+        for (int sh = 0; sh < nsh; ++sh) stdVel[d1] += uloc[d1 * nsh + sh] * N[sh];
+    number vn = 0;
+    for (int d = 0; d < dim; ++d) vn += stdVel[d] * nn[d];
+    auto Jx = [&](int f1, int s1, int f2, int s2) -> number& { return Jloc[((f1 * nsh + s1) * b + f2) * nsh + s2]; };
+    if (dloc) {
+        number gradVel[3][3], df[3] = {0, 0, 0};
+        for (int d1 = 0; d1 < dim; ++d1)
+            for (int d2 = 0; d2 < dim; ++d2) {
+                gradVel[d1][d2] = 0.0;
+                for (int sh = 0; sh < nsh; ++sh) gradVel[d1][d2] += G[sh][d2] * uloc[d1 * nsh + sh];
+            }
+        for (int d1 = 0; d1 < dim; ++d1) for (int d2 = 0; d2 < dim; ++d2) df[d1] += gradVel[d1][d2] * nn[d2];
+        if (!disc.bLaplace)
+            for (int d1 = 0; d1 < dim; ++d1) for (int d2 = 0; d2 < dim; ++d2) df[d1] += gradVel[d2][d1] * nn[d2];
+        number dot = 0;
+        for (int d = 0; d < dim; ++d) dot += df[d] * nn[d];
+        for (int d = 0; d < dim; ++d) df[d] += -dot * nn[d];
+        for (int d = 0; d < dim; ++d) df[d] *= -nu * rho;
+        for (int d1 = 0; d1 < dim; ++d1) dloc[d1 * nsh + node] += sc * df[d1];
+        if (!disc.bStokes) {
+            number flux = vn * rho;
+            if (flux < 0) flux = 0;
+            for (int d1 = 0; d1 < dim; ++d1) dloc[d1 * nsh + node] += sc * (flux * stdVel[d1]);
+        }
+        dloc[Pc * nsh + node] += sc * (vn * rho);
+    }
+    if (Jloc) {
+        for (int sh = 0; sh < nsh; ++sh) {
+            number M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, ns[3] = {0, 0, 0}, gn = 0;
+            for (int d = 0; d < dim; ++d) gn += G[sh][d] * nn[d];
+            for (int d = 0; d < dim; ++d) M[d][d] = gn;
+            if (!disc.bLaplace)
+                for (int d1 = 0; d1 < dim; ++d1) for (int d2 = 0; d2 < dim; ++d2) M[d1][d2] += G[sh][d1] * nn[d2];
+            for (int d2 = 0; d2 < dim; ++d2) for (int d1 = 0; d1 < dim; ++d1) ns[d2] += M[d1][d2] * nn[d1];
+            for (int d1 = 0; d1 < dim; ++d1)
+                for (int d2 = 0; d2 < dim; ++d2) Jx(d1, node, d2, sh) += sc * ((M[d1][d2] - nn[d1] * ns[d2]) * (-nu * rho));
+        }
+        if (!disc.bStokes) {
+            number old = vn * rho;
+            if (old < 0) old = 0;
+            for (int sh = 0; sh < nsh; ++sh)
+                for (int d1 = 0; d1 < dim; ++d1) Jx(d1, node, d1, sh) += sc * (old * N[sh]);
+        }
+        for (int sh = 0; sh < nsh; ++sh)
+            for (int d2 = 0; d2 < dim; ++d2) Jx(Pc, node, d2, sh) += sc * (N[sh] * nn[d2] * rho);
+    }
+}
+
+/* The boundary faces of one element side given by its element-local corners loc[nco]
+ * (cyclic order): per corner the face {corner, side-edge midpoints, side centre} (2D:
+ * {corner, side midpoint}), its integration point at the mean of those points in local
+ * coordinates and its outward area-weighted normal. */
+static void side_outflow_faces(int roid, const number* corners, const int* loc, int nco, int64_t elem, std::vector<OutflowBF>& out) {
+    const RefElem& R = ref_elem(roid);
+    const int dim = R.dim, nsh = R.nco;
+    number x[4][3] = {{0}}, cen[3] = {0, 0, 0}, lx[4][3] = {{0}}, lsc[3] = {0, 0, 0};
+    for (int j = 0; j < nco; ++j)
+        for (int d = 0; d < dim; ++d) {
+            x[j][d] = corners[loc[j] * dim + d];
+            lx[j][d] = R.co[loc[j]][d];
+            lsc[d] += lx[j][d] / nco;
+        }
+    for (int i = 0; i < nsh; ++i) for (int d = 0; d < dim; ++d) cen[d] += corners[i * dim + d] / nsh;
+    for (int j = 0; j < nco; ++j) {
+        OutflowBF bf;
+        bf.elem = elem;
+        bf.local = loc[j];
+        boundary_face_normal(dim, nco, x, j, cen, bf.n);
+        for (int d = 0; d < 3; ++d) bf.xi[d] = 0.0;
+        if (dim == 2) {
+            const int o = 1 - j;
+            for (int d = 0; d < 2; ++d) bf.xi[d] = 0.5 * (lx[j][d] + 0.5 * (lx[j][d] + lx[o][d]));
+        } else {
+            const int nx = (j + 1) % nco, pv = (j + nco - 1) % nco;
+            for (int d = 0; d < 3; ++d) bf.xi[d] = 0.25 * (lx[j][d] + 0.5 * (lx[j][d] + lx[nx][d]) + lsc[d] + 0.5 * (lx[pv][d] + lx[j][d]));
+        }
+        out.push_back(bf);
+    }
+}
+
 static void assemble(Problem& P, const number* U, const number* Uold, number dt, number* D, number* JV, int nthreads) {
     Mesh& m = P.mesh;
     P.disc.check();
@@ -1503,79 +1634,24 @@ static void assemble(Problem& P, const number* U, const number* Uold, number dt,
     }
     // outflow boundaries without normal stress (no_normal_stress_outflow_fv1.cpp:343-504),
     // dt-scaled when transient like the other stiffness terms
-    const number sc = transient ? dt : 1.0;
-    for (const OutflowBF& bf : P.outflow) {
-        const int dim = m.dim, Pc = dim;
-        number corners[MAXCO * 3], uloc[4 * MAXCO];
-        gather_elem(m, bf.elem, U, corners, uloc, b);
-        number N[MAXCO], LG[MAXCO][3], J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, JtInv[3][3], G[MAXCO][3];
-        p1_shapes(m.roid, bf.xi, N);
-        p1_grads(m.roid, bf.xi, LG);
-        for (int k = 0; k < nsh; ++k)
-            for (int r = 0; r < dim; ++r)
-                for (int c = 0; c < dim; ++c) J[r][c] += corners[k * dim + r] * LG[k][c];
-        det_and_jtinv(dim, J, JtInv);
-        for (int k = 0; k < nsh; ++k)
-            for (int r = 0; r < 3; ++r) {
-                G[k][r] = 0;
-                if (r < dim) for (int c = 0; c < dim; ++c) G[k][r] += JtInv[r][c] * LG[k][c];
-            }
-        const number* nn = bf.n;
-        const number nu = P.disc.kinVisco, rho = P.disc.density;
-        const int64_t node = m.conn[bf.elem * nsh + bf.local];
-        number stdVel[3] = {0, 0, 0};
-        for (int d1 = 0; d1 < dim; ++d1)
-            for (int sh = 0; sh < nsh; ++sh) stdVel[d1] += uloc[d1 * nsh + sh] * N[sh];
-        number vn = 0;
-        for (int d = 0; d < dim; ++d) vn += stdVel[d] * nn[d];
-        if (D) {
-            // momentum: the tangential part of the viscous flux, the outgoing convective flux
-            number gradVel[3][3], df[3] = {0, 0, 0};
-            for (int d1 = 0; d1 < dim; ++d1)
-                for (int d2 = 0; d2 < dim; ++d2) {
-                    gradVel[d1][d2] = 0.0;
-                    for (int sh = 0; sh < nsh; ++sh) gradVel[d1][d2] += G[sh][d2] * uloc[d1 * nsh + sh];
+    if (!P.outflow.empty()) {
+        const number sc = transient ? dt : 1.0;
+        std::vector<number> dl(n), Jl(n * n);
+        for (const OutflowBF& bf : P.outflow) {
+            number corners[MAXCO * 3], uloc[4 * MAXCO];
+            gather_elem(m, bf.elem, U, corners, uloc, b);
+            std::fill(dl.begin(), dl.end(), 0.0);
+            std::fill(Jl.begin(), Jl.end(), 0.0);
+            outflow_face_terms(P.disc, m.roid, corners, uloc, bf, sc, D ? dl.data() : nullptr, JV ? Jl.data() : nullptr);
+            const int i = bf.local;
+            const int64_t row = m.conn[bf.elem * nsh + i];
+            if (D) for (int f = 0; f < b; ++f) D[row * b + f] += dl[f * nsh + i];
+            if (JV)
+                for (int j = 0; j < nsh; ++j) {
+                    number* blk = JV + m.elemBlk[(bf.elem * nsh + i) * nsh + j] * b * b;
+                    for (int f1 = 0; f1 < b; ++f1)
+                        for (int f2 = 0; f2 < b; ++f2) blk[f1 * b + f2] += Jl[((f1 * nsh + i) * b + f2) * nsh + j];
                 }
-            for (int d1 = 0; d1 < dim; ++d1) for (int d2 = 0; d2 < dim; ++d2) df[d1] += gradVel[d1][d2] * nn[d2];
-            if (!P.disc.bLaplace)
-                for (int d1 = 0; d1 < dim; ++d1) for (int d2 = 0; d2 < dim; ++d2) df[d1] += gradVel[d2][d1] * nn[d2];
-            number dot = 0;
-            for (int d = 0; d < dim; ++d) dot += df[d] * nn[d];
-            for (int d = 0; d < dim; ++d) df[d] += -dot * nn[d];
-            for (int d = 0; d < dim; ++d) df[d] *= -nu * rho;
-            for (int d1 = 0; d1 < dim; ++d1) D[node * b + d1] += sc * df[d1];
-            if (!P.disc.bStokes) {
-                number flux = vn * rho;
-                if (flux < 0) flux = 0;
-                for (int d1 = 0; d1 < dim; ++d1) D[node * b + d1] += sc * (flux * stdVel[d1]);
-            }
-            D[node * b + Pc] += sc * (vn * rho);
-        }
-        if (JV) {
-            auto blk = [&](int sh) { return JV + m.elemBlk[(bf.elem * nsh + bf.local) * nsh + sh] * b * b; };
-            for (int sh = 0; sh < nsh; ++sh) {
-                number M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, ns[3] = {0, 0, 0}, gn = 0;
-                for (int d = 0; d < dim; ++d) gn += G[sh][d] * nn[d];
-                for (int d = 0; d < dim; ++d) M[d][d] = gn;
-                if (!P.disc.bLaplace)
-                    for (int d1 = 0; d1 < dim; ++d1) for (int d2 = 0; d2 < dim; ++d2) M[d1][d2] += G[sh][d1] * nn[d2];
-                for (int d2 = 0; d2 < dim; ++d2) for (int d1 = 0; d1 < dim; ++d1) ns[d2] += M[d1][d2] * nn[d1];
-                number* B = blk(sh);
-                for (int d1 = 0; d1 < dim; ++d1)
-                    for (int d2 = 0; d2 < dim; ++d2) B[d1 * b + d2] += sc * ((M[d1][d2] - nn[d1] * ns[d2]) * (-nu * rho));
-            }
-            if (!P.disc.bStokes) {
-                number old = vn * rho;
-                if (old < 0) old = 0;
-                for (int sh = 0; sh < nsh; ++sh) {
-                    number* B = blk(sh);
-                    for (int d1 = 0; d1 < dim; ++d1) B[d1 * b + d1] += sc * (old * N[sh]);
-                }
-            }
-            for (int sh = 0; sh < nsh; ++sh) {
-                number* B = blk(sh);
-                for (int d2 = 0; d2 < dim; ++d2) B[Pc * b + d2] += sc * (N[sh] * nn[d2] * rho);
-            }
         }
     }
     // inflow boundaries: the continuity rows' Neumann flux (a right-hand side: dt-scaled when transient)
@@ -2057,6 +2133,7 @@ static bool point_in_elem(int roid, int dim, int nsh, const number* c, const num
     const number tol = 1e-10;
     if (roid == ROID_TRIANGLE) return xi[0] >= -tol && xi[1] >= -tol && 1.0 - xi[0] - xi[1] >= -tol;
     if (roid == ROID_TETRAHEDRON) return xi[0] >= -tol && xi[1] >= -tol && xi[2] >= -tol && 1.0 - xi[0] - xi[1] - xi[2] >= -tol;
+    if (roid == ROID_PRISM) return xi[0] >= -tol && xi[1] >= -tol && 1.0 - xi[0] - xi[1] >= -tol && xi[2] >= -tol && xi[2] <= 1.0 + tol;
     for (int d = 0; d < dim; ++d) if (!(xi[d] >= -tol && xi[d] <= 1.0 + tol)) return false;
     return true;
 }
@@ -2266,7 +2343,6 @@ int ora_add_outflow(void* h, int64_t nSides, int nco, const int32_t* sides) {
     auto* P = static_cast<Problem*>(h);
     Mesh& m = P->mesh;
     const int dim = m.dim, nsh = m.nsh;
-    const RefElem& R = ref_elem(m.roid);
     for (int64_t s = 0; s < nSides; ++s) {
         const int32_t* sn = sides + s * nco;
         int64_t owner = -1;
@@ -2278,33 +2354,37 @@ int ora_add_outflow(void* h, int64_t nSides, int nco, const int32_t* sides) {
             if (found == nco) { owner = e; ++owners; }
         }
         if (owners != 1) { P->lastError = "outflow side is not a boundary side of exactly one element"; return 1; }
-        number x[4][3] = {{0}}, cen[3] = {0, 0, 0}, lx[4][3] = {{0}}, lsc[3] = {0, 0, 0};
-        int loc[4];
-        for (int j = 0; j < nco; ++j) {
-            for (int d = 0; d < dim; ++d) x[j][d] = m.coords[(int64_t)sn[j] * dim + d];
-            loc[j] = -1;
-            for (int i = 0; i < nsh; ++i) if (m.conn[owner * nsh + i] == sn[j]) loc[j] = i;
-            for (int d = 0; d < dim; ++d) { lx[j][d] = R.co[loc[j]][d]; lsc[d] += lx[j][d] / nco; }
+        number corners[MAXCO * 3];
+        int loc[4] = {0, 0, 0, 0};
+        for (int i = 0; i < nsh; ++i) {
+            for (int d = 0; d < dim; ++d) corners[i * dim + d] = m.coords[(int64_t)m.conn[owner * nsh + i] * dim + d];
+            for (int j = 0; j < nco; ++j) if (m.conn[owner * nsh + i] == sn[j]) loc[j] = i;
         }
-        for (int i = 0; i < nsh; ++i) for (int d = 0; d < dim; ++d) cen[d] += m.coords[(int64_t)m.conn[owner * nsh + i] * dim + d] / nsh;
-        for (int j = 0; j < nco; ++j) {
-            OutflowBF bf;
-            bf.elem = owner;
-            bf.local = loc[j];
-            boundary_face_normal(dim, nco, x, j, cen, bf.n);
-            for (int d = 0; d < 3; ++d) bf.xi[d] = 0.0;
-            if (dim == 2) {
-                const int o = 1 - j;
-                for (int d = 0; d < 2; ++d) bf.xi[d] = 0.5 * (lx[j][d] + 0.5 * (lx[j][d] + lx[o][d]));
-            } else {
-                const int nx = (j + 1) % nco, pv = (j + nco - 1) % nco;
-                for (int d = 0; d < 3; ++d)
-                    bf.xi[d] = 0.25 * (lx[j][d] + 0.5 * (lx[j][d] + lx[nx][d]) + lsc[d] + 0.5 * (lx[pv][d] + lx[j][d]));
-            }
-            P->outflow.push_back(bf);
-        }
+        side_outflow_faces(m.roid, corners, loc, nco, owner, P->outflow);
     }
     return 0;
+}
+
+/* The outflow disc on n independent elements (element-local layouts, outputs zeroed):
+ * sideMask[e] bit s marks side s of the reference element as outflow boundary. */
+int ora_outflow_elem(void* h, int roid, int64_t n, const double* corners, const double* u, const unsigned* sideMask, double* defA,
+                     double* jacA) {
+    auto* P = static_cast<Problem*>(h);
+    try {
+        const RefElem& R = ref_elem(roid);
+        const int dim = R.dim, nsh = R.nco, nl = (dim + 1) * nsh;
+        for (int64_t e = 0; e < n; ++e) {
+            const double* c = corners + e * nsh * dim;
+            if (defA) std::fill(defA + e * nl, defA + (e + 1) * nl, 0.0);
+            if (jacA) std::fill(jacA + e * nl * nl, jacA + (e + 1) * nl * nl, 0.0);
+            std::vector<OutflowBF> bfs;
+            for (int s = 0; s < R.nside; ++s)
+                if (sideMask[e] >> s & 1u) side_outflow_faces(roid, c, R.side[s], R.side_nco[s], e, bfs);
+            for (const OutflowBF& bf : bfs)
+                outflow_face_terms(P->disc, roid, c, u + e * nl, bf, 1.0, defA ? defA + e * nl : nullptr, jacA ? jacA + e * nl * nl : nullptr);
+        }
+        return 0;
+    } catch (std::exception& ex) { P->lastError = ex.what(); return 3; }
 }
 
 int ora_bsr_mv(void* h, const double* V, const double* x, double* y) {

@@ -28,6 +28,8 @@
 #include "upwind.cpp"
 #include "incompressible/fv1/stabilization.cpp"
 #include "incompressible/fv1/navier_stokes_fv1.cpp"
+#include "incompressible/bnd/no_normal_stress_outflow_base.cpp"
+#include "incompressible/fv1/bnd/no_normal_stress_outflow_fv1.cpp"
 
 #include <cstdint>
 #include <cstdio>
@@ -39,6 +41,8 @@ namespace NavierStokes {
 // UG_DIM_x); this driver calls the callbacks directly, so nothing is registered.
 template <> void NavierStokesFV1<Domain2d>::register_all_funcs(bool) {}
 template <> void NavierStokesFV1<Domain3d>::register_all_funcs(bool) {}
+template <> void NavierStokesNoNormalStressOutflowFV1<Domain2d>::register_all_funcs(bool) {}
+template <> void NavierStokesNoNormalStressOutflowFV1<Domain3d>::register_all_funcs(bool) {}
 }  // namespace NavierStokes
 }  // namespace ug
 
@@ -261,6 +265,46 @@ void run_export(const ref_config& c, int which, int64_t n, const double* corners
     disc.template fsh_elem_loop<TElem, TGeom>();
 }
 
+// The reference's NavierStokesNoNormalStressOutflowFV1 (no_normal_stress_outflow_fv1.cpp:
+// 343-504) on n elements: sideMask[e] marks the element's sides on the outflow boundary
+// (bit s = side s; the stand-in's boundary faces); the disc's add_def_A_elem /
+// add_jac_A_elem in the element-local layouts.
+template <int dim, class TElem>
+void run_outflow(const ref_config& c, int64_t n, const double* corners, const double* u, const unsigned* sideMask, double* defA,
+                 double* jacA) {
+    typedef typename DomainOf<dim>::type TDomain;
+    typedef FV1Geometry<TElem, dim> TGeom;
+    static const int nsh = (int)TGeom::nsh, b = dim + 1, nloc = b * nsh;
+    const ReferenceObjectID roid = TGeom::ROID;
+    SmartPtr<NavierStokesFV1<TDomain> > master(new NavierStokesFV1<TDomain>(dim == 2 ? "u,v,p" : "u,v,w,p", "Inner"));
+    configure<dim>(*master, c);
+    NavierStokesNoNormalStressOutflowFV1<TDomain> outflow(master);
+    outflow.add("Outflow");
+    outflow.template prep_elem_loop<TElem, TGeom>(roid, 0);
+    LocalVector U(b, nsh), d(b, nsh);
+    LocalMatrix J(b, nsh);
+    MathVector<dim> co[nsh];
+    for (int64_t e = 0; e < n; ++e) {
+        for (int k = 0; k < nsh; ++k)
+            for (int x = 0; x < dim; ++x) co[k][x] = corners[(e * nsh + k) * dim + x];
+        for (int q = 0; q < nloc; ++q) U.data()[q] = u[e * nloc + q];
+        shim_boundary_sides() = sideMask[e];
+        outflow.template prep_elem<TElem, TGeom>(U, nullptr, roid, co);
+        if (defA) {
+            d.zero();
+            outflow.template add_def_A_elem<TElem, TGeom>(d, U, nullptr, co);
+            std::copy(d.data(), d.data() + nloc, defA + e * nloc);
+        }
+        if (jacA) {
+            J.zero();
+            outflow.template add_jac_A_elem<TElem, TGeom>(J, U, nullptr, co);
+            std::copy(J.data(), J.data() + nloc * nloc, jacA + e * nloc * nloc);
+        }
+    }
+    shim_boundary_sides() = 0;
+    outflow.template fsh_elem_loop<TElem, TGeom>();
+}
+
 thread_local std::string g_err;
 
 }  // namespace
@@ -277,6 +321,7 @@ int ref_elem_batch(int roid, int64_t n, const ref_config* c, const double* corne
             case ROID_TRIANGLE: run_batch<2, Triangle>(*c, n, corners, u, u_old, dt, defA, jacA, defM, jacM, rhs); return 0;
             case ROID_QUADRILATERAL: run_batch<2, Quadrilateral>(*c, n, corners, u, u_old, dt, defA, jacA, defM, jacM, rhs); return 0;
             case ROID_TETRAHEDRON: run_batch<3, Tetrahedron>(*c, n, corners, u, u_old, dt, defA, jacA, defM, jacM, rhs); return 0;
+            case ROID_PRISM: run_batch<3, Prism>(*c, n, corners, u, u_old, dt, defA, jacA, defM, jacM, rhs); return 0;
             case ROID_HEXAHEDRON: run_batch<3, Hexahedron>(*c, n, corners, u, u_old, dt, defA, jacA, defM, jacM, rhs); return 0;
         }
         return 2;
@@ -293,7 +338,25 @@ int ref_export(int which, int roid, int64_t n, const ref_config* c, const double
             case ROID_TRIANGLE: run_export<2, Triangle>(*c, which, n, corners, u, u_old, dt, ipKind, nip, lips, values, derivs); return 0;
             case ROID_QUADRILATERAL: run_export<2, Quadrilateral>(*c, which, n, corners, u, u_old, dt, ipKind, nip, lips, values, derivs); return 0;
             case ROID_TETRAHEDRON: run_export<3, Tetrahedron>(*c, which, n, corners, u, u_old, dt, ipKind, nip, lips, values, derivs); return 0;
+            case ROID_PRISM: run_export<3, Prism>(*c, which, n, corners, u, u_old, dt, ipKind, nip, lips, values, derivs); return 0;
             case ROID_HEXAHEDRON: run_export<3, Hexahedron>(*c, which, n, corners, u, u_old, dt, ipKind, nip, lips, values, derivs); return 0;
+        }
+        return 2;
+    } catch (std::exception& e) {
+        g_err = e.what();
+        return 1;
+    }
+}
+
+int ref_outflow_batch(int roid, int64_t n, const ref_config* c, const double* corners, const double* u, const unsigned* sideMask, double* defA,
+                      double* jacA) {
+    try {
+        switch (roid) {
+            case ROID_TRIANGLE: run_outflow<2, Triangle>(*c, n, corners, u, sideMask, defA, jacA); return 0;
+            case ROID_QUADRILATERAL: run_outflow<2, Quadrilateral>(*c, n, corners, u, sideMask, defA, jacA); return 0;
+            case ROID_TETRAHEDRON: run_outflow<3, Tetrahedron>(*c, n, corners, u, sideMask, defA, jacA); return 0;
+            case ROID_PRISM: run_outflow<3, Prism>(*c, n, corners, u, sideMask, defA, jacA); return 0;
+            case ROID_HEXAHEDRON: run_outflow<3, Hexahedron>(*c, n, corners, u, sideMask, defA, jacA); return 0;
         }
         return 2;
     } catch (std::exception& e) {
@@ -308,6 +371,7 @@ int ref_geometry(int roid, const double* corners, double* out) {
             case ROID_TRIANGLE: geometry<2, Triangle>(corners, out); return 0;
             case ROID_QUADRILATERAL: geometry<2, Quadrilateral>(corners, out); return 0;
             case ROID_TETRAHEDRON: geometry<3, Tetrahedron>(corners, out); return 0;
+            case ROID_PRISM: geometry<3, Prism>(corners, out); return 0;
             case ROID_HEXAHEDRON: geometry<3, Hexahedron>(corners, out); return 0;
         }
         return 2;

@@ -129,7 +129,7 @@ class FV1Geometry : public FVGeometryBase {
 
     void update(GridObject* /*elem*/, const MathVector<worldDim>* vCornerCoords, const ISubsetHandler* /*ish*/ = nullptr) {
         if (!(dim == worldDim && (ROID == ROID_TRIANGLE || ROID == ROID_QUADRILATERAL || ROID == ROID_TETRAHEDRON ||
-                                  ROID == ROID_HEXAHEDRON)))
+                                  ROID == ROID_PRISM || ROID == ROID_HEXAHEDRON)))
             UG_THROW("FV1Geometry: element type " << (int)ROID << " in dimension " << worldDim << " not available in this shim");
         const RefTables& R = ref_tables<ROID>();
         for (size_t c = 0; c < nsh; ++c) m_corners[c] = vCornerCoords[c];
@@ -258,7 +258,129 @@ class FV1Geometry : public FVGeometryBase {
             m_scvGips[a] = m_corners[a];
             m_scvLips[a] = v.m_lip;
         }
+        update_boundary_faces(R, lC, gC);
     }
+
+    // Boundary faces (ugcore FV1Geometry::BF, restated): for every element side on a
+    // registered boundary subset and every corner of that side, the corner's part of
+    // the side -- 2D {corner, side midpoint}, 3D {corner, midpoint of the side edge to
+    // the next corner, side centre, midpoint of the side edge from the previous
+    // corner} -- with its integration point at the mean of those points, its normal
+    // (the half side turned outward; in 3D half the cross product of the diagonals)
+    // pointing out of the element, and the shapes / gradients at that point.
+    class BF {
+      public:
+        size_t node_id() const { return m_node; }
+        const MathVector<worldDim>& normal() const { return m_normal; }
+        size_t num_ip() const { return 1; }
+        const MathVector<dim>& local_ip() const { return m_lip; }
+        const MathVector<worldDim>& global_ip() const { return m_gip; }
+        size_t num_sh() const { return nsh; }
+        number shape(size_t sh) const { return m_shape[sh]; }
+        const MathVector<dim>& local_grad(size_t sh) const { return m_lgrad[sh]; }
+        const MathVector<worldDim>& global_grad(size_t sh) const { return m_ggrad[sh]; }
+        number volume() const { return m_vol; }
+
+      private:
+        friend class FV1Geometry;
+        size_t m_node = 0;
+        number m_vol = 0;
+        MathVector<worldDim> m_normal, m_gip;
+        MathVector<dim> m_lip;
+        number m_shape[nsh];
+        MathVector<dim> m_lgrad[nsh];
+        MathVector<worldDim> m_ggrad[nsh];
+    };
+    void add_boundary_subset(int si) { if (si == 1) m_bnd1 = true; }
+    void remove_boundary_subset(int si) { if (si == 1) m_bnd1 = false; }
+    size_t num_bf(int si) const { return si == 1 ? m_bf1.size() : 0; }
+    const std::vector<BF>& bf(int si) const {
+        if (si != 1) UG_THROW("FV1Geometry: no boundary faces of subset " << si);
+        return m_bf1;
+    }
+
+  private:
+    void update_boundary_faces(const RefTables& R, const number* lC, const number* gC) {
+        m_bf1.clear();
+        if (!m_bnd1 || dim != worldDim) return;
+        const unsigned mask = shim_boundary_sides();
+        for (int s = 0; s < R.numSides; ++s) {
+            if (!(mask >> s & 1u)) continue;
+            const int nco = dim == 2 ? 2 : R.sideNco[s];
+            const int* sc = dim == 2 ? R.edge[s] : R.side[s];
+            number lS[3] = {0, 0, 0}, gS[3] = {0, 0, 0};
+            for (int j = 0; j < nco; ++j)
+                for (int d = 0; d < 3; ++d) {
+                    lS[d] += (d < dim ? R.co[sc[j]][d] : 0.0) / nco;
+                    gS[d] += (d < worldDim ? m_corners[sc[j]][d] : 0.0) / nco;
+                }
+            for (int j = 0; j < nco; ++j) {
+                BF f;
+                const int co = sc[j];
+                f.m_node = co;
+                number lq[4][3] = {{0}}, gq[4][3] = {{0}};
+                int nq;
+                for (int d = 0; d < 3; ++d) {
+                    lq[0][d] = d < dim ? R.co[co][d] : 0.0;
+                    gq[0][d] = d < worldDim ? m_corners[co][d] : 0.0;
+                }
+                if (dim == 2) {
+                    nq = 2;
+                    for (int d = 0; d < 3; ++d) { lq[1][d] = lS[d]; gq[1][d] = gS[d]; }
+                } else {
+                    nq = 4;
+                    const int nx = sc[(j + 1) % nco], pv = sc[(j + nco - 1) % nco];
+                    for (int d = 0; d < 3; ++d) {
+                        lq[1][d] = 0.5 * (R.co[co][d] + R.co[nx][d]);
+                        gq[1][d] = 0.5 * (m_corners[co][d] + m_corners[nx][d]);
+                        lq[2][d] = lS[d];
+                        gq[2][d] = gS[d];
+                        lq[3][d] = 0.5 * (R.co[pv][d] + R.co[co][d]);
+                        gq[3][d] = 0.5 * (m_corners[pv][d] + m_corners[co][d]);
+                    }
+                }
+                for (int d = 0; d < dim; ++d) { number l = 0; for (int q = 0; q < nq; ++q) l += lq[q][d]; f.m_lip[d] = l / nq; }
+                for (int d = 0; d < worldDim; ++d) { number g = 0; for (int q = 0; q < nq; ++q) g += gq[q][d]; f.m_gip[d] = g / nq; }
+                number n[3] = {0, 0, 0};
+                if (dim == 2) {
+                    n[0] = gq[1][1] - gq[0][1];
+                    n[1] = -(gq[1][0] - gq[0][0]);
+                } else {
+                    number d1[3], d2[3];
+                    for (int d = 0; d < 3; ++d) { d1[d] = gq[2][d] - gq[0][d]; d2[d] = gq[3][d] - gq[1][d]; }
+                    n[0] = 0.5 * (d1[1] * d2[2] - d1[2] * d2[1]);
+                    n[1] = 0.5 * (d1[2] * d2[0] - d1[0] * d2[2]);
+                    n[2] = 0.5 * (d1[0] * d2[1] - d1[1] * d2[0]);
+                }
+                number dot = 0, nn = 0;
+                for (int d = 0; d < worldDim; ++d) { dot += n[d] * (gS[d] - gC[d]); nn += n[d] * n[d]; }
+                if (dot < 0) for (int d = 0; d < 3; ++d) n[d] = -n[d];
+                for (int d = 0; d < worldDim; ++d) f.m_normal[d] = n[d];
+                f.m_vol = std::sqrt(nn);
+                // shapes and gradients at the local integration point
+                number xi[3] = {0, 0, 0};
+                for (int d = 0; d < dim; ++d) xi[d] = f.m_lip[d];
+                number J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, G[3][3];
+                for (size_t k = 0; k < nsh; ++k) {
+                    f.m_shape[k] = p1_shape(ROID, k, xi);
+                    for (int c = 0; c < dim; ++c) {
+                        f.m_lgrad[k][c] = p1_deriv(ROID, k, c, xi);
+                        for (int r = 0; r < worldDim; ++r) J[r][c] += m_corners[k][r] * f.m_lgrad[k][c];
+                    }
+                }
+                shim_detail::det_jtinv(dim, J, G);
+                for (size_t k = 0; k < nsh; ++k)
+                    for (int r = 0; r < worldDim; ++r) {
+                        number v = 0;
+                        for (int c = 0; c < dim; ++c) v += G[r][c] * f.m_lgrad[k][c];
+                        f.m_ggrad[k][r] = v;
+                    }
+                m_bf1.push_back(f);
+            }
+        }
+    }
+
+  public:
 
     size_t num_scvf() const { return numSCVF; }
     const SCVF& scvf(size_t i) const { return m_scvf[i]; }
@@ -307,6 +429,8 @@ class FV1Geometry : public FVGeometryBase {
         UG_THROW("FV1Geometry: no side through three corners");
     }
 
+    bool m_bnd1 = false;
+    std::vector<BF> m_bf1;
     MathVector<worldDim> m_corners[nsh];
     SCVF m_scvf[numSCVF];
     SCV m_scv[numSCV];

@@ -138,6 +138,7 @@ class MathVector {
   public:
     static const int Size = N;
     MathVector() { for (int i = 0; i < N; ++i) m_v[i] = T(0); }
+    explicit MathVector(const T& s) { for (int i = 0; i < N; ++i) m_v[i] = s; }
     MathVector& operator=(const T& s) { for (int i = 0; i < N; ++i) m_v[i] = s; return *this; }
     T& operator[](size_t i) { return m_v[i]; }
     const T& operator[](size_t i) const { return m_v[i]; }
@@ -157,6 +158,7 @@ class MathMatrix {
   public:
     MathMatrix() { for (int i = 0; i < N; ++i) for (int j = 0; j < M; ++j) m_a[i][j] = T(0); }
     MathMatrix& operator=(const T& s) { for (int i = 0; i < N; ++i) for (int j = 0; j < M; ++j) m_a[i][j] = s; return *this; }
+    MathMatrix& operator*=(const T& s) { for (int i = 0; i < N; ++i) for (int j = 0; j < M; ++j) m_a[i][j] *= s; return *this; }
     T& operator()(size_t i, size_t j) { return m_a[i][j]; }
     const T& operator()(size_t i, size_t j) const { return m_a[i][j]; }
     T* operator[](size_t i) { return m_a[i]; }
@@ -209,6 +211,11 @@ template <int N, int M> inline void MatVecMultAdd(MathVector<N>& o, number a, co
                                                   const MathVector<M>& v) {
     for (int i = 0; i < N; ++i) { number s = 0; for (int j = 0; j < M; ++j) s += A(i, j) * v[j]; o[i] = a * w[i] + b * s; }
 }
+template <int N, int M> inline void TransposedMatVecMult(MathVector<M>& o, const MathMatrix<N, M>& A, const MathVector<N>& v) {
+    for (int j = 0; j < M; ++j) { number s = 0; for (int i = 0; i < N; ++i) s += A(i, j) * v[i]; o[j] = s; }
+}
+// the diagonal entries set to s, the others kept
+template <int N> inline void MatDiagSet(MathMatrix<N, N>& A, number s) { for (int i = 0; i < N; ++i) A(i, i) = s; }
 template <int N, int M> inline void TransposedMatVecMultAdd(MathVector<M>& o, const MathMatrix<N, M>& A, const MathVector<N>& v) {
     for (int j = 0; j < M; ++j) { number s = 0; for (int i = 0; i < N; ++i) s += A(i, j) * v[i]; o[j] += s; }
 }
@@ -305,7 +312,26 @@ enum ReferenceObjectID {
 };
 
 class GridObject {};
-class ISubsetHandler {};
+// Subsets: index 0 is the element subset, 1 the boundary subset a driver marks
+// (the element-local sides that lie on it are set per element with
+// shim_boundary_sides() before the geometry update).
+class ISubsetHandler {
+  public:
+    int num_subsets() const { return 2; }
+};
+class SubsetGroup {
+  public:
+    size_t size() const { return m_si.size(); }
+    int operator[](size_t i) const { return m_si[i]; }
+    void add(int si) { m_si.push_back(si); }
+
+  private:
+    std::vector<int> m_si;
+};
+inline unsigned& shim_boundary_sides() {
+    static thread_local unsigned mask = 0;
+    return mask;
+}
 
 // Reference-element tables in ugcore numbering: corners, edges (= the SCVFs of
 // the FV1 dual mesh, oriented from corner 0 to corner 1) and sides.
@@ -481,6 +507,12 @@ inline number p1_shape(ReferenceObjectID roid, size_t k, const number* x) {
             const number b = (k >= 2) ? x[1] : 1.0 - x[1];
             return a * b;
         }
+        case ROID_PRISM: {
+            // triangle shape of corner k % 3 times the linear shape in z
+            const size_t q = k % 3;
+            const number t = q == 0 ? 1.0 - x[0] - x[1] : x[q - 1];
+            return t * ((k >= 3) ? x[2] : 1.0 - x[2]);
+        }
         case ROID_HEXAHEDRON: {
             const size_t q = k % 4;
             const number a = (q == 1 || q == 2) ? x[0] : 1.0 - x[0];
@@ -502,6 +534,14 @@ inline number p1_deriv(ReferenceObjectID roid, size_t k, int d, const number* x)
             const number a = (k == 1 || k == 2) ? x[0] : 1.0 - x[0];
             const number b = (k >= 2) ? x[1] : 1.0 - x[1];
             return d == 0 ? s0 * b : s1 * a;
+        }
+        case ROID_PRISM: {
+            const size_t q = k % 3;
+            const number t = q == 0 ? 1.0 - x[0] - x[1] : x[q - 1];
+            const number z = (k >= 3) ? x[2] : 1.0 - x[2];
+            if (d == 2) return (k >= 3) ? t : -t;
+            const number dt = q == 0 ? -1.0 : ((size_t)d == q - 1 ? 1.0 : 0.0);
+            return dt * z;
         }
         case ROID_HEXAHEDRON: {
             const size_t q = k % 4;
@@ -756,14 +796,27 @@ class IElemDisc {
     void register_import(IDataImport&) {}
     virtual void prepare_setting(const std::vector<LFEID>&, bool) {}
     virtual bool requests_local_time_series() { return false; }
-    virtual std::string disc_type() const = 0;
+    virtual std::string disc_type() const { return ""; }
     // time dependence as set by the driver: the current and the old local solution
     bool is_time_dependent() const { return m_pTimeSeries != nullptr; }
     const LocalVectorTimeSeries* local_time_solutions() const { return m_pTimeSeries; }
     void set_time_series(const LocalVectorTimeSeries* ts) { m_pTimeSeries = ts; }
     const ISubsetHandler& subset_handler() const { return m_sh; }
+    const std::vector<std::string>& symb_fcts() const { return m_vFct; }
+    const std::vector<std::string>& symb_subsets() const { return m_vSubset; }
+    // every boundary subset name maps to subset 1
+    struct ApproxSpace {
+        SubsetGroup subset_grp_by_name(const char*) const { SubsetGroup g; g.add(1); return g; }
+    };
+    struct FunctionPattern {
+        const ISubsetHandler* sh;
+        const ISubsetHandler* subset_handler() const { return sh; }
+    };
+    const ApproxSpace* approx_space() const { static const ApproxSpace a; return &a; }
+    const FunctionPattern* function_pattern() const { m_fp.sh = &m_sh; return &m_fp; }
 
   protected:
+    mutable FunctionPattern m_fp{nullptr};
     std::vector<std::string> m_vFct, m_vSubset;
     const LocalVectorTimeSeries* m_pTimeSeries = nullptr;
     ISubsetHandler m_sh;

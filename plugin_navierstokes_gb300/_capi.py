@@ -27,9 +27,10 @@ ERR_TIMEOUT = 8
 TRIANGLE = 2
 QUADRILATERAL = 3
 TETRAHEDRON = 4
+PRISM = 6
 HEXAHEDRON = 8
-NSH = {TRIANGLE: 3, QUADRILATERAL: 4, TETRAHEDRON: 4, HEXAHEDRON: 8}
-DIM = {TRIANGLE: 2, QUADRILATERAL: 2, TETRAHEDRON: 3, HEXAHEDRON: 3}
+NSH = {TRIANGLE: 3, QUADRILATERAL: 4, TETRAHEDRON: 4, PRISM: 6, HEXAHEDRON: 8}
+DIM = {TRIANGLE: 2, QUADRILATERAL: 2, TETRAHEDRON: 3, PRISM: 3, HEXAHEDRON: 3}
 
 F64 = 0
 F32 = 1

@@ -54,12 +54,15 @@ static int difflen_id(const char* name) {
     return -1;
 }
 
-int ref_dim(int roid) { return (roid == ROID_TRIANGLE || roid == ROID_QUADRILATERAL) ? 2 : (roid == ROID_TETRAHEDRON || roid == ROID_HEXAHEDRON) ? 3 : 0; }
+int ref_dim(int roid) {
+    return (roid == ROID_TRIANGLE || roid == ROID_QUADRILATERAL) ? 2 : (roid == ROID_TETRAHEDRON || roid == ROID_PRISM || roid == ROID_HEXAHEDRON) ? 3 : 0;
+}
 int ref_nsh(int roid) {
     switch (roid) {
         case ROID_TRIANGLE: return 3;
         case ROID_QUADRILATERAL: return 4;
         case ROID_TETRAHEDRON: return 4;
+        case ROID_PRISM: return 6;
         case ROID_HEXAHEDRON: return 8;
     }
     return 0;
@@ -601,6 +604,7 @@ double ref_co(int roid, int c, int d) {
         case ROID_TRIANGLE: return Ref<ROID_TRIANGLE>::co(c, d);
         case ROID_QUADRILATERAL: return Ref<ROID_QUADRILATERAL>::co(c, d);
         case ROID_TETRAHEDRON: return Ref<ROID_TETRAHEDRON>::co(c, d);
+        case ROID_PRISM: return Ref<ROID_PRISM>::co(c, d);
         case ROID_HEXAHEDRON: return Ref<ROID_HEXAHEDRON>::co(c, d);
     }
     return 0.0;
@@ -970,6 +974,7 @@ int nsfv1_ref_tables(int elem_type, int* nco, int* nedge, int* edges, int* nside
         case ROID_TRIANGLE: fill(std::integral_constant<int, ROID_TRIANGLE>{}); return NSFV1_OK;
         case ROID_QUADRILATERAL: fill(std::integral_constant<int, ROID_QUADRILATERAL>{}); return NSFV1_OK;
         case ROID_TETRAHEDRON: fill(std::integral_constant<int, ROID_TETRAHEDRON>{}); return NSFV1_OK;
+        case ROID_PRISM: fill(std::integral_constant<int, ROID_PRISM>{}); return NSFV1_OK;
         case ROID_HEXAHEDRON: fill(std::integral_constant<int, ROID_HEXAHEDRON>{}); return NSFV1_OK;
     }
     return NSFV1_ERR_ARGUMENT;

@@ -80,10 +80,12 @@ template <int ROID, typename F> constexpr ElemTabT<F> make_tab() {
 static __constant__ ElemTabT<double> c_tabTri = make_tab<ROID_TRIANGLE, double>();
 static __constant__ ElemTabT<double> c_tabQuad = make_tab<ROID_QUADRILATERAL, double>();
 static __constant__ ElemTabT<double> c_tabTet = make_tab<ROID_TETRAHEDRON, double>();
+static __constant__ ElemTabT<double> c_tabPrism = make_tab<ROID_PRISM, double>();
 static __constant__ ElemTabT<double> c_tabHex = make_tab<ROID_HEXAHEDRON, double>();
 static __constant__ ElemTabT<float> c_tabTriF = make_tab<ROID_TRIANGLE, float>();
 static __constant__ ElemTabT<float> c_tabQuadF = make_tab<ROID_QUADRILATERAL, float>();
 static __constant__ ElemTabT<float> c_tabTetF = make_tab<ROID_TETRAHEDRON, float>();
+static __constant__ ElemTabT<float> c_tabPrismF = make_tab<ROID_PRISM, float>();
 static __constant__ ElemTabT<float> c_tabHexF = make_tab<ROID_HEXAHEDRON, float>();
 
 template <int ROID, typename F = double> __device__ __forceinline__ const ElemTabT<F>& tab() {
@@ -91,11 +93,13 @@ template <int ROID, typename F = double> __device__ __forceinline__ const ElemTa
         if constexpr (ROID == ROID_TRIANGLE) return c_tabTriF;
         else if constexpr (ROID == ROID_QUADRILATERAL) return c_tabQuadF;
         else if constexpr (ROID == ROID_TETRAHEDRON) return c_tabTetF;
+        else if constexpr (ROID == ROID_PRISM) return c_tabPrismF;
         else return c_tabHexF;
     } else {
         if constexpr (ROID == ROID_TRIANGLE) return c_tabTri;
         else if constexpr (ROID == ROID_QUADRILATERAL) return c_tabQuad;
         else if constexpr (ROID == ROID_TETRAHEDRON) return c_tabTet;
+        else if constexpr (ROID == ROID_PRISM) return c_tabPrism;
         else return c_tabHex;
     }
 }
@@ -134,7 +138,7 @@ __device__ __forceinline__ double flip_sign(const double v) {
 }
 __device__ __forceinline__ float flip_sign(const float v) { return __int_as_float(__float_as_int(v) ^ (int)0x80000000u); }
 
-// Affine test: simplices always; a quadrilateral / hexahedron when every corner
+// Affine test: simplices always, prisms never; a quadrilateral / hexahedron when every corner
 // equals x0 + the sum of its edge vectors to within rtol of the element size.
 // On such elements the mapping Jacobian is one constant matrix and the FV1
 // quantities below are evaluated from it (algebraically identical to the
@@ -145,6 +149,8 @@ template <typename T> __device__ __forceinline__ T nanmax(const T a, const T b) 
 template <int ROID, typename T>
 __device__ __forceinline__ bool elem_is_affine(const Elem<ROID, T>& E) {
     if constexpr (ROID == ROID_TRIANGLE || ROID == ROID_TETRAHEDRON) return true;
+    // prisms always take the general path (J at every integration point)
+    if constexpr (ROID == ROID_PRISM) return false;
     const T rtol = sizeof(T) == 8 ? T(1e-14) : T(1e-6);
     T sz = T(0), dev = T(0);
     if constexpr (ROID == ROID_QUADRILATERAL) {
@@ -367,6 +373,15 @@ __device__ __forceinline__ void p1_eval(const double* x, double (&N)[Ref<ROID>::
         N[0] = (1.0 - a) * (1.0 - b); N[1] = a * (1.0 - b); N[2] = a * b; N[3] = (1.0 - a) * b;
         G[0][0] = -(1.0 - b); G[0][1] = -(1.0 - a); G[1][0] = 1.0 - b; G[1][1] = -a;
         G[2][0] = b;          G[2][1] = a;          G[3][0] = -b;      G[3][1] = 1.0 - a;
+    } else if constexpr (ROID == ROID_PRISM) {
+        const double t[3] = {1.0 - a - b, a, b}, dt[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const int i = k % 3;
+            const double z = k >= 3 ? c : 1.0 - c, dz = k >= 3 ? 1.0 : -1.0;
+            N[k] = t[i] * z;
+            G[k][0] = dt[i][0] * z; G[k][1] = dt[i][1] * z; G[k][2] = t[i] * dz;
+        }
     } else if constexpr (ROID == ROID_TETRAHEDRON) {
         N[0] = 1.0 - a - b - c; N[1] = a; N[2] = b; N[3] = c;
 #pragma unroll
@@ -432,10 +447,12 @@ __device__ __forceinline__ bool ray_upwind(const Elem<ROID, T>& E, const T* from
     T gInt[3] = {T(0), T(0), T(0)}, lInt[3] = {T(0), T(0), T(0)};
 #pragma unroll 1
     for (int s = 0; s < R::nside && hitSide < 0; ++s) {
-        constexpr int ntri = (dim == 3 && R::side_nco(0) == 4) ? 2 : 1;
+        // quadrilateral sides as two triangles (a prism mixes triangle and quadrilateral sides)
+        constexpr int ntriMax = (dim == 3 && (R::side_nco(0) == 4 || ROID == ROID_PRISM)) ? 2 : 1;
+        const int ntri = (ROID == ROID_PRISM) ? (tb.sideNco[s] == 4 ? 2 : 1) : ntriMax;
 #pragma unroll
-        for (int tr = 0; tr < ntri; ++tr) {
-            if (hitSide >= 0) break;
+        for (int tr = 0; tr < ntriMax; ++tr) {
+            if (hitSide >= 0 || tr >= ntri) break;
             if constexpr (dim == 2) {
                 const int i0 = tb.side[s][0], i1 = tb.side[s][1];
                 T p0[2], p1[2];
@@ -507,6 +524,10 @@ __device__ __forceinline__ bool ray_upwind(const Elem<ROID, T>& E, const T* from
                 const T xa = (k == 1 || k == 2) ? lInt[0] : T(1) - lInt[0];
                 const T xb = (k == 2 || k == 3) ? lInt[1] : T(1) - lInt[1];
                 v = xa * xb;
+            } else if constexpr (ROID == ROID_PRISM) {
+                const int q = k % 3;
+                const T t = q == 0 ? T(1) - lInt[0] - lInt[1] : lInt[q - 1];
+                v = t * ((k >= 3) ? lInt[2] : T(1) - lInt[2]);
             } else {
                 const T xa = (k == 1 || k == 2 || k == 5 || k == 6) ? lInt[0] : T(1) - lInt[0];
                 const T xb = (k == 2 || k == 3 || k == 6 || k == 7) ? lInt[1] : T(1) - lInt[1];
@@ -644,7 +665,10 @@ __device__ __forceinline__ bool upwind_shapes(const int type, const Elem<ROID, T
         convLen = T(1);
         return true;
     }
-    if (type == UPW_LPS && E.affine) return lps_affine<ROID, T>(tab<ROID, T>(), wref, ip, down, vnorm, up, convLen);
+    // (prisms are never affine here, so they always take the general ray test)
+    if constexpr (ROID != ROID_PRISM) {
+        if (type == UPW_LPS && E.affine) return lps_affine<ROID, T>(tab<ROID, T>(), wref, ip, down, vnorm, up, convLen);
+    }
     return ray_upwind<ROID, T>(E, G.gip, vel, type == UPW_LPS, up, convLen);
 }
 

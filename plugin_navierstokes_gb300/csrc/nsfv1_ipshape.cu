@@ -385,6 +385,7 @@ cudaError_t dispatch_roid_ip(int roid, F&& f) {
         case ROID_TRIANGLE: f(std::integral_constant<int, ROID_TRIANGLE>{}); break;
         case ROID_QUADRILATERAL: f(std::integral_constant<int, ROID_QUADRILATERAL>{}); break;
         case ROID_TETRAHEDRON: f(std::integral_constant<int, ROID_TETRAHEDRON>{}); break;
+        case ROID_PRISM: f(std::integral_constant<int, ROID_PRISM>{}); break;
         case ROID_HEXAHEDRON: f(std::integral_constant<int, ROID_HEXAHEDRON>{}); break;
         default: return cudaErrorInvalidValue;
     }

@@ -3,7 +3,7 @@
 
 namespace nsfv1 {
 
-enum { ROID_TRIANGLE = 2, ROID_QUADRILATERAL = 3, ROID_TETRAHEDRON = 4, ROID_HEXAHEDRON = 8 };
+enum { ROID_TRIANGLE = 2, ROID_QUADRILATERAL = 3, ROID_TETRAHEDRON = 4, ROID_PRISM = 6, ROID_HEXAHEDRON = 8 };
 enum { UPW_NO = 0, UPW_FULL = 1, UPW_SKEWED = 2, UPW_LPS = 3, UPW_POS = 4 };
 enum { STAB_FIELDS = 0, STAB_FLOW = 1, STAB_WITHOUT = 2 };
 enum { DL_RAW = 0, DL_FIVEPOINT = 1, DL_COR = 2 };

@@ -96,6 +96,33 @@ template <> struct Ref<ROID_HEXAHEDRON> {
     }
 };
 
+// Prism: triangle (0, 1, 2) at z = 0 extruded to (3, 4, 5) at z = 1; sides 0 and 4
+// are the triangles, 1..3 the quadrilaterals (outward corner order as the others).
+template <> struct Ref<ROID_PRISM> {
+    static constexpr int dim = 3, nsh = 6, nip = 9, nside = 5, b = 4;
+    NSFV1_HD static constexpr double co(int c, int d) {
+        return d == 0 ? ((c == 1 || c == 4) ? 1.0 : 0.0) : d == 1 ? ((c == 2 || c == 5) ? 1.0 : 0.0) : (c >= 3 ? 1.0 : 0.0);
+    }
+    NSFV1_HD static constexpr int edge(int e, int k) {
+        constexpr int t[9][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 4}, {2, 5}, {3, 4}, {4, 5}, {5, 3}};
+        return t[e][k];
+    }
+    NSFV1_HD static constexpr int side_nco(int s) { return (s == 0 || s == 4) ? 3 : 4; }
+    NSFV1_HD static constexpr int side(int s, int j) {
+        constexpr int t[5][4] = {{0, 2, 1, 0}, {0, 1, 4, 3}, {1, 2, 5, 4}, {2, 0, 3, 5}, {3, 4, 5, 3}};
+        return t[s][j];
+    }
+    NSFV1_HD static constexpr int edge_face(int e, int k) {
+        constexpr int t[9][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 3}, {2, 1}, {3, 2}, {1, 4}, {2, 4}, {3, 4}};
+        return t[e][k];
+    }
+    NSFV1_HD static constexpr int scv_tab(int a, int k) {
+        constexpr int t[6][6] = {{0, 0, 2, 3, 1, 3}, {0, 0, 1, 4, 1, 2}, {1, 0, 2, 5, 2, 3},
+                                 {3, 1, 6, 8, 3, 4}, {4, 1, 6, 7, 2, 4}, {5, 2, 7, 8, 3, 4}};
+        return t[a][k];
+    }
+};
+
 // ---- derived compile-time quantities --------------------------------------
 
 // local (reference) coordinates of the element centre, face centres, edge mids,
@@ -125,6 +152,10 @@ template <int ROID> NSFV1_HD constexpr double p1_shape(int k, double a, double b
     if (ROID == ROID_QUADRILATERAL)
         return k == 0 ? (1.0 - a) * (1.0 - b) : k == 1 ? a * (1.0 - b) : k == 2 ? a * b : (1.0 - a) * b;
     if (ROID == ROID_TETRAHEDRON) return k == 0 ? 1.0 - a - b - c : k == 1 ? a : k == 2 ? b : c;
+    if (ROID == ROID_PRISM) {
+        const double t = k == 0 || k == 3 ? 1.0 - a - b : (k == 1 || k == 4) ? a : b;
+        return t * (k >= 3 ? c : 1.0 - c);
+    }
     // hexahedron
     return k == 0 ? (1.0 - a) * (1.0 - b) * (1.0 - c) : k == 1 ? a * (1.0 - b) * (1.0 - c)
          : k == 2 ? a * b * (1.0 - c) : k == 3 ? (1.0 - a) * b * (1.0 - c)
@@ -138,6 +169,12 @@ template <int ROID> NSFV1_HD constexpr double p1_grad(int k, int d, double a, do
         return k == 0 ? -(1.0 - a) : k == 1 ? -a : k == 2 ? a : (1.0 - a);
     }
     if (ROID == ROID_TETRAHEDRON) return k == 0 ? -1.0 : (k - 1 == d ? 1.0 : 0.0);
+    if (ROID == ROID_PRISM) {
+        const double t = k == 0 || k == 3 ? 1.0 - a - b : (k == 1 || k == 4) ? a : b;
+        const double dt = k == 0 || k == 3 ? -1.0 : ((k == 1 || k == 4) ? (d == 0 ? 1.0 : 0.0) : (d == 1 ? 1.0 : 0.0));
+        const double z = k >= 3 ? c : 1.0 - c;
+        return d == 2 ? (k >= 3 ? t : -t) : dt * z;
+    }
     const double xa = (k == 1 || k == 2 || k == 5 || k == 6) ? a : 1.0 - a;
     const double xb = (k == 2 || k == 3 || k == 6 || k == 7) ? b : 1.0 - b;
     const double xc = (k >= 4) ? c : 1.0 - c;

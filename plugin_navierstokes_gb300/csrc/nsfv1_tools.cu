@@ -122,6 +122,7 @@ __device__ bool point_in_elem(const Elem<ROID, double>& E, const double* x, doub
     const double tol = 1e-10;
     if constexpr (ROID == ROID_TRIANGLE) return xi[0] >= -tol && xi[1] >= -tol && 1.0 - xi[0] - xi[1] >= -tol;
     if constexpr (ROID == ROID_TETRAHEDRON) return xi[0] >= -tol && xi[1] >= -tol && xi[2] >= -tol && 1.0 - xi[0] - xi[1] - xi[2] >= -tol;
+    if constexpr (ROID == ROID_PRISM) return xi[0] >= -tol && xi[1] >= -tol && 1.0 - xi[0] - xi[1] >= -tol && xi[2] >= -tol && xi[2] <= 1.0 + tol;
     bool in = true;
 #pragma unroll
     for (int d = 0; d < dim; ++d) in &= (xi[d] >= -tol && xi[d] <= 1.0 + tol);
@@ -324,6 +325,7 @@ cudaError_t dispatch_roid_tools(int roid, F&& f) {
         case ROID_TRIANGLE: f(std::integral_constant<int, ROID_TRIANGLE>{}); break;
         case ROID_QUADRILATERAL: f(std::integral_constant<int, ROID_QUADRILATERAL>{}); break;
         case ROID_TETRAHEDRON: f(std::integral_constant<int, ROID_TETRAHEDRON>{}); break;
+        case ROID_PRISM: f(std::integral_constant<int, ROID_PRISM>{}); break;
         case ROID_HEXAHEDRON: f(std::integral_constant<int, ROID_HEXAHEDRON>{}); break;
         default: return cudaErrorInvalidValue;
     }

@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from ._capi import HEXAHEDRON, QUADRILATERAL, TETRAHEDRON, TRIANGLE
+from ._capi import HEXAHEDRON, PRISM, QUADRILATERAL, TETRAHEDRON, TRIANGLE
 
 _GOLDEN = np.uint64(0x9E3779B97F4A7C15)
 
@@ -81,6 +81,23 @@ def jittered_triangles(n: int, seed: int = 2, jitter: float = 0.2):
     t2 = np.where(even[:, None], np.stack([q0, q2, q3], 1), np.stack([q1, q2, q3], 1))
     conn = np.stack([t1, t2], axis=1).reshape(-1, 3).astype(np.int32)
     return TRIANGLE, coords, conn
+
+
+def extruded_prisms(n: int, nz: int | None = None, seed: int = 2, jitter: float = 0.2):
+    """The jittered n x n triangulation of [0,1]^2 (jittered_triangles) extruded to
+    nz layers in z (nz = n by default): 2 n^2 nz prisms, corners (t0, t1, t2) of a
+    layer's bottom then the same of its top (the reference prism's order)."""
+    nz = n if nz is None else nz
+    _, xy, tri = jittered_triangles(n, seed=seed, jitter=jitter)
+    # counter-clockwise triangles (positive orientation of the bottom face seen from above)
+    a, b, c = xy[tri[:, 0]], xy[tri[:, 1]], xy[tri[:, 2]]
+    cw = ((b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0])) < 0
+    tri = np.where(cw[:, None], tri[:, [0, 2, 1]], tri)
+    nn = xy.shape[0]
+    z = np.arange(nz + 1, dtype=np.float64) / nz
+    coords = np.concatenate([np.column_stack([xy, np.full(nn, zk)]) for zk in z])
+    layers = [np.concatenate([tri + k * nn, tri + (k + 1) * nn], axis=1) for k in range(nz)]
+    return PRISM, coords, np.concatenate(layers).astype(np.int32)
 
 
 def cavity_dirichlet(coords: np.ndarray, lid: float = 1.0, tol: float = 1e-12):

@@ -358,8 +358,8 @@ def mesh_pattern(elem_type: int, n_nodes: int, conn: np.ndarray):
 
 
 EX_VELOCITY, EX_VELOCITY_GRAD, EX_VELOCITY_IP, EX_PRESSURE, EX_PRESSURE_GRAD = range(5)
-_NSCVF = {2: 3, 3: 4, 4: 6, 8: 12}
-_NSH = {2: 3, 3: 4, 4: 4, 8: 8}
+_NSCVF = {2: 3, 3: 4, 4: 6, 6: 9, 8: 12}
+_NSH = {2: 3, 3: 4, 4: 4, 6: 6, 8: 8}
 
 
 class DataExport:

@@ -6,13 +6,14 @@ import numpy as np
 
 from plugin_navierstokes_gb300.mesh import uniform
 
-ROIDS = {"tri": 2, "quad": 3, "tet": 4, "hex": 8}
-NSH = {2: 3, 3: 4, 4: 4, 8: 8}
-DIM = {2: 2, 3: 2, 4: 3, 8: 3}
+ROIDS = {"tri": 2, "quad": 3, "tet": 4, "prism": 6, "hex": 8}
+NSH = {2: 3, 3: 4, 4: 4, 6: 6, 8: 8}
+DIM = {2: 2, 3: 2, 4: 3, 6: 3, 8: 3}
 REF = {
     2: np.array([[0, 0], [1, 0], [0, 1.0]]),
     3: np.array([[0, 0], [1, 0], [1, 1], [0, 1.0]]),
     4: np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1.0]]),
+    6: np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [0, 1, 1.0]]),
     8: np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1.0]]),
 }
 

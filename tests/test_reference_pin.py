@@ -255,3 +255,24 @@ def test_oracle_exports_match_the_reference_live(tname, which):
             v, d = o.export(which, roid, corners, u, uo, 0.01, kind, lips if kind == 2 else None)
             rv, rd = oracle.ref_export(which, roid, ref_config(dim, cfg), corners, u, uo, 0.01, kind, lips if kind == 2 else None)
             assert rel_err(v, rv) <= TOL and rel_err(d, rd) <= TOL, (tname, oracle.EXPORTS[which], cfg_name(cfg), kind)
+
+
+@pytest.mark.skipif(not has_ref, reason="reference checkout not present")
+@pytest.mark.parametrize("tname", list(ROIDS))
+@pytest.mark.parametrize("ci", range(len(DISC_CASES)))
+def test_oracle_outflow_matches_the_reference_live(tname, ci):
+    """NavierStokesNoNormalStressOutflowFV1 (no_normal_stress_outflow_fv1.cpp:343-504) on
+    elements with random outflow sides: the reference's own disc, on the stand-in's
+    boundary faces, against the oracle's element-level evaluation."""
+    roid = ROIDS[tname]
+    dim = DIM[roid]
+    nside = {2: 3, 3: 4, 4: 4, 6: 5, 8: 6}[roid]
+    cfg = DISC_CASES[ci]
+    corners = np.concatenate([random_elements(roid, 16, 900 + ci + roid), random_elements(roid, 4, 950 + ci, affine=True)])
+    u = random_local_u(roid, 20, 990 + ci)
+    masks = np.random.default_rng(ci + roid).integers(1, 2 ** nside, 20)
+    o = oracle.Oracle(dim)
+    configure(o, dim, cfg)
+    d, J = o.outflow_elem(roid, corners, u, masks)
+    rd, rJ = oracle.ref_outflow(roid, ref_config(dim, cfg), corners, u, masks)
+    assert np.abs(rd).max() > 0 and rel_err(d, rd) <= TOL and rel_err(J, rJ) <= TOL, (tname, cfg_name(cfg))
