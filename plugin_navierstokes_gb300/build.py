@@ -18,7 +18,7 @@ CSRC = HERE / "csrc"
 OUT_DIR = HERE / "lib"
 BUILD_DIR = HERE / "_build"
 LIB = OUT_DIR / "libnsfv1_gb300.so"
-SOURCES = ["nsfv1_assemble.cu", "nsfv1_ipshape.cu", "nsfv1_tools.cu", "nsfv1_solver.cu", "nsfv1_capi.cpp", "nsfv1_noalloc.cu", "nsfv1_batch.cu",
+SOURCES = ["nsfv1_assemble.cu", "nsfv1_jac_lanes.cu", "nsfv1_ipshape.cu", "nsfv1_tools.cu", "nsfv1_solver.cu", "nsfv1_capi.cpp", "nsfv1_noalloc.cu", "nsfv1_batch.cu",
            "nsfv1_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -327,6 +327,7 @@ cudaError_t launch_defect(int roid, const DiscParams& P, const AsmArgs& a, cudaS
 cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s, int threads) {
     if (a.count <= 0) return cudaSuccess;
     if (uses_ipshape(P)) return launch_jacobian_ipshape(roid, P, a, prec, s);
+    if (prec != 0) return launch_jacobian_lanes(roid, P, a, s);
     const int t = clamp_threads(threads);
     const int grid = (a.count + t - 1) / t;
     return dispatch_roid(roid, [&](auto r) {

@@ -1084,11 +1084,14 @@ __device__ __forceinline__ void jac_ip_factors(const DiscParams& P, const IpGeo<
     J.riVn = rho * S.idiag * Vn;
 }
 
-// The b x b block of SCVF ip and column corner k (added to row 'from', subtracted
-// from row 'to' by the caller), from the SCVF's factors.
-template <int ROID, typename T, bool PAC>
-__device__ __forceinline__ void jac_block(const DiscParams& P, const JacIp<ROID, T>& Jf, const int ip, const int k, const T nu,
-                                          T (&B)[Ref<ROID>::b][Ref<ROID>::b]) {
+// The b x b block of one SCVF and one column corner k (added to row 'from',
+// subtracted from row 'to' by the caller), from the SCVF's factors Jf (JacIp or
+// any type with its scalar members) and the column's inputs: lg = the reference
+// gradient and N the value of shape k at the SCVF's ip, upCk / upSk / dnSk its
+// convection-upwind, stabilisation-upwind and downwind shapes.
+template <int ROID, typename T, bool PAC, class F>
+__device__ __forceinline__ void jac_block_col(const DiscParams& P, const F& Jf, const T (&lg)[3], const T N, const T upCk,
+                                              const T upSk, const T dnSk, const T nu, T (&B)[Ref<ROID>::b][Ref<ROID>::b]) {
     using R = Ref<ROID>;
     constexpr int dim = R::dim, Pc = dim;
     const T rho = T(P.rho), irho = T(1) / rho;
@@ -1106,17 +1109,13 @@ __device__ __forceinline__ void jac_block(const DiscParams& P, const JacIp<ROID,
     {
         {
             T g[3];
-            {
-                const auto& tb = tab<ROID, T>();
 #pragma unroll
-                for (int r = 0; r < dim; ++r) {
-                    T sacc = T(0);
+            for (int r = 0; r < dim; ++r) {
+                T sacc = T(0);
 #pragma unroll
-                    for (int c = 0; c < dim; ++c) sacc += G.JtInv[r][c] * T(tb.ipLGrad[ip][k][c]);
-                    g[r] = sacc;
-                }
+                for (int c = 0; c < dim; ++c) sacc += G.JtInv[r][c] * lg[c];
+                g[r] = sacc;
             }
-            const T N = ipN<ROID, T>(ip, k);
             T gn = T(0), Vg = T(0);
 #pragma unroll
             for (int d = 0; d < dim; ++d) { gn += g[d] * G.n[d]; Vg += S.StdVel[d] * g[d]; }
@@ -1124,7 +1123,7 @@ __device__ __forceinline__ void jac_block(const DiscParams& P, const JacIp<ROID,
             T dd = mnr * gn;
             // convection (fixpoint part) on the diagonal: the upwind shape, the Peclet blend
             if (!P.stokes) {
-                if (!pac) dd += S.upC[k] * pw;
+                if (!pac) dd += upCk * pw;
                 if (P.peclet) dd += ppe * N;
             }
 #pragma unroll
@@ -1139,7 +1138,7 @@ __device__ __forceinline__ void jac_block(const DiscParams& P, const JacIp<ROID,
 #pragma unroll
                 for (int d2 = 0; d2 < dim; ++d2) {
                     // upwind used as upwind (:521-534, the factor is not applied there) and the Peclet blend
-                    T pv = pac ? T(0) : w * S.upC[k] * nrho[d2];
+                    T pv = pac ? T(0) : w * upCk * nrho[d2];
                     if (P.peclet) pv += (T(1) - w) * N * nrho[d2];
 #pragma unroll
                     for (int d1 = 0; d1 < dim; ++d1) B[d1][d2] += pv * UpwindVel[d1];
@@ -1157,8 +1156,8 @@ __device__ __forceinline__ void jac_block(const DiscParams& P, const JacIp<ROID,
             } else {
                 Sk = S.nuL * N;
                 if (!P.stokes) {
-                    Sk += S.nsvcl * S.upS[k];
-                    if (P.stab == STAB_FLOW) Sk += S.nsvdl * (S.dnS[k] - S.upS[k]);
+                    Sk += S.nsvcl * upSk;
+                    if (P.stab == STAB_FLOW) Sk += S.nsvdl * (dnSk - upSk);
                 }
                 if (P.stab == STAB_FLOW) {
                     const T sv = Sk - Vg;
@@ -1221,6 +1220,16 @@ __device__ __forceinline__ void jac_block(const DiscParams& P, const JacIp<ROID,
             }
         }
     }
+}
+
+// The block of SCVF ip and column corner k from the SCVF's JacIp and the
+// reference-element tables.
+template <int ROID, typename T, bool PAC>
+__device__ __forceinline__ void jac_block(const DiscParams& P, const JacIp<ROID, T>& Jf, const int ip, const int k, const T nu,
+                                          T (&B)[Ref<ROID>::b][Ref<ROID>::b]) {
+    const auto& tb = tab<ROID, T>();
+    const T lg[3] = {T(tb.ipLGrad[ip][k][0]), T(tb.ipLGrad[ip][k][1]), Ref<ROID>::dim == 3 ? T(tb.ipLGrad[ip][k][2]) : T(0)};
+    jac_block_col<ROID, T, PAC>(P, Jf, lg, ipN<ROID, T>(ip, k), Jf.upC[k], Jf.upS[k], Jf.dnS[k], nu, B);
 }
 
 template <int ROID, typename T, bool PAC, class Sink>

@@ -44,6 +44,8 @@ cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int
 // state) at the same state, one launch per colour
 cudaError_t launch_defect_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s, int threads = 128);
 cudaError_t launch_elem_batch(int roid, const DiscParams& P, const ElemBatchArgs& a, cudaStream_t s);
+// FP32 Jacobian (values only, no defect) with one lane per element corner
+cudaError_t launch_jacobian_lanes(int roid, const DiscParams& P, const AsmArgs& a, cudaStream_t s);
 // The positive-upwind element path (uses_ipshape(P)): defect, Jacobian (prec 0: FP64,
 // 1: FP32 values of FP64 arithmetic) and the stiffness part of the element batch;
 // P.ipws must hold ipws_doubles_host(dim) doubles for each of P.ipwsStride threads.
