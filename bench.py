@@ -337,7 +337,7 @@ def main():
     torch.cuda.synchronize()
     ms64 = sum(t64) / args.steps
     ms32 = sum(t32) / args.steps
-    J32f = J32.cpu().numpy()   # the fused pass's FP32 Jacobian, for the oracle check
+    J32f = J32.cpu().numpy()   # the FP32 Jacobian of the defect + Jacobian call, for the oracle check
     # the FP32 Jacobian kernel alone (the Newton loop assembles it at an iterate whose defect is known)
     (tjac32,) = timed([lambda: d.assemble_jacobian(tu, J32, stream=stream)], args.steps)
     if world > 1:
@@ -438,9 +438,9 @@ def main():
                                    "autotune_ms": dict(zip(("32", "64", "128"), [round(x, 3) for x in asm_ms])),
                                    "oracle_check": check,
                                    "fp32_jacobian_mode": {"value": world * n_el / (ms32 * 1e-3), "ms_per_step": ms32,
-                                                          "step": "FP64 defect + FP32 Jacobian in one pass (blocks from the FP64 state)",
+                                                          "step": "FP64 defect + FP32 Jacobian (nsfv1_assemble_defect_jacobian with FP32 values: per colour the FP64 defect kernel, then the lane-per-corner FP32 Jacobian kernel)",
                                                           "jacobian_only_ms": jac32_ms,
-                                                          "roofline": {"bound": "hbm", "kernel": "FP32 Jacobian assembly alone",
+                                                          "roofline": {"bound": "hbm", "kernel": "FP32 Jacobian assembly alone (k_jacobian_lanes, one lane per element corner)",
                                                                        "achieved": alg32 / (jac32_ms * 1e-3) / 1e9, "peak": peak,
                                                                        "unit": "GB/s", "frac": alg32 / (jac32_ms * 1e-3) / 1e9 / peak,
                                                                        "algorithmic_bytes": alg32,

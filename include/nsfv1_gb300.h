@@ -199,8 +199,9 @@ int nsfv1_assemble_jacobian(nsfv1_disc* h, const double* u, const double* u_old,
  * stabilisation feed both, where the reference evaluates them in each of
  * add_def_A_elem and add_jac_A_elem (navier_stokes_fv1.cpp:296-309, 645-659).
  * NSFV1_F64: the same results as nsfv1_assemble_defect + nsfv1_assemble_jacobian.
- * NSFV1_F32: the FP64 defect, and FP32 Jacobian blocks formed in FP32 from the
- * FP64 per-SCVF state (vals 16-byte aligned for 3D meshes). */
+ * NSFV1_F32: the FP64 defect and the FP32 Jacobian of nsfv1_assemble_jacobian,
+ * colour by colour (vals 16-byte aligned for 3D meshes); the same results as the
+ * two calls. */
 int nsfv1_assemble_defect_jacobian(nsfv1_disc* h, const double* u, const double* u_old, double dt, double* d, void* vals, int prec,
                                    void* stream);
 /* The reference's per-element callbacks, batched over n independent elements

@@ -36,15 +36,23 @@ def _flags(extra: list[str] | None = None) -> list[str]:
     return f + (extra or [])
 
 
-def compile_bounds_checked(out: Path) -> Path:
+BOUNDS_CHECKED_SOURCES = ["nsfv1_assemble.cu", "nsfv1_jac_lanes.cu"]
+
+
+def compile_bounds_checked(out: Path) -> list[Path]:
     """Compiles the assembly kernels with NSFV1_BOUNDS_CHECK (every node id and
     block index checked, out-of-range accesses skipped and reported through the
-    error word) into the object file out."""
-    cmd = [nvcc_path()] + _flags(["-DNSFV1_BOUNDS_CHECK"]) + ["-c", str(CSRC / "nsfv1_assemble.cu"), "-o", str(out)]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("nvcc failed for the bounds-checked assembly:\n" + r.stdout + r.stderr)
-    return out
+    error word): one object file per assembly source, named after out."""
+    def one(src: str) -> Path:
+        obj = out.with_name(out.stem + "_" + Path(src).stem + out.suffix)
+        cmd = [nvcc_path()] + _flags(["-DNSFV1_BOUNDS_CHECK"]) + ["-c", str(CSRC / src), "-o", str(obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for the bounds-checked {src}:\n" + r.stdout + r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(BOUNDS_CHECKED_SOURCES)) as ex:
+        return list(ex.map(one, BOUNDS_CHECKED_SOURCES))
 
 
 def _needs_rebuild() -> bool:

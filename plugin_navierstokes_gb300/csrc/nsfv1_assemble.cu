@@ -123,8 +123,9 @@ __global__ void __launch_bounds__(kThreads) k_jacobian(const DiscParams P, const
 // Defect and FP64 Jacobian at the same state in one pass over the elements of a
 // colour (one launch per colour instead of two): the per-SCVF geometry, upwinds
 // and stabilisation are evaluated once for both outputs.
-template <int ROID, bool TRANSIENT, typename VT, bool PAC>
+template <int ROID, bool TRANSIENT, bool PAC>
 __global__ void __launch_bounds__(kThreads) k_defect_jacobian(const DiscParams P, const AsmArgs A) {
+    using VT = double;
     using R = Ref<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, b = R::b;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -163,13 +164,8 @@ __global__ void __launch_bounds__(kThreads) k_defect_jacobian(const DiscParams P
     } ss{sink, P.dt};
     const double* uoPtr = TRANSIENT ? &uo[0][0] : &u[0][0];
     const double(&uoRef)[dim][nsh] = *reinterpret_cast<const double(*)[dim][nsh]>(uoPtr);
-    if constexpr (std::is_same<VT, double>::value) {
-        if constexpr (TRANSIENT) ok = elem_def_jac_A<ROID, double, PAC>(Q, E, u, uoRef, ss, P.dt, jsink, nuEl);
-        else ok = elem_def_jac_A<ROID, double, PAC>(Q, E, u, uoRef, sink, 1.0, jsink, nuEl);
-    } else {
-        if constexpr (TRANSIENT) ok = elem_def_jac_A_mixed<ROID, PAC>(Q, E, u, uoRef, ss, (float)P.dt, jsink, nuEl);
-        else ok = elem_def_jac_A_mixed<ROID, PAC>(Q, E, u, uoRef, sink, 1.0f, jsink, nuEl);
-    }
+    if constexpr (TRANSIENT) ok = elem_def_jac_A<ROID, double, PAC>(Q, E, u, uoRef, ss, P.dt, jsink, nuEl);
+    else ok = elem_def_jac_A<ROID, double, PAC>(Q, E, u, uoRef, sink, 1.0, jsink, nuEl);
     if (!ok) atomicOr(A.err, 1);
     // mass (implicit Euler) and source parts, per SCV: defect as in k_defect, Jacobian as in k_jacobian
     const double rho = P.rho;
@@ -332,13 +328,8 @@ cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int
     const int grid = (a.count + t - 1) / t;
     return dispatch_roid(roid, [&](auto r) {
         constexpr int RO = decltype(r)::value;
-        if (P.pac && !P.stokes) {
-            if (prec == 0) k_jacobian<RO, double, double, true><<<grid, t, 0, s>>>(P, a);
-            else k_jacobian<RO, float, float, true><<<grid, t, 0, s>>>(P, a);
-        } else {
-            if (prec == 0) k_jacobian<RO, double, double, false><<<grid, t, 0, s>>>(P, a);
-            else k_jacobian<RO, float, float, false><<<grid, t, 0, s>>>(P, a);
-        }
+        if (P.pac && !P.stokes) k_jacobian<RO, double, double, true><<<grid, t, 0, s>>>(P, a);
+        else k_jacobian<RO, double, double, false><<<grid, t, 0, s>>>(P, a);
     });
 }
 
@@ -349,27 +340,23 @@ cudaError_t launch_defect_jacobian(int roid, const DiscParams& P, const AsmArgs&
         const cudaError_t e = launch_defect_ipshape(roid, P, a, s);
         return e != cudaSuccess ? e : launch_jacobian_ipshape(roid, P, a, prec, s);
     }
+    if (prec != 0) {
+        // FP32 blocks: the FP64 defect, then the lane-per-corner FP32 Jacobian of the
+        // same colour (faster than forming FP32 blocks inside the FP64 pass)
+        const cudaError_t e = launch_defect(roid, P, a, s, threads);
+        return e != cudaSuccess ? e : launch_jacobian_lanes(roid, P, a, s);
+    }
     const int t = clamp_threads(threads);
     const int grid = (a.count + t - 1) / t;
     return dispatch_roid(roid, [&](auto r) {
         constexpr int RO = decltype(r)::value;
         const bool pac = P.pac && !P.stokes;
-        if (prec == 0) {
-            if (P.transient) {
-                if (pac) k_defect_jacobian<RO, true, double, true><<<grid, t, 0, s>>>(P, a);
-                else k_defect_jacobian<RO, true, double, false><<<grid, t, 0, s>>>(P, a);
-            } else {
-                if (pac) k_defect_jacobian<RO, false, double, true><<<grid, t, 0, s>>>(P, a);
-                else k_defect_jacobian<RO, false, double, false><<<grid, t, 0, s>>>(P, a);
-            }
+        if (P.transient) {
+            if (pac) k_defect_jacobian<RO, true, true><<<grid, t, 0, s>>>(P, a);
+            else k_defect_jacobian<RO, true, false><<<grid, t, 0, s>>>(P, a);
         } else {
-            if (P.transient) {
-                if (pac) k_defect_jacobian<RO, true, float, true><<<grid, t, 0, s>>>(P, a);
-                else k_defect_jacobian<RO, true, float, false><<<grid, t, 0, s>>>(P, a);
-            } else {
-                if (pac) k_defect_jacobian<RO, false, float, true><<<grid, t, 0, s>>>(P, a);
-                else k_defect_jacobian<RO, false, float, false><<<grid, t, 0, s>>>(P, a);
-            }
+            if (pac) k_defect_jacobian<RO, false, true><<<grid, t, 0, s>>>(P, a);
+            else k_defect_jacobian<RO, false, false><<<grid, t, 0, s>>>(P, a);
         }
     });
 }

@@ -1274,67 +1274,6 @@ __device__ __forceinline__ bool elem_jac_A(const DiscParams& P, const Elem<ROID,
     return ok;
 }
 
-// FP32 copies of the per-SCVF geometry and state (the FP32-Jacobian blocks of
-// the fused pass are formed from the FP64 state the defect used)
-__device__ __forceinline__ void narrow(const IpGeo<double>& a, IpGeo<float>& o) {
-    o.from = a.from; o.to = a.to;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        o.n[d] = (float)a.n[d]; o.gip[d] = (float)a.gip[d]; o.em[d] = (float)a.em[d];
-        o.xf[d] = (float)a.xf[d]; o.xt[d] = (float)a.xt[d];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) o.JtInv[d][c] = (float)a.JtInv[d][c];
-    }
-}
-template <int ROID>
-__device__ __forceinline__ void narrow(const IpState<ROID, double>& a, IpState<ROID, float>& o) {
-#pragma unroll
-    for (int d = 0; d < 3; ++d) o.StdVel[d] = (float)a.StdVel[d];
-#pragma unroll
-    for (int k = 0; k < Ref<ROID>::nsh; ++k) { o.upC[k] = (float)a.upC[k]; o.upS[k] = (float)a.upS[k]; o.dnS[k] = (float)a.dnS[k]; }
-    o.nuL = (float)a.nuL; o.nsvcl = (float)a.nsvcl; o.nsvdl = (float)a.nsvdl;
-    o.diag = (float)a.diag; o.idiag = (float)a.idiag; o.ok = a.ok;
-}
-
-// FP64 defect and FP32 Jacobian of one element in one pass: geometry, upwinds,
-// stabilisation and defect in FP64; the Jacobian blocks in FP32 from that state.
-template <int ROID, bool PAC, class DSink, class JSink>
-__device__ __forceinline__ bool elem_def_jac_A_mixed(const DiscParams& P, const Elem<ROID, double>& E,
-                                                     const double (&u)[Ref<ROID>::b][Ref<ROID>::nsh],
-                                                     const double (&uo)[Ref<ROID>::dim][Ref<ROID>::nsh], DSink& dsink, const float jscale,
-                                                     JSink& jsink, const double nu) {
-    using R = Ref<ROID>;
-    constexpr int b = R::b, nsh = R::nsh;
-    double corMinN = 0.0, corMinD = 0.0, corAvgN = 1.0;
-    if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, double>(E, corMinN, corMinD, corAvgN);
-    constexpr int dim = R::dim;
-    float uf[b][nsh], uof[dim][nsh];
-#pragma unroll
-    for (int f = 0; f < b; ++f)
-#pragma unroll
-        for (int k = 0; k < nsh; ++k) uf[f][k] = (float)u[f][k];
-#pragma unroll
-    for (int f = 0; f < dim; ++f)
-#pragma unroll
-        for (int k = 0; k < nsh; ++k) uof[f][k] = P.transient ? (float)uo[f][k] : 0.0f;
-    bool ok = true;
-#pragma unroll 1
-    for (int ip = 0; ip < R::nip; ++ip) {
-        IpGeo<double> G;
-        ip_geom<ROID, double>(E, ip, G);
-        IpState<ROID, double> S;
-        ip_state<ROID, double>(P, E, G, ip, u, corMinN, corMinD, corAvgN, nu, S);
-        ok &= S.ok;
-        scvf_def_A<ROID, double>(P, E, G, S, ip, u, uo, dsink, nu);
-        IpGeo<float> Gf;
-        IpState<ROID, float> Sf;
-        narrow(G, Gf);
-        narrow<ROID>(S, Sf);
-        scvf_jac_A<ROID, float, PAC>(P, Gf, Sf, ip, uf, uof, jscale, jsink, (float)nu);
-    }
-    return ok;
-}
-
 // Defect and Jacobian of one element at the same state in one pass: the
 // geometry, upwind shapes and stabilisation of every SCVF are computed once and
 // feed both (the reference evaluates them separately in add_def_A_elem and

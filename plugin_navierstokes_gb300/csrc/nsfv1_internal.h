@@ -40,8 +40,8 @@ struct ElemBatchArgs {
 // threads: CTA size of the colour launches (32..128, a multiple of 32)
 cudaError_t launch_defect(int roid, const DiscParams& P, const AsmArgs& a, cudaStream_t s, int threads = 128);
 cudaError_t launch_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s, int threads = 128);
-// FP64 defect (a.D) and the Jacobian (a.vals; prec 0: FP64, 1: FP32 blocks from the FP64
-// state) at the same state, one launch per colour
+// FP64 defect (a.D) and the Jacobian (a.vals) at the same state: prec 0 one FP64 launch
+// per colour, prec 1 the FP64 defect and the lane-per-corner FP32 Jacobian of the colour
 cudaError_t launch_defect_jacobian(int roid, const DiscParams& P, const AsmArgs& a, int prec, cudaStream_t s, int threads = 128);
 cudaError_t launch_elem_batch(int roid, const DiscParams& P, const ElemBatchArgs& a, cudaStream_t s);
 // FP32 Jacobian (values only, no defect) with one lane per element corner

@@ -35,6 +35,9 @@ struct Lanes {
     static constexpr int EPC = WARPS * EPW;                 // elements per CTA
 };
 
+// floats per corner in the gather stage: coordinates (3), state (4), old state (4, PAC only)
+template <bool PAC> __host__ __device__ constexpr int corner_floats() { return PAC ? 12 : 8; }
+
 // slot layout: the scalar factors of JacIp, then its per-corner shapes
 enum : int {
     F_N = 0, F_IDIAG = 3, F_JT = 4, F_VEL = 13, F_UPV = 16, F_NUL = 19, F_NSVCL = 20, F_NSVDL = 21,
@@ -98,13 +101,31 @@ __device__ __forceinline__ void load_factors(const float* __restrict__ sl, LaneF
     F.w = a6.x; F.riVn = a6.y;
 }
 
-template <int ROID, bool PAC>
-__global__ void __launch_bounds__(Lanes<ROID>::THREADS, 3) k_jacobian_lanes(const DiscParams P, const AsmArgs A) {
+// SPEC fixes flags at compile time (the common configurations, much smaller
+// unrolled column loop): 0 = none, 1 = FLOW, 2 = FIELDS, both without Stokes,
+// Laplace or Peclet blend
+enum : int { SPEC_GENERIC = 0, SPEC_FLOW = 1, SPEC_FIELDS = 2 };
+
+inline int lanes_spec(const DiscParams& P) {
+    if (P.stokes || P.laplace || P.peclet) return SPEC_GENERIC;
+    return P.stab == STAB_FLOW ? SPEC_FLOW : P.stab == STAB_FIELDS ? SPEC_FIELDS : SPEC_GENERIC;
+}
+
+template <int ROID, bool PAC, int SPEC>
+__global__ void __launch_bounds__(Lanes<ROID>::THREADS, 3) k_jacobian_lanes(const DiscParams Pin, const AsmArgs A) {
+    // a local copy whose fixed members the compiler folds into the element code
+    DiscParams P = Pin;
+    if constexpr (SPEC != SPEC_GENERIC) {
+        P.stokes = 0; P.laplace = 0; P.peclet = 0;
+        P.stab = SPEC == SPEC_FLOW ? STAB_FLOW : STAB_FIELDS;
+    }
     using R = Ref<ROID>;
     using C = Lanes<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, nip = R::nip, b = R::b;
     constexpr int L = C::L, EPW = C::EPW, FS = C::FS;
+    constexpr int CF = corner_floats<PAC>();
     __shared__ __align__(16) float sSlots[C::EPC * nip * FS];
+    __shared__ __align__(16) float sCor[C::EPC * nsh * CF];   // the element's corners, converted once
     __shared__ float4 sTab[nip * nsh];   // (reference gradient, value) of shape k at SCVF ip
     {
         const auto& tb = tab<ROID, float>();
@@ -124,38 +145,59 @@ __global__ void __launch_bounds__(Lanes<ROID>::THREADS, 3) k_jacobian_lanes(cons
     // the lanes of this element (the whole group returns together above)
     const unsigned mask = ((1u << L) - 1u) << (grp * L);
     const float nuEl = (float)(A.nuElem ? __ldg(A.nuElem + e) : P.nu);
-    int32_t nodes[nsh];
+    // ---- gather: lane k converts corner k (coordinates relative to corner 0, in
+    // FP64 before the rounding, and the states) once for the whole group
+    const int32_t node0 = __ldg(A.conn + (int64_t)e * nsh);
+    const int32_t nodek = __ldg(A.conn + (int64_t)e * nsh + k);
+#ifdef NSFV1_BOUNDS_CHECK
+    // the group leaves together (the syncs below wait for all of its lanes)
+    const bool inRange = NSFV1_IN_RANGE(node0, A.nNodes, A.err) && NSFV1_IN_RANGE(nodek, A.nNodes, A.err);
+    if (!__all_sync(mask, inRange)) return;
+#endif
+    const bool withOld = PAC && P.transient && P.pac && P.fullNewton != 0.0;
+    float* myCor = sCor + (warp * EPW + grp) * nsh * CF;
+    {
+        float* dst = myCor + k * CF;
 #pragma unroll
-    for (int c = 0; c < nsh; ++c) {
-        nodes[c] = __ldg(A.conn + (int64_t)e * nsh + c);
-        if (!NSFV1_IN_RANGE(nodes[c], A.nNodes, A.err)) return;
+        for (int d = 0; d < dim; ++d)
+            dst[d] = (float)(__ldg(A.coords + (int64_t)nodek * dim + d) - __ldg(A.coords + (int64_t)node0 * dim + d));
+#pragma unroll
+        for (int f = 0; f < b; ++f) dst[3 + f] = (float)__ldg(A.U + (int64_t)nodek * b + f);
+        if constexpr (PAC) {
+#pragma unroll
+            for (int f = 0; f < dim; ++f) dst[7 + f] = withOld ? (float)__ldg(A.Uold + (int64_t)nodek * b + f) : 0.f;
+        }
     }
+    __syncwarp(mask);
     float* mySlots = sSlots + (warp * EPW + grp) * nip * FS;
     float volk = 0.f;
     bool ok = true;
     {
         // ---- phase 1: the factors of SCVFs k, k + nsh, ...
         Elem<ROID, float> E;
-        load_corners<ROID, float>(A.coords, nodes, E);
+        float u[b][nsh];
+        float uo[dim][nsh];
+#pragma unroll
+        for (int c = 0; c < nsh; ++c) {
+            const float4 a = *reinterpret_cast<const float4*>(myCor + c * CF);
+            const float4 v = *reinterpret_cast<const float4*>(myCor + c * CF + 4);
+            E.x[c][0] = a.x; E.x[c][1] = a.y;
+            if constexpr (dim == 3) E.x[c][2] = a.z;
+            u[0][c] = a.w; u[1][c] = v.x; u[2][c] = v.y;
+            if constexpr (b == 4) u[3][c] = v.z;
+            if constexpr (PAC) {
+                const float4 o = *reinterpret_cast<const float4*>(myCor + c * CF + 8);
+                // the stored old state starts at float 7: v.w, then o.x, o.y
+                uo[0][c] = v.w; uo[1][c] = o.x;
+                if constexpr (dim == 3) uo[2][c] = o.y;
+            } else {
+#pragma unroll
+                for (int d = 0; d < dim; ++d) uo[d][c] = 0.f;
+            }
+        }
         elem_setup<ROID, float>(E);
 #pragma unroll
         for (int c = 0; c < nsh; ++c) volk = (c == k) ? E.vol[c] : volk;
-        float u[b][nsh];
-        load_u<ROID, float>(A.U, nodes, u);
-        float uo[dim][nsh];
-        if (PAC && P.transient && P.pac && P.fullNewton != 0.0) {
-            float t4[b][nsh];
-            load_u<ROID, float>(A.Uold, nodes, t4);
-#pragma unroll
-            for (int d = 0; d < dim; ++d)
-#pragma unroll
-                for (int c = 0; c < nsh; ++c) uo[d][c] = t4[d][c];
-        } else {
-#pragma unroll
-            for (int d = 0; d < dim; ++d)
-#pragma unroll
-                for (int c = 0; c < nsh; ++c) uo[d][c] = 0.f;
-        }
         float corMinN = 0.f, corMinD = 0.f, corAvgN = 1.f;
         if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, float>(E, corMinN, corMinD, corAvgN);
 #pragma unroll 1
@@ -254,8 +296,11 @@ cudaError_t launch_jacobian_lanes(int roid, const DiscParams& P, const AsmArgs& 
         constexpr int RO = decltype(r)::value;
         using C = Lanes<RO>;
         const int grid = (a.count + C::EPC - 1) / C::EPC;
-        if (P.pac && !P.stokes) k_jacobian_lanes<RO, true><<<grid, C::THREADS, 0, s>>>(P, a);
-        else k_jacobian_lanes<RO, false><<<grid, C::THREADS, 0, s>>>(P, a);
+        const int spec = lanes_spec(P);
+        if (P.pac && !P.stokes) k_jacobian_lanes<RO, true, SPEC_GENERIC><<<grid, C::THREADS, 0, s>>>(P, a);
+        else if (spec == SPEC_FLOW) k_jacobian_lanes<RO, false, SPEC_FLOW><<<grid, C::THREADS, 0, s>>>(P, a);
+        else if (spec == SPEC_FIELDS) k_jacobian_lanes<RO, false, SPEC_FIELDS><<<grid, C::THREADS, 0, s>>>(P, a);
+        else k_jacobian_lanes<RO, false, SPEC_GENERIC><<<grid, C::THREADS, 0, s>>>(P, a);
     });
 }
 

@@ -176,5 +176,6 @@ def test_bounds_checked_assembly_compiles(tmp_path):
     an error bit instead of trapping) builds for sm_103a."""
     from plugin_navierstokes_gb300 import build
 
-    obj = build.compile_bounds_checked(tmp_path / "assemble_bc.o")
-    assert obj.exists() and obj.stat().st_size > 0
+    objs = build.compile_bounds_checked(tmp_path / "assemble_bc.o")
+    assert len(objs) == len(build.BOUNDS_CHECKED_SOURCES)
+    assert all(o.exists() and o.stat().st_size > 0 for o in objs)
