@@ -5,6 +5,7 @@
 // method, float for the FP32-Jacobian mode); Krylov vectors are FP64 in both;
 // reductions accumulate in FP64 with a fixed grid and a fixed summation tree,
 // so results are bitwise reproducible run to run.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <type_traits>
@@ -185,10 +186,14 @@ struct RowAcc<float, float, b> {
     }
 };
 
+// gate: null, or a flag in device memory; a nonzero flag makes the launch a no-op
+// (the BiCGStab iterations queued after the solver stopped)
 template <typename VT, typename XT, int b, int G>
 __global__ void __launch_bounds__(256) k_bsr_mv(int64_t nRows, const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx,
-                                                const VT* __restrict__ vals, const XT* __restrict__ x, XT* __restrict__ y) {
+                                                const VT* __restrict__ vals, const XT* __restrict__ x, XT* __restrict__ y,
+                                                const double* __restrict__ gate) {
     static_assert(G >= b, "a lane per row component");
+    if (gate && *gate != 0.0) return;
     const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t row = gid / G;
     const int lane = threadIdx.x % G;
@@ -238,7 +243,9 @@ template <typename VT, int K>
 struct DotArgs { const VT* a[K]; const VT* c[K]; };
 
 template <typename VT, int K>
-__global__ void __launch_bounds__(kRedThreads) k_dot_partial(int64_t n, DotArgs<VT, K> A, double* __restrict__ partials) {
+__global__ void __launch_bounds__(kRedThreads) k_dot_partial(int64_t n, DotArgs<VT, K> A, double* __restrict__ partials,
+                                                             const double* __restrict__ gate) {
+    if (gate && *gate != 0.0) return;
     __shared__ double sh[K][kRedThreads];
     double acc[K];
 #pragma unroll
@@ -290,7 +297,11 @@ __device__ __forceinline__ void block_sum_partials(const double* __restrict__ pa
 }
 
 // scalar slots of the BiCGStab state in ws.scal
-enum { S_RHO = 0, S_ALPHA, S_OMEGA, S_RHO1, S_BETA, S_R0V, S_TS, S_TT, S_NR2, S_NR02, S_FLAG, S_NSCAL = 16 };
+// S_DONE: 0 while iterating; set by the end-of-iteration kernel to 1 (converged), 2 (non-finite
+// residual) or 3 (breakdown: restart), after which every kernel of the iteration returns at once.
+// S_ITER counts the iterations run.
+enum { S_RHO = 0, S_ALPHA, S_OMEGA, S_RHO1, S_BETA, S_R0V, S_TS, S_TT, S_NR2, S_NR02, S_FLAG, S_DONE, S_ITER, S_NSCAL = 16 };
+enum { DONE_CONVERGED = 1, DONE_NONFINITE = 2, DONE_BREAKDOWN = 3 };
 
 template <int K>
 __global__ void k_dot_final(const double* partials, int nb, double* out) { block_sum_partials<K>(partials, nb, out); }
@@ -310,6 +321,7 @@ __global__ void k_bicg_beta(const double* partials, int nb, double* S) {
 }
 // alpha = rho1 / (r0, v); breakdown when (r0, v) = 0 or alpha is not finite
 __global__ void k_bicg_alpha(const double* partials, int nb, double* S) {
+    if (S[S_DONE] != 0.0) return;
     double v[1];
     block_sum_partials<1>(partials, nb, v);
     if (threadIdx.x == 0) {
@@ -321,6 +333,7 @@ __global__ void k_bicg_alpha(const double* partials, int nb, double* S) {
 }
 // omega = (t, s) / (t, t)
 __global__ void k_bicg_omega(const double* partials, int nb, double* S) {
+    if (S[S_DONE] != 0.0) return;
     double v[2];
     block_sum_partials<2>(partials, nb, v);
     if (threadIdx.x == 0) {
@@ -334,6 +347,113 @@ __global__ void k_bicg_rnorm(const double* partials, int nb, double* S) {
     double v[1];
     block_sum_partials<1>(partials, nb, v);
     if (threadIdx.x == 0) { S[S_NR2] = v[0]; S[S_RHO] = S[S_RHO1]; }
+}
+
+// ---- fused BiCGStab steps (FP64 Krylov vectors, Jacobian / inverse blocks of type MT) ----
+
+// sums the per-thread values v[k] of one block in a fixed tree into partials[k * gridDim.x + block]
+template <int K>
+__device__ __forceinline__ void block_partials(double (&v)[K], double* __restrict__ partials) {
+    __shared__ double sh[K][kRedThreads];
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[k][threadIdx.x] = v[k];
+    __syncthreads();
+    for (int st = kRedThreads / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) partials[k * gridDim.x + blockIdx.x] = sh[k][0];
+    }
+}
+
+// out = Dinv_row x (the point-block Jacobi apply of k_prec, same summation)
+template <typename MT, int b>
+__device__ __forceinline__ void prec_row(const MT* __restrict__ M, const double (&x)[b], double* __restrict__ out) {
+#pragma unroll
+    for (int i = 0; i < b; ++i) {
+        double a = 0.0;
+#pragma unroll
+        for (int j = 0; j < b; ++j) a += (double)M[i * b + j] * x[j];
+        out[i] = a;
+    }
+}
+
+// p = r + beta (p - omega v); ph = Dinv p
+template <typename MT, int b>
+__global__ void k_bicg_p_prec(int64_t nRows, const double* __restrict__ S, const double* __restrict__ r, const double* __restrict__ v,
+                              double* __restrict__ p, const MT* __restrict__ Dinv, double* __restrict__ ph) {
+    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= nRows || S[S_DONE] != 0.0) return;
+    const double beta = S[S_BETA], omega = S[S_OMEGA];
+    double x[b];
+#pragma unroll
+    for (int j = 0; j < b; ++j) {
+        const int64_t i = row * b + j;
+        x[j] = r[i] + beta * (p[i] - omega * v[i]);
+        p[i] = x[j];
+    }
+    prec_row<MT, b>(Dinv + row * b * b, x, ph + row * b);
+}
+
+// s = r - alpha v; sh = Dinv s
+template <typename MT, int b>
+__global__ void k_bicg_s_prec(int64_t nRows, const double* __restrict__ S, const double* __restrict__ r, const double* __restrict__ v,
+                              double* __restrict__ sv, const MT* __restrict__ Dinv, double* __restrict__ shv) {
+    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= nRows || S[S_DONE] != 0.0) return;
+    const double alpha = S[S_ALPHA];
+    double x[b];
+#pragma unroll
+    for (int j = 0; j < b; ++j) {
+        const int64_t i = row * b + j;
+        x[j] = r[i] - alpha * v[i];
+        sv[i] = x[j];
+    }
+    prec_row<MT, b>(Dinv + row * b * b, x, shv + row * b);
+}
+
+// x += alpha ph + omega sh; r = s - omega t; partials of (r, r) and (r0, r)
+// (the grid-stride layout of k_dot_partial, kRedBlocks blocks)
+__global__ void __launch_bounds__(kRedThreads) k_bicg_x_dots(int64_t n, const double* __restrict__ S, const double* __restrict__ ph,
+                                                              const double* __restrict__ shv, const double* __restrict__ sv,
+                                                              const double* __restrict__ t, const double* __restrict__ r0,
+                                                              double* __restrict__ x, double* __restrict__ r, double* __restrict__ partials) {
+    if (S[S_DONE] != 0.0) return;
+    const double alpha = S[S_ALPHA], omega = S[S_OMEGA];
+    double d[2] = {0.0, 0.0};
+    for (int64_t i = (int64_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRedThreads) {
+        x[i] += alpha * ph[i] + omega * shv[i];
+        const double ri = sv[i] - omega * t[i];
+        r[i] = ri;
+        d[0] += ri * ri;
+        d[1] += r0[i] * ri;
+    }
+    block_partials<2>(d, partials);
+}
+
+// end of an iteration: ||r||^2, the stop tests of the host loop (finite, converged,
+// breakdown), then the next iteration's rho1 = (r0, r) and beta (as k_bicg_beta)
+__global__ void k_bicg_end(const double* partials, int nb, double* S, double nr0, double rtol) {
+    if (S[S_DONE] != 0.0) return;
+    double v[2];
+    block_sum_partials<2>(partials, nb, v);
+    if (threadIdx.x != 0) return;
+    S[S_NR2] = v[0];
+    S[S_RHO] = S[S_RHO1];
+    S[S_ITER] += 1.0;
+    const double nr = sqrt(v[0]);
+    if (!isfinite(nr)) { S[S_DONE] = DONE_NONFINITE; return; }
+    if (nr / nr0 < rtol) { S[S_DONE] = DONE_CONVERGED; return; }
+    if (S[S_FLAG] != 0.0 || S[S_OMEGA] == 0.0) { S[S_DONE] = DONE_BREAKDOWN; return; }
+    S[S_RHO1] = v[1];
+    double beta = (v[1] / S[S_RHO]) * (S[S_ALPHA] / S[S_OMEGA]);
+    if (v[1] == 0.0 || !isfinite(beta)) { S[S_FLAG] = 1.0; beta = 0.0; }
+    S[S_BETA] = beta;
 }
 
 // p = r + beta (p - omega v)
@@ -460,15 +580,15 @@ static inline int grid_for(int64_t n, int t = 256) { return (int)((n + t - 1) / 
 template <int b> constexpr int spmv_lanes() { return b == 4 ? 8 : 4; }
 
 template <typename MT, typename VT>
-static cudaError_t spmv(const Disc& D, const MT* vals, const VT* x, VT* y, cudaStream_t s) {
+static cudaError_t spmv(const Disc& D, const MT* vals, const VT* x, VT* y, cudaStream_t s, const double* gate = nullptr) {
     const int64_t nR = D.nNodes;
     const int b = D.dim + 1;
     if (b == 4) {
         constexpr int G = spmv_lanes<4>();
-        k_bsr_mv<MT, VT, 4, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y);
+        k_bsr_mv<MT, VT, 4, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y, gate);
     } else {
         constexpr int G = spmv_lanes<3>();
-        k_bsr_mv<MT, VT, 3, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y);
+        k_bsr_mv<MT, VT, 3, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, vals, x, y, gate);
     }
     return cudaGetLastError();
 }
@@ -480,10 +600,11 @@ static void prec_apply(const Disc& D, const MT* Dinv, const VT* in, VT* out, cud
 }
 
 template <typename VT, int K>
-static void dots(int64_t n, const VT* const (&a)[K], const VT* const (&c)[K], double* partials, cudaStream_t s) {
+static void dots(int64_t n, const VT* const (&a)[K], const VT* const (&c)[K], double* partials, cudaStream_t s,
+                 const double* gate = nullptr) {
     DotArgs<VT, K> A;
     for (int k = 0; k < K; ++k) { A.a[k] = a[k]; A.c[k] = c[k]; }
-    k_dot_partial<VT, K><<<kRedBlocks, kRedThreads, 0, s>>>(n, A, partials);
+    k_dot_partial<VT, K><<<kRedBlocks, kRedThreads, 0, s>>>(n, A, partials, gate);
 }
 
 // ||x||_2^2 of an FP64 vector into out (device)
@@ -538,6 +659,31 @@ static bool read_scal(Disc& D, int first, int k, cudaStream_t s) {
 // BiCGStab on J x = rhs (right point-block-Jacobi preconditioning), x = 0 start.
 // Returns iterations, or -1 on breakdown / failure (D.status set on CUDA errors).
 static constexpr int kMaxBicgRestarts = 20;
+// Iterations queued between two host reads of the solver state: the stop tests
+// run on the device (k_bicg_end) and every kernel of a later iteration returns at
+// once, so the iterates are those of a test after every iteration.
+static constexpr int kBicgBatch = 16;
+
+template <typename MT, int b>
+static void bicg_iteration(Disc& D, const MT* J, const MT* Dinv, double* const (&V)[8], double* x, double nr0, double rtol, cudaStream_t s) {
+    Workspace& W = D.ws;
+    double *r = V[0], *r0 = V[1], *p = V[2], *v = V[3], *sv = V[4], *t = V[5], *ph = V[6], *shv = V[7];
+    double* S = W.scal;
+    const double* done = S + S_DONE;
+    const int64_t nR = D.nNodes, n = W.n;
+    const int gn = grid_for(nR);
+    k_bicg_p_prec<MT, b><<<gn, 256, 0, s>>>(nR, S, r, v, p, Dinv, ph);
+    spmv<MT, double>(D, J, ph, v, s, done);
+    { const double* a[1] = {r0}; const double* c[1] = {v}; dots<double, 1>(n, a, c, W.red, s, done); }
+    k_bicg_alpha<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
+    k_bicg_s_prec<MT, b><<<gn, 256, 0, s>>>(nR, S, r, v, sv, Dinv, shv);
+    spmv<MT, double>(D, J, shv, t, s, done);
+    { const double* a[2] = {t, t}; const double* c[2] = {sv, t}; dots<double, 2>(n, a, c, W.red, s, done); }
+    k_bicg_omega<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
+    k_bicg_x_dots<<<kRedBlocks, kRedThreads, 0, s>>>(W.n, S, ph, shv, sv, t, r0, x, r, W.red);
+    k_bicg_end<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S, nr0, rtol);
+}
+
 // The Krylov vectors are FP64 whatever the precision MT of the stored Jacobian:
 // an FP32 matrix then only perturbs the operator (relative 6e-8 per entry),
 // while FP32 vectors would let the recursive residual drift from the true one.
@@ -546,8 +692,9 @@ static int bicgstab(Disc& D, const MT* J, const MT* Dinv, const double* rhs, dou
     using VT = double;
     Workspace& W = D.ws;
     const int64_t n = W.n;
-    VT* V = (VT*)W.vec;
-    VT *r = V + 0 * n, *r0 = V + 1 * n, *p = V + 2 * n, *v = V + 3 * n, *sv = V + 4 * n, *t = V + 5 * n, *ph = V + 6 * n, *shv = V + 7 * n;
+    VT* Vb = (VT*)W.vec;
+    double* const V[8] = {Vb, Vb + n, Vb + 2 * n, Vb + 3 * n, Vb + 4 * n, Vb + 5 * n, Vb + 6 * n, Vb + 7 * n};
+    VT *r = V[0], *r0 = V[1], *p = V[2], *v = V[3];
     double* S = W.scal;
     const int g = grid_for(n);
     k_fill<VT><<<g, 256, 0, s>>>(n, x, VT(0));
@@ -568,42 +715,43 @@ static int bicgstab(Disc& D, const MT* J, const MT* Dinv, const double* rhs, dou
     const double nr0 = std::sqrt(W.hscal[S_NR02]);
     *relres = 1.0;
     if (nr0 == 0.0) return 0;
-    int restarts = 0;
-    for (int it = 1; it <= maxit; ++it) {
-        { const VT* a[1] = {r0}; const VT* c[1] = {r}; dots<VT, 1>(n, a, c, W.red, s); }
-        k_bicg_beta<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
-        k_bicg_p<VT><<<g, 256, 0, s>>>(n, S, r, v, p);
-        prec_apply<MT, VT>(D, Dinv, p, ph, s);
-        spmv<MT, VT>(D, J, ph, v, s);
-        { const VT* a[1] = {r0}; const VT* c[1] = {v}; dots<VT, 1>(n, a, c, W.red, s); }
-        k_bicg_alpha<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
-        k_bicg_s<VT><<<g, 256, 0, s>>>(n, S, r, v, sv);
-        prec_apply<MT, VT>(D, Dinv, sv, shv, s);
-        spmv<MT, VT>(D, J, shv, t, s);
-        { const VT* a[2] = {t, t}; const VT* c[2] = {sv, t}; dots<VT, 2>(n, a, c, W.red, s); }
-        k_bicg_omega<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
-        k_bicg_x<VT><<<g, 256, 0, s>>>(n, S, ph, shv, sv, t, x, r);
-        { const VT* a[1] = {r}; dots<VT, 1>(n, a, a, W.red, s); }
-        k_bicg_rnorm<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
+    const int b = D.dim + 1;
+    int restarts = 0, it = 0;
+    bool needBeta = true;   // rho1 and beta of the first iteration (later ones come from k_bicg_end)
+    while (it < maxit) {
+        const int K = std::min(kBicgBatch, maxit - it);
+        for (int j = 0; j < K; ++j) {
+            if (j == 0 && needBeta) {
+                const VT* a[1] = {r0}; const VT* c[1] = {r};
+                dots<VT, 1>(n, a, c, W.red, s);
+                k_bicg_beta<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
+            }
+            if (b == 4) bicg_iteration<MT, 4>(D, J, Dinv, V, x, nr0, rtol, s);
+            else bicg_iteration<MT, 3>(D, J, Dinv, V, x, nr0, rtol, s);
+        }
+        needBeta = false;
         if (!D.cuda_ok(cudaGetLastError(), "bicgstab launch")) return -1;
         if (!read_scal(D, 0, S_NSCAL, s)) return -1;
+        it = (int)W.hscal[S_ITER];
         const double nr = std::sqrt(W.hscal[S_NR2]);
         *relres = nr / nr0;
-        if (!std::isfinite(nr)) return -1;   // hard failure: x is not usable
-        if (*relres < rtol) return it;
-        // breakdown (rho1 = 0, (r0, v) = 0, a non-finite coefficient, omega = 0): restart
-        // with the current residual as the shadow vector; after too many restarts stop
-        // with the last finite iterate and let the Newton line search judge it
-        if (W.hscal[S_FLAG] != 0.0 || W.hscal[S_OMEGA] == 0.0) {
+        const int done = (int)W.hscal[S_DONE];
+        if (done == DONE_NONFINITE) return -1;   // hard failure: x is not usable
+        if (done == DONE_CONVERGED) return it;
+        if (done == DONE_BREAKDOWN) {
+            // breakdown (rho1 = 0, (r0, v) = 0, a non-finite coefficient, omega = 0): restart
+            // with the current residual as the shadow vector; after too many restarts stop
+            // with the last finite iterate and let the Newton line search judge it
             if (++restarts > kMaxBicgRestarts) return it;
             cudaMemcpyAsync(r0, r, n * sizeof(VT), cudaMemcpyDeviceToDevice, s);
             k_fill<VT><<<g, 256, 0, s>>>(n, p, VT(0));
             k_fill<VT><<<g, 256, 0, s>>>(n, v, VT(0));
             double re[S_NSCAL];
             std::memcpy(re, W.hscal, sizeof(re));
-            re[S_RHO] = 1.0; re[S_ALPHA] = 1.0; re[S_OMEGA] = 1.0; re[S_FLAG] = 0.0; re[S_NR02] = re[S_NR2];
+            re[S_RHO] = 1.0; re[S_ALPHA] = 1.0; re[S_OMEGA] = 1.0; re[S_FLAG] = 0.0; re[S_NR02] = re[S_NR2]; re[S_DONE] = 0.0;
             std::memcpy(W.hscal, re, sizeof(re));
             cudaMemcpyAsync(S, W.hscal, sizeof(re), cudaMemcpyHostToDevice, s);
+            needBeta = true;
         }
     }
     return maxit;
