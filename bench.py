@@ -372,6 +372,38 @@ def main():
     h2d = hu.numel() * 8
     d2h = (hD.numel() + hJ.numel()) * 8
 
+    # the same host-buffer steps back to back: step k's device-to-host copies (a copy stream)
+    # overlap step k+1's upload and assembly (two device buffer sets); every step still copies
+    # its state in and its defect and Jacobian out
+    ov_steps = max(2, args.steps // 2)
+    copy_stream = torch.cuda.Stream(device=dev)
+    bufs = [(torch.empty_like(tu), torch.empty_like(D), J64), (torch.empty_like(tu), torch.empty_like(D), torch.empty_like(J64))]
+    done_asm = [torch.cuda.Event() for _ in bufs]
+    done_copy = [torch.cuda.Event() for _ in bufs]
+    torch.cuda.synchronize()
+    flush.fill_(1.0)
+    torch.cuda.synchronize()
+    o0, o1 = ev(), ev()
+    o0.record(stream)
+    for k in range(ov_steps):
+        bu, bD, bJ = bufs[k % 2]
+        with torch.cuda.stream(stream):
+            if k >= 2:
+                stream.wait_event(done_copy[k % 2])
+            bu.copy_(hu, non_blocking=True)
+            d.assemble_defect_jacobian(bu, bD, bJ, stream=stream)
+            done_asm[k % 2].record(stream)
+        with torch.cuda.stream(copy_stream):
+            copy_stream.wait_event(done_asm[k % 2])
+            hD.copy_(bD, non_blocking=True)
+            hJ.copy_(bJ, non_blocking=True)
+            done_copy[k % 2].record(copy_stream)
+    stream.wait_stream(copy_stream)
+    o1.record(stream)
+    o1.synchronize()
+    e2e_ov_ms = o0.elapsed_time(o1) / ov_steps
+    del bufs
+
     # kernel launches of one step of each mode (counted by the profiler interface, after the timed region)
     launches64 = launches32 = {"ours": None, "skipped": True}
     if not args.no_launch_count:
@@ -447,7 +479,10 @@ def main():
                                                                        "traffic": traffic32,
                                                                        "traffic_source": prof.get("source_f32")}}}),
             "e2e": {"value": world * n_el / (e2e_ms * 1e-3), "unit": "elems/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                    "overlapped": {"value": world * n_el / (e2e_ov_ms * 1e-3), "ms_per_step": e2e_ov_ms, "steps": ov_steps,
+                                   "note": "consecutive host-buffer steps: step k's device-to-host copies overlap step k+1's "
+                                           "upload and assembly (copy stream, two device buffer sets)"}},
             "roofline": {"bound": "hbm", "kernel": "fused FP64 defect + Jacobian assembly (one launch per colour)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "traffic_source": prof.get("source_f64"),

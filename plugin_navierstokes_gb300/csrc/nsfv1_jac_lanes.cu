@@ -1,9 +1,9 @@
 // nsfv1_jac_lanes.cu -- the FP32 Jacobian assembly (the Newton loop's FP32-matrix
 // mode) with one lane group per element: one lane per corner of the element.
 //
-// The thread-per-element kernel k_jacobian<ROID, float, float> runs one colour of
-// a 64^3 hexahedral mesh as 1024 warps (6.7 per SM), latency-bound, and reduces
-// each SCVF's blocks straight into the matrix: three reductions per block and
+// With one thread per element (the structure of the FP64 k_jacobian) one colour
+// of a 64^3 hexahedral mesh is 1024 warps (6.7 per SM), latency-bound, and each
+// SCVF's blocks go straight into the matrix: three reductions per block and
 // element, spread over the whole kernel, so the colour's 134 MB of blocks cycle
 // through L2 three times. Here every element of a colour gets nsh lanes:
 //  1. lane k evaluates SCVFs k, k + nsh, ... (geometry, upwinds, stabilisation,
