@@ -268,6 +268,16 @@ int nsfv1_elem_batch_host(nsfv1_disc* h, int elem_type, int64_t n, const double*
 /* y = J x with J in the handle's block CSR (prec as above; x, y FP64) */
 int nsfv1_bsr_mv(nsfv1_disc* h, const void* vals, int prec, const double* x, double* y, void* stream);
 
+/* The FP64 vector x[n] as float pairs xs[2n] (xs[2i] the leading 24 bits of
+ * x[i], xs[2i+1] the next 24; device arrays), the operand of
+ * nsfv1_bsr_mv_split. */
+int nsfv1_split_vector(int64_t n, const double* x, float* xs, void* stream);
+/* y = J x for FP32 values and x given split by nsfv1_split_vector (xs 8-byte
+ * aligned): the result of nsfv1_bsr_mv with NSFV1_F32, bit for bit, without
+ * splitting x once per matrix block (the form the Newton loop's BiCGStab
+ * applies: its update kernels write the split of every vector they produce). */
+int nsfv1_bsr_mv_split(nsfv1_disc* h, const float* vals, const float* xs, double* y, void* stream);
+
 /* Point-block Jacobi preconditioner of a Jacobian on the handle's pattern
  * (the preconditioner of the Newton loop's linear solves): inverts every
  * b x b diagonal block of vals (prec NSFV1_F64 / NSFV1_F32) in FP64 into

@@ -125,6 +125,8 @@ _SIGS = {
     "nsfv1_export": (c_int, [c_void_p, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_double, c_int, c_int, c_void_p,
                              c_void_p, c_void_p, c_void_p]),
     "nsfv1_bsr_mv": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "nsfv1_split_vector": (c_int, [c_int64, c_void_p, c_void_p, c_void_p]),
+    "nsfv1_bsr_mv_split": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "nsfv1_block_jacobi": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "nsfv1_block_jacobi_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "nsfv1_newton_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(NewtonResult), c_void_p]),

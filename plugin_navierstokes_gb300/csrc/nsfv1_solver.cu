@@ -118,6 +118,19 @@ struct RowAcc<float, double, b> {
         float xh[b], xl[b];
 #pragma unroll
         for (int j = 0; j < b; ++j) split_double(__ldg(xc + j), xh[j], xl[j]);
+        accumulate(blk, xh, xl);
+    }
+    // x already split (split_double by the kernel that produced it): the same products
+    __device__ __forceinline__ void block(const float* __restrict__ blk, const float2* __restrict__ xc) {
+        float xh[b], xl[b];
+#pragma unroll
+        for (int j = 0; j < b; ++j) {
+            const float2 t = __ldg(xc + j);
+            xh[j] = t.x; xl[j] = t.y;
+        }
+        accumulate(blk, xh, xl);
+    }
+    __device__ __forceinline__ void accumulate(const float* __restrict__ blk, const float (&xh)[b], const float (&xl)[b]) {
 #pragma unroll
         for (int i = 0; i < b; ++i)
 #pragma unroll
@@ -207,6 +220,36 @@ __global__ void __launch_bounds__(256) k_bsr_mv(int64_t nRows, const int32_t* __
     acc.template reduce<G>();
     // lanes 0..b-1 of the group each store one component (G >= b)
     if (valid && lane < b) y[row * b + lane] = (XT)acc.value(lane);
+}
+
+// xs[i] = split_double(x[i]) (the SpMV operand of k_bsr_mv_split)
+__global__ void k_split_vector(int64_t n, const double* __restrict__ x, float2* __restrict__ xs) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float h, l;
+    split_double(x[i], h, l);
+    xs[i] = make_float2(h, l);
+}
+
+// k_bsr_mv for an FP32 matrix and an FP64 x stored as split float pairs (xs[i] =
+// split_double(x[i])): the FP64 result of k_bsr_mv<float, double>, bit for bit,
+// without the split per block
+template <int b, int G>
+__global__ void __launch_bounds__(256) k_bsr_mv_split(int64_t nRows, const int32_t* __restrict__ rowPtr, const int32_t* __restrict__ colIdx,
+                                                      const float* __restrict__ vals, const float2* __restrict__ xs, double* __restrict__ y,
+                                                      const double* __restrict__ gate) {
+    static_assert(G >= b, "a lane per row component");
+    if (gate && *gate != 0.0) return;
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t row = gid / G;
+    const int lane = threadIdx.x % G;
+    const bool valid = row < nRows;
+    const int q0 = valid ? rowPtr[row] : 0, q1 = valid ? rowPtr[row + 1] : 0;
+    RowAcc<float, double, b> acc;
+    acc.zero();
+    for (int q = q0 + lane; q < q1; q += G) acc.block(vals + (size_t)q * (b * b), xs + (size_t)__ldg(colIdx + q) * b);
+    acc.template reduce<G>();
+    if (valid && lane < b) y[row * b + lane] = acc.value(lane);
 }
 
 template <typename VT, typename OT, int b>
@@ -383,10 +426,28 @@ __device__ __forceinline__ void prec_row(const MT* __restrict__ M, const double 
     }
 }
 
+// the preconditioned vector of a row, and for FP32 matrices its split float pairs
+// (the SpMV's x operand, k_bsr_mv_split)
+template <typename MT, int b>
+__device__ __forceinline__ void prec_row_out(const MT* __restrict__ M, const double (&x)[b], double* __restrict__ out,
+                                             float2* __restrict__ outSplit) {
+    double z[b];
+    prec_row<MT, b>(M, x, z);
+#pragma unroll
+    for (int i = 0; i < b; ++i) {
+        out[i] = z[i];
+        if constexpr (std::is_same<MT, float>::value) {
+            float h, l;
+            split_double(z[i], h, l);
+            outSplit[i] = make_float2(h, l);
+        }
+    }
+}
+
 // p = r + beta (p - omega v); ph = Dinv p
 template <typename MT, int b>
 __global__ void k_bicg_p_prec(int64_t nRows, const double* __restrict__ S, const double* __restrict__ r, const double* __restrict__ v,
-                              double* __restrict__ p, const MT* __restrict__ Dinv, double* __restrict__ ph) {
+                              double* __restrict__ p, const MT* __restrict__ Dinv, double* __restrict__ ph, float2* __restrict__ phs) {
     const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= nRows || S[S_DONE] != 0.0) return;
     const double beta = S[S_BETA], omega = S[S_OMEGA];
@@ -397,13 +458,13 @@ __global__ void k_bicg_p_prec(int64_t nRows, const double* __restrict__ S, const
         x[j] = r[i] + beta * (p[i] - omega * v[i]);
         p[i] = x[j];
     }
-    prec_row<MT, b>(Dinv + row * b * b, x, ph + row * b);
+    prec_row_out<MT, b>(Dinv + row * b * b, x, ph + row * b, phs + row * b);
 }
 
 // s = r - alpha v; sh = Dinv s
 template <typename MT, int b>
 __global__ void k_bicg_s_prec(int64_t nRows, const double* __restrict__ S, const double* __restrict__ r, const double* __restrict__ v,
-                              double* __restrict__ sv, const MT* __restrict__ Dinv, double* __restrict__ shv) {
+                              double* __restrict__ sv, const MT* __restrict__ Dinv, double* __restrict__ shv, float2* __restrict__ shs) {
     const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= nRows || S[S_DONE] != 0.0) return;
     const double alpha = S[S_ALPHA];
@@ -414,7 +475,7 @@ __global__ void k_bicg_s_prec(int64_t nRows, const double* __restrict__ S, const
         x[j] = r[i] - alpha * v[i];
         sv[i] = x[j];
     }
-    prec_row<MT, b>(Dinv + row * b * b, x, shv + row * b);
+    prec_row_out<MT, b>(Dinv + row * b * b, x, shv + row * b, shs + row * b);
 }
 
 // x += alpha ph + omega sh; r = s - omega t; partials of (r, r) and (r0, r)
@@ -631,7 +692,7 @@ void Disc::free_workspace() {
 bool Disc::ensure_workspace(int prec, int gmresM) {
     const int b = dim + 1;
     const int64_t n = nNodes * b;
-    const int nvec = 9 + 2 * (gmresM + 1);
+    const int nvec = 10 + 2 * (gmresM + 1);   // BiCGStab: 10 work vectors, then the linear solve's rhs and solution
     if (ws.prec == prec && ws.n == n && ws.nvec >= nvec) return true;
     free_workspace();
     const size_t vt = prec == NSFV1_F64 ? sizeof(double) : sizeof(float);
@@ -665,19 +726,29 @@ static constexpr int kMaxBicgRestarts = 20;
 static constexpr int kBicgBatch = 16;
 
 template <typename MT, int b>
-static void bicg_iteration(Disc& D, const MT* J, const MT* Dinv, double* const (&V)[8], double* x, double nr0, double rtol, cudaStream_t s) {
+static void bicg_iteration(Disc& D, const MT* J, const MT* Dinv, double* const (&V)[10], double* x, double nr0, double rtol, cudaStream_t s) {
     Workspace& W = D.ws;
     double *r = V[0], *r0 = V[1], *p = V[2], *v = V[3], *sv = V[4], *t = V[5], *ph = V[6], *shv = V[7];
+    float2* phs = reinterpret_cast<float2*>(V[8]);   // split copies of ph and shv (FP32 matrices)
+    float2* shs = reinterpret_cast<float2*>(V[9]);
     double* S = W.scal;
     const double* done = S + S_DONE;
     const int64_t nR = D.nNodes, n = W.n;
     const int gn = grid_for(nR);
-    k_bicg_p_prec<MT, b><<<gn, 256, 0, s>>>(nR, S, r, v, p, Dinv, ph);
-    spmv<MT, double>(D, J, ph, v, s, done);
+    auto mv = [&](const double* xd, const float2* xsplit, double* y) {
+        if constexpr (std::is_same<MT, float>::value) {
+            constexpr int G = spmv_lanes<b>();
+            k_bsr_mv_split<b, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D.d_rowPtr, D.d_colIdx, J, xsplit, y, done);
+        } else {
+            spmv<MT, double>(D, J, xd, y, s, done);
+        }
+    };
+    k_bicg_p_prec<MT, b><<<gn, 256, 0, s>>>(nR, S, r, v, p, Dinv, ph, phs);
+    mv(ph, phs, v);
     { const double* a[1] = {r0}; const double* c[1] = {v}; dots<double, 1>(n, a, c, W.red, s, done); }
     k_bicg_alpha<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
-    k_bicg_s_prec<MT, b><<<gn, 256, 0, s>>>(nR, S, r, v, sv, Dinv, shv);
-    spmv<MT, double>(D, J, shv, t, s, done);
+    k_bicg_s_prec<MT, b><<<gn, 256, 0, s>>>(nR, S, r, v, sv, Dinv, shv, shs);
+    mv(shv, shs, t);
     { const double* a[2] = {t, t}; const double* c[2] = {sv, t}; dots<double, 2>(n, a, c, W.red, s, done); }
     k_bicg_omega<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
     k_bicg_x_dots<<<kRedBlocks, kRedThreads, 0, s>>>(W.n, S, ph, shv, sv, t, r0, x, r, W.red);
@@ -693,7 +764,7 @@ static int bicgstab(Disc& D, const MT* J, const MT* Dinv, const double* rhs, dou
     Workspace& W = D.ws;
     const int64_t n = W.n;
     VT* Vb = (VT*)W.vec;
-    double* const V[8] = {Vb, Vb + n, Vb + 2 * n, Vb + 3 * n, Vb + 4 * n, Vb + 5 * n, Vb + 6 * n, Vb + 7 * n};
+    double* const V[10] = {Vb, Vb + n, Vb + 2 * n, Vb + 3 * n, Vb + 4 * n, Vb + 5 * n, Vb + 6 * n, Vb + 7 * n, Vb + 8 * n, Vb + 9 * n};
     VT *r = V[0], *r0 = V[1], *p = V[2], *v = V[3];
     double* S = W.scal;
     const int g = grid_for(n);
@@ -973,6 +1044,33 @@ int nsfv1_bsr_mv(nsfv1_disc* h, const void* vals, int prec, const double* x, dou
         return D->status;
     }
     return D->cuda_ok(cudaGetLastError(), "bsr_mv") ? NSFV1_OK : D->status;
+}
+
+int nsfv1_split_vector(int64_t n, const double* x, float* xs, void* stream) {
+    if (n < 0 || (n > 0 && (!x || !xs))) return NSFV1_ERR_ARGUMENT;
+    if (n == 0) return NSFV1_OK;
+    k_split_vector<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(n, x, reinterpret_cast<float2*>(xs));
+    return cudaGetLastError() == cudaSuccess ? NSFV1_OK : NSFV1_ERR_CUDA;
+}
+
+int nsfv1_bsr_mv_split(nsfv1_disc* h, const float* vals, const float* xs, double* y, void* stream) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "bsr_mv_split: no mesh"); return D->status; }
+    if (!vals || !xs || !y) { D->fail(NSFV1_ERR_ARGUMENT, "bsr_mv_split: null pointer"); return D->status; }
+    if (reinterpret_cast<uintptr_t>(xs) & 7) { D->fail(NSFV1_ERR_ARGUMENT, "bsr_mv_split: xs must be 8-byte aligned"); return D->status; }
+    const int64_t nR = D->nNodes;
+    cudaStream_t s = (cudaStream_t)stream;
+    const float2* x2 = reinterpret_cast<const float2*>(xs);
+    if (D->dim == 3) {
+        constexpr int G = spmv_lanes<4>();
+        k_bsr_mv_split<4, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D->d_rowPtr, D->d_colIdx, vals, x2, y, nullptr);
+    } else {
+        constexpr int G = spmv_lanes<3>();
+        k_bsr_mv_split<3, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D->d_rowPtr, D->d_colIdx, vals, x2, y, nullptr);
+    }
+    return D->cuda_ok(cudaGetLastError(), "bsr_mv_split") ? NSFV1_OK : D->status;
 }
 
 int nsfv1_block_jacobi(nsfv1_disc* h, const void* vals, int prec, const double* r, double* z, void* stream) {

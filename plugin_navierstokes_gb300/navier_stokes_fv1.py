@@ -227,6 +227,21 @@ class NavierStokesFV1:
         prec = _capi.F64 if vals.dtype == torch.float64 else _capi.F32
         self._c(self._lib.nsfv1_bsr_mv(self._h, _ptr(vals), prec, _ptr(x), _ptr(y), _stream_ptr(stream)))
 
+    def split_vector(self, x, xs=None, stream=None):
+        """x (FP64, device) as float pairs (xs: float32 of twice the length), the operand of bsr_mv_split."""
+        import torch
+
+        if xs is None:
+            xs = torch.empty(2 * x.numel(), dtype=torch.float32, device=x.device)
+        st = self._lib.nsfv1_split_vector(int(x.numel()), _ptr(x), _ptr(xs), _stream_ptr(stream))
+        if st != 0:
+            raise _capi.NSFV1Error(st, "split_vector failed")
+        return xs
+
+    def bsr_mv_split(self, vals, xs, y, stream=None) -> None:
+        """y = J x for FP32 values and x split by split_vector (the BiCGStab loop's SpMV)."""
+        self._c(self._lib.nsfv1_bsr_mv_split(self._h, _ptr(vals), _ptr(xs), _ptr(y), _stream_ptr(stream)))
+
     def block_jacobi(self, vals, r, z, stream=None) -> None:
         """z = D^-1 r with D the block diagonal of the Jacobian vals."""
         import torch

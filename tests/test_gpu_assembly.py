@@ -230,6 +230,15 @@ def test_bsr_spmv_matches_oracle(cuda):
         d.bsr_mv(V, tx, ty)
         torch.cuda.synchronize()
         assert rel_err(ty.cpu().numpy(), y_ref) <= (TOL64 if dt_ == torch.float64 else TOL32)
+        if dt_ == torch.float32:
+            # the BiCGStab form: x split once into float pairs, the same product bit for bit
+            xs = d.split_vector(tx)
+            ys = torch.empty_like(tx)
+            d.bsr_mv_split(V, xs, ys)
+            torch.cuda.synchronize()
+            assert torch.equal(ys, ty)
+            h, l = xs.view(-1, 2)[:, 0].double(), xs.view(-1, 2)[:, 1].double()
+            assert float(((h + l - tx).abs() / tx.abs().clamp_min(1e-300)).max()) <= 2.0 ** -46
 
 
 def test_lps_no_cut_side_is_reported(cuda):
@@ -346,6 +355,13 @@ def test_fused_defect_jacobian_matches_oracle(cuda, gen, cfgi):
     torch.cuda.synchronize()
     assert rel_err(D32.cpu().numpy(), Dref) <= TOL64
     assert rel_err(J32.double().cpu().numpy(), Jref) <= TOL32
+    # with FP32 values the call is the FP64 defect and the FP32 Jacobian of the separate calls,
+    # bit for bit, and repeatable
+    Ds, J32s = torch.empty_like(D), torch.empty_like(J32)
+    d.assemble_defect(tu, Ds, tuo, dt)
+    d.assemble_jacobian(tu, J32s, tuo, dt)
+    torch.cuda.synchronize()
+    assert torch.equal(Ds, D32) and torch.equal(J32s, J32)
     # determinism of the fused pass
     D2, J2 = torch.empty_like(D), torch.empty_like(J)
     d.assemble_defect_jacobian(tu, D2, J2, tuo, dt)
