@@ -362,35 +362,6 @@ __global__ void k_bicg_beta(const double* partials, int nb, double* S) {
         S[S_BETA] = beta;
     }
 }
-// alpha = rho1 / (r0, v); breakdown when (r0, v) = 0 or alpha is not finite
-__global__ void k_bicg_alpha(const double* partials, int nb, double* S) {
-    if (S[S_DONE] != 0.0) return;
-    double v[1];
-    block_sum_partials<1>(partials, nb, v);
-    if (threadIdx.x == 0) {
-        S[S_R0V] = v[0];
-        double alpha = (v[0] != 0.0) ? S[S_RHO1] / v[0] : 0.0;
-        if (v[0] == 0.0 || !isfinite(alpha)) { S[S_FLAG] = 1.0; alpha = 0.0; }
-        S[S_ALPHA] = alpha;
-    }
-}
-// omega = (t, s) / (t, t)
-__global__ void k_bicg_omega(const double* partials, int nb, double* S) {
-    if (S[S_DONE] != 0.0) return;
-    double v[2];
-    block_sum_partials<2>(partials, nb, v);
-    if (threadIdx.x == 0) {
-        S[S_TS] = v[0]; S[S_TT] = v[1];
-        const double omega = (v[1] != 0.0) ? v[0] / v[1] : 0.0;
-        S[S_OMEGA] = isfinite(omega) ? omega : 0.0;
-    }
-}
-// ||r||^2 and rho <- rho1
-__global__ void k_bicg_rnorm(const double* partials, int nb, double* S) {
-    double v[1];
-    block_sum_partials<1>(partials, nb, v);
-    if (threadIdx.x == 0) { S[S_NR2] = v[0]; S[S_RHO] = S[S_RHO1]; }
-}
 
 // ---- fused BiCGStab steps (FP64 Krylov vectors, Jacobian / inverse blocks of type MT) ----
 
@@ -412,6 +383,46 @@ __device__ __forceinline__ void block_partials(double (&v)[K], double* __restric
 #pragma unroll
         for (int k = 0; k < K; ++k) partials[k * gridDim.x + blockIdx.x] = sh[k][0];
     }
+}
+
+// After block_partials<K>: the block that finishes last (counted in *counter)
+// sums the partials of all blocks, in block order (the sums of block_sum_partials),
+// into out (valid in thread 0) and returns true; the counter is left at 0.
+// Partials are read past L1 (other SMs wrote them).
+template <int K>
+__device__ __forceinline__ bool last_block_sum(const double* __restrict__ partials, unsigned* counter, double (&out)[K]) {
+    __shared__ bool amLast;
+    __shared__ double sh[K][kRedThreads];
+    if (threadIdx.x == 0) {
+        __threadfence();
+        amLast = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!amLast) return false;
+    __threadfence();
+    const int nb = gridDim.x;
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.0;
+    for (int i = threadIdx.x; i < nb; i += kRedThreads)
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[k] += __ldcg(partials + k * nb + i);
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int st = kRedThreads / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[k] = sh[k][0];
+        *counter = 0u;
+    }
+    return true;
 }
 
 // out = Dinv_row x (the point-block Jacobi apply of k_prec, same summation)
@@ -480,30 +491,51 @@ __global__ void k_bicg_s_prec(int64_t nRows, const double* __restrict__ S, const
 
 // x += alpha ph + omega sh; r = s - omega t; partials of (r, r) and (r0, r)
 // (the grid-stride layout of k_dot_partial, kRedBlocks blocks)
-__global__ void __launch_bounds__(kRedThreads) k_bicg_x_dots(int64_t n, const double* __restrict__ S, const double* __restrict__ ph,
-                                                              const double* __restrict__ shv, const double* __restrict__ sv,
-                                                              const double* __restrict__ t, const double* __restrict__ r0,
-                                                              double* __restrict__ x, double* __restrict__ r, double* __restrict__ partials) {
-    if (S[S_DONE] != 0.0) return;
-    const double alpha = S[S_ALPHA], omega = S[S_OMEGA];
-    double d[2] = {0.0, 0.0};
-    for (int64_t i = (int64_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRedThreads) {
-        x[i] += alpha * ph[i] + omega * shv[i];
-        const double ri = sv[i] - omega * t[i];
-        r[i] = ri;
-        d[0] += ri * ri;
-        d[1] += r0[i] * ri;
-    }
-    block_partials<2>(d, partials);
+
+// the scalar updates that follow the reductions (thread 0 of the last block)
+__device__ __forceinline__ void bicg_alpha_update(double* S, const double r0v) {
+    S[S_R0V] = r0v;
+    double alpha = (r0v != 0.0) ? S[S_RHO1] / r0v : 0.0;
+    if (r0v == 0.0 || !isfinite(alpha)) { S[S_FLAG] = 1.0; alpha = 0.0; }
+    S[S_ALPHA] = alpha;
+}
+__device__ __forceinline__ void bicg_omega_update(double* S, const double ts, const double tt) {
+    S[S_TS] = ts; S[S_TT] = tt;
+    const double omega = (tt != 0.0) ? ts / tt : 0.0;
+    S[S_OMEGA] = isfinite(omega) ? omega : 0.0;
 }
 
-// end of an iteration: ||r||^2, the stop tests of the host loop (finite, converged,
-// breakdown), then the next iteration's rho1 = (r0, r) and beta (as k_bicg_beta)
-__global__ void k_bicg_end(const double* partials, int nb, double* S, double nr0, double rtol) {
+// (r0, v) and alpha in one launch (k_dot_partial's grid and tree, then the last block)
+__global__ void __launch_bounds__(kRedThreads) k_bicg_dot_alpha(int64_t n, const double* __restrict__ r0, const double* __restrict__ v,
+                                                                 double* __restrict__ partials, unsigned* counter, double* S) {
     if (S[S_DONE] != 0.0) return;
-    double v[2];
-    block_sum_partials<2>(partials, nb, v);
-    if (threadIdx.x != 0) return;
+    double d[1] = {0.0};
+    for (int64_t i = (int64_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRedThreads)
+        d[0] += r0[i] * v[i];
+    block_partials<1>(d, partials);
+    double tot[1];
+    if (last_block_sum<1>(partials, counter, tot) && threadIdx.x == 0) bicg_alpha_update(S, tot[0]);
+}
+
+// (t, s), (t, t) and omega in one launch
+__global__ void __launch_bounds__(kRedThreads) k_bicg_dot_omega(int64_t n, const double* __restrict__ t, const double* __restrict__ sv,
+                                                                 double* __restrict__ partials, unsigned* counter, double* S) {
+    if (S[S_DONE] != 0.0) return;
+    double d[2] = {0.0, 0.0};
+    for (int64_t i = (int64_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRedThreads) {
+        const double ti = t[i];
+        d[0] += ti * sv[i];
+        d[1] += ti * ti;
+    }
+    block_partials<2>(d, partials);
+    double tot[2];
+    if (last_block_sum<2>(partials, counter, tot) && threadIdx.x == 0) bicg_omega_update(S, tot[0], tot[1]);
+}
+
+// end of an iteration (thread 0 of the last block of k_bicg_x_end): ||r||^2, the stop
+// tests of the host loop (finite, converged, breakdown), then the next iteration's
+// rho1 = (r0, r) and beta (as k_bicg_beta)
+__device__ __forceinline__ void bicg_end_update(double* S, const double (&v)[2], const double nr0, const double rtol) {
     S[S_NR2] = v[0];
     S[S_RHO] = S[S_RHO1];
     S[S_ITER] += 1.0;
@@ -517,30 +549,26 @@ __global__ void k_bicg_end(const double* partials, int nb, double* S, double nr0
     S[S_BETA] = beta;
 }
 
-// p = r + beta (p - omega v)
-template <typename VT>
-__global__ void k_bicg_p(int64_t n, const double* S, const VT* __restrict__ r, const VT* __restrict__ v, VT* __restrict__ p) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const VT beta = (VT)S[S_BETA], omega = (VT)S[S_OMEGA];
-    p[i] = r[i] + beta * (p[i] - omega * v[i]);
-}
-// s = r - alpha v
-template <typename VT>
-__global__ void k_bicg_s(int64_t n, const double* S, const VT* __restrict__ r, const VT* __restrict__ v, VT* __restrict__ s) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    s[i] = r[i] - (VT)S[S_ALPHA] * v[i];
-}
-// x += alpha ph + omega sh ; r = s - omega t
-template <typename VT>
-__global__ void k_bicg_x(int64_t n, const double* S, const VT* __restrict__ ph, const VT* __restrict__ sh, const VT* __restrict__ s,
-                         const VT* __restrict__ t, VT* __restrict__ x, VT* __restrict__ r) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const VT alpha = (VT)S[S_ALPHA], omega = (VT)S[S_OMEGA];
-    x[i] += alpha * ph[i] + omega * sh[i];
-    r[i] = s[i] - omega * t[i];
+// x += alpha ph + omega sh; r = s - omega t; (r, r) and (r0, r) (the grid-stride layout
+// of k_dot_partial, kRedBlocks blocks); the last block ends the iteration
+__global__ void __launch_bounds__(kRedThreads) k_bicg_x_end(int64_t n, double* S, const double* __restrict__ ph,
+                                                             const double* __restrict__ shv, const double* __restrict__ sv,
+                                                             const double* __restrict__ t, const double* __restrict__ r0,
+                                                             double* __restrict__ x, double* __restrict__ r, double* __restrict__ partials,
+                                                             unsigned* counter, double nr0, double rtol) {
+    if (S[S_DONE] != 0.0) return;
+    const double alpha = S[S_ALPHA], omega = S[S_OMEGA];
+    double d[2] = {0.0, 0.0};
+    for (int64_t i = (int64_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kRedThreads) {
+        x[i] += alpha * ph[i] + omega * shv[i];
+        const double ri = sv[i] - omega * t[i];
+        r[i] = ri;
+        d[0] += ri * ri;
+        d[1] += r0[i] * ri;
+    }
+    block_partials<2>(d, partials);
+    double tot[2];
+    if (last_block_sum<2>(partials, counter, tot) && threadIdx.x == 0) bicg_end_update(S, tot, nr0, rtol);
 }
 
 template <typename A, typename B>
@@ -721,9 +749,12 @@ static bool read_scal(Disc& D, int first, int k, cudaStream_t s) {
 // Returns iterations, or -1 on breakdown / failure (D.status set on CUDA errors).
 static constexpr int kMaxBicgRestarts = 20;
 // Iterations queued between two host reads of the solver state: the stop tests
-// run on the device (k_bicg_end) and every kernel of a later iteration returns at
+// run on the device (k_bicg_x_end) and every kernel of a later iteration returns at
 // once, so the iterates are those of a test after every iteration.
 static constexpr int kBicgBatch = 16;
+
+// the last-block counters of the BiCGStab reductions (unsigned, in the scalar buffer)
+static unsigned* bicg_counters(Workspace& W) { return reinterpret_cast<unsigned*>(W.scal + 200); }
 
 template <typename MT, int b>
 static void bicg_iteration(Disc& D, const MT* J, const MT* Dinv, double* const (&V)[10], double* x, double nr0, double rtol, cudaStream_t s) {
@@ -743,16 +774,14 @@ static void bicg_iteration(Disc& D, const MT* J, const MT* Dinv, double* const (
             spmv<MT, double>(D, J, xd, y, s, done);
         }
     };
+    unsigned* counters = bicg_counters(W);
     k_bicg_p_prec<MT, b><<<gn, 256, 0, s>>>(nR, S, r, v, p, Dinv, ph, phs);
     mv(ph, phs, v);
-    { const double* a[1] = {r0}; const double* c[1] = {v}; dots<double, 1>(n, a, c, W.red, s, done); }
-    k_bicg_alpha<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
+    k_bicg_dot_alpha<<<kRedBlocks, kRedThreads, 0, s>>>(n, r0, v, W.red, counters + 0, S);
     k_bicg_s_prec<MT, b><<<gn, 256, 0, s>>>(nR, S, r, v, sv, Dinv, shv, shs);
     mv(shv, shs, t);
-    { const double* a[2] = {t, t}; const double* c[2] = {sv, t}; dots<double, 2>(n, a, c, W.red, s, done); }
-    k_bicg_omega<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S);
-    k_bicg_x_dots<<<kRedBlocks, kRedThreads, 0, s>>>(W.n, S, ph, shv, sv, t, r0, x, r, W.red);
-    k_bicg_end<<<1, kRedThreads, 0, s>>>(W.red, kRedBlocks, S, nr0, rtol);
+    k_bicg_dot_omega<<<kRedBlocks, kRedThreads, 0, s>>>(n, t, sv, W.red, counters + 1, S);
+    k_bicg_x_end<<<kRedBlocks, kRedThreads, 0, s>>>(n, S, ph, shv, sv, t, r0, x, r, W.red, counters + 2, nr0, rtol);
 }
 
 // The Krylov vectors are FP64 whatever the precision MT of the stored Jacobian:
@@ -777,6 +806,7 @@ static int bicgstab(Disc& D, const MT* J, const MT* Dinv, const double* rhs, dou
     init[S_RHO] = 1.0; init[S_ALPHA] = 1.0; init[S_OMEGA] = 1.0;
     std::memcpy(W.hscal, init, sizeof(init));
     cudaMemcpyAsync(S, W.hscal, sizeof(init), cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(bicg_counters(W), 0, 4 * sizeof(unsigned), s);
     {
         const VT* a[1] = {r};
         dots<VT, 1>(n, a, a, W.red, s);
@@ -788,7 +818,7 @@ static int bicgstab(Disc& D, const MT* J, const MT* Dinv, const double* rhs, dou
     if (nr0 == 0.0) return 0;
     const int b = D.dim + 1;
     int restarts = 0, it = 0;
-    bool needBeta = true;   // rho1 and beta of the first iteration (later ones come from k_bicg_end)
+    bool needBeta = true;   // rho1 and beta of the first iteration (later ones come from k_bicg_x_end)
     while (it < maxit) {
         const int K = std::min(kBicgBatch, maxit - it);
         for (int j = 0; j < K; ++j) {
