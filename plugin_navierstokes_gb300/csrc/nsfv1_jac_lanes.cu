@@ -35,8 +35,20 @@ struct Lanes {
     static constexpr int EPC = WARPS * EPW;                 // elements per CTA
 };
 
-// floats per corner in the gather stage: coordinates (3), state (4), old state (4, PAC only)
-template <bool PAC> __host__ __device__ constexpr int corner_floats() { return PAC ? 12 : 8; }
+// Shared memory of one CTA (dynamic): the SCVF factor slots, then per element its
+// geometry (Elem, filled by the group) and states, then the reference tables.
+template <int ROID, bool PAC>
+struct LaneSmem {
+    using R = Ref<ROID>;
+    using C = Lanes<ROID>;
+    static constexpr size_t slots = sizeof(float) * C::EPC * R::nip * C::FS;
+    static constexpr size_t elemBytes = (sizeof(Elem<ROID, float>) + 15) / 16 * 16;
+    static constexpr size_t elems = elemBytes * C::EPC;
+    static constexpr size_t uFloats = R::b * R::nsh + (PAC ? R::dim * R::nsh : 0);   // u [b][nsh], then uo [dim][nsh]
+    static constexpr size_t us = (sizeof(float) * uFloats * C::EPC + 15) / 16 * 16;
+    static constexpr size_t tab = sizeof(float4) * R::nip * R::nsh;
+    static constexpr size_t bytes = slots + elems + us + tab;
+};
 
 // slot layout: the scalar factors of JacIp, then its per-corner shapes
 enum : int {
@@ -123,10 +135,12 @@ __global__ void __launch_bounds__(Lanes<ROID>::THREADS, 3) k_jacobian_lanes(cons
     using C = Lanes<ROID>;
     constexpr int dim = R::dim, nsh = R::nsh, nip = R::nip, b = R::b;
     constexpr int L = C::L, EPW = C::EPW, FS = C::FS;
-    constexpr int CF = corner_floats<PAC>();
-    __shared__ __align__(16) float sSlots[C::EPC * nip * FS];
-    __shared__ __align__(16) float sCor[C::EPC * nsh * CF];   // the element's corners, converted once
-    __shared__ float4 sTab[nip * nsh];   // (reference gradient, value) of shape k at SCVF ip
+    using M = LaneSmem<ROID, PAC>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* sSlots = reinterpret_cast<float*>(smem);
+    unsigned char* sElems = smem + M::slots;
+    float* sU = reinterpret_cast<float*>(smem + M::slots + M::elems);
+    float4* sTab = reinterpret_cast<float4*>(smem + M::slots + M::elems + M::us);   // (reference gradient, value) of shape k at SCVF ip
     {
         const auto& tb = tab<ROID, float>();
         for (int j = threadIdx.x; j < nip * nsh; j += blockDim.x) {
@@ -155,49 +169,31 @@ __global__ void __launch_bounds__(Lanes<ROID>::THREADS, 3) k_jacobian_lanes(cons
     if (!__all_sync(mask, inRange)) return;
 #endif
     const bool withOld = PAC && P.transient && P.pac && P.fullNewton != 0.0;
-    float* myCor = sCor + (warp * EPW + grp) * nsh * CF;
+    const int slot = warp * EPW + grp;
+    Elem<ROID, float>& E = *reinterpret_cast<Elem<ROID, float>*>(sElems + slot * M::elemBytes);
+    float (&u)[b][nsh] = *reinterpret_cast<float(*)[b][nsh]>(sU + slot * M::uFloats);
+    // the old state (PAC with the exact-Jacobian terms only; otherwise any array, unread)
+    float (&uo)[dim][nsh] = *reinterpret_cast<float(*)[dim][nsh]>(sU + slot * M::uFloats + (PAC ? b * nsh : 0));
     {
-        float* dst = myCor + k * CF;
 #pragma unroll
         for (int d = 0; d < dim; ++d)
-            dst[d] = (float)(__ldg(A.coords + (int64_t)nodek * dim + d) - __ldg(A.coords + (int64_t)node0 * dim + d));
+            E.x[k][d] = (float)(__ldg(A.coords + (int64_t)nodek * dim + d) - __ldg(A.coords + (int64_t)node0 * dim + d));
 #pragma unroll
-        for (int f = 0; f < b; ++f) dst[3 + f] = (float)__ldg(A.U + (int64_t)nodek * b + f);
+        for (int f = 0; f < b; ++f) u[f][k] = (float)__ldg(A.U + (int64_t)nodek * b + f);
         if constexpr (PAC) {
 #pragma unroll
-            for (int f = 0; f < dim; ++f) dst[7 + f] = withOld ? (float)__ldg(A.Uold + (int64_t)nodek * b + f) : 0.f;
+            for (int f = 0; f < dim; ++f) uo[f][k] = withOld ? (float)__ldg(A.Uold + (int64_t)nodek * b + f) : 0.f;
         }
     }
     __syncwarp(mask);
-    float* mySlots = sSlots + (warp * EPW + grp) * nip * FS;
-    float volk = 0.f;
+    // the element geometry once per group, in shared memory (read by every lane's SCVFs)
+    if (k == 0) elem_setup<ROID, float>(E);
+    __syncwarp(mask);
+    float* mySlots = sSlots + slot * nip * FS;
+    const float volk = E.vol[k];
     bool ok = true;
     {
         // ---- phase 1: the factors of SCVFs k, k + nsh, ...
-        Elem<ROID, float> E;
-        float u[b][nsh];
-        float uo[dim][nsh];
-#pragma unroll
-        for (int c = 0; c < nsh; ++c) {
-            const float4 a = *reinterpret_cast<const float4*>(myCor + c * CF);
-            const float4 v = *reinterpret_cast<const float4*>(myCor + c * CF + 4);
-            E.x[c][0] = a.x; E.x[c][1] = a.y;
-            if constexpr (dim == 3) E.x[c][2] = a.z;
-            u[0][c] = a.w; u[1][c] = v.x; u[2][c] = v.y;
-            if constexpr (b == 4) u[3][c] = v.z;
-            if constexpr (PAC) {
-                const float4 o = *reinterpret_cast<const float4*>(myCor + c * CF + 8);
-                // the stored old state starts at float 7: v.w, then o.x, o.y
-                uo[0][c] = v.w; uo[1][c] = o.x;
-                if constexpr (dim == 3) uo[2][c] = o.y;
-            } else {
-#pragma unroll
-                for (int d = 0; d < dim; ++d) uo[d][c] = 0.f;
-            }
-        }
-        elem_setup<ROID, float>(E);
-#pragma unroll
-        for (int c = 0; c < nsh; ++c) volk = (c == k) ? E.vol[c] : volk;
         float corMinN = 0.f, corMinD = 0.f, corAvgN = 1.f;
         if (P.stab != STAB_WITHOUT && P.diffLen == DL_COR) cor_data<ROID, float>(E, corMinN, corMinD, corAvgN);
 #pragma unroll 1
@@ -297,10 +293,19 @@ cudaError_t launch_jacobian_lanes(int roid, const DiscParams& P, const AsmArgs& 
         using C = Lanes<RO>;
         const int grid = (a.count + C::EPC - 1) / C::EPC;
         const int spec = lanes_spec(P);
-        if (P.pac && !P.stokes) k_jacobian_lanes<RO, true, SPEC_GENERIC><<<grid, C::THREADS, 0, s>>>(P, a);
-        else if (spec == SPEC_FLOW) k_jacobian_lanes<RO, false, SPEC_FLOW><<<grid, C::THREADS, 0, s>>>(P, a);
-        else if (spec == SPEC_FIELDS) k_jacobian_lanes<RO, false, SPEC_FIELDS><<<grid, C::THREADS, 0, s>>>(P, a);
-        else k_jacobian_lanes<RO, false, SPEC_GENERIC><<<grid, C::THREADS, 0, s>>>(P, a);
+        auto go = [&](auto kern, size_t bytes) {
+            // dynamic shared memory above 48 KB needs the per-kernel opt-in (set once)
+            static bool attr = false;
+            if (!attr && bytes > 48 * 1024) {
+                if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) return;
+                attr = true;
+            }
+            kern<<<grid, C::THREADS, bytes, s>>>(P, a);
+        };
+        if (P.pac && !P.stokes) go(k_jacobian_lanes<RO, true, SPEC_GENERIC>, LaneSmem<RO, true>::bytes);
+        else if (spec == SPEC_FLOW) go(k_jacobian_lanes<RO, false, SPEC_FLOW>, LaneSmem<RO, false>::bytes);
+        else if (spec == SPEC_FIELDS) go(k_jacobian_lanes<RO, false, SPEC_FIELDS>, LaneSmem<RO, false>::bytes);
+        else go(k_jacobian_lanes<RO, false, SPEC_GENERIC>, LaneSmem<RO, false>::bytes);
     });
 }
 
