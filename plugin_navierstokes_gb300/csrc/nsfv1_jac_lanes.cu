@@ -6,6 +6,8 @@
 // SCVF's blocks go straight into the matrix: three reductions per block and
 // element, spread over the whole kernel, so the colour's 134 MB of blocks cycle
 // through L2 three times. Here every element of a colour gets nsh lanes:
+//  0. lane k converts corner k (coordinates, state) into the element's shared-
+//     memory record, and one lane computes the element geometry there;
 //  1. lane k evaluates SCVFs k, k + nsh, ... (geometry, upwinds, stabilisation,
 //     the per-SCVF factors of add_jac_A_elem, navier_stokes_fv1.cpp:250-595) and
 //     leaves the factors in shared memory;
