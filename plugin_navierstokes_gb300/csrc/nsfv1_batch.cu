@@ -471,15 +471,24 @@ __global__ void __launch_bounds__(kGT) k_gmres_batch(const GmresBatchArgs<VT> A)
                         }
                         cluster_sum(j + 1);
                         if (tid <= j) hcol[tid] += sum[tid];
+                        // the second pass also sums ||w||^2 of the result (norm2's order: each
+                        // thread its own entries in turn, then the cluster sum)
+                        VT nacc = VT(0);
 #pragma unroll 2
                         for (int64_t e = ctid; e < n; e += cth) {
                             VT a = w[e];
                             for (int k = 0; k <= j; ++k) a -= (VT)sum[k] * Vk(k)[e];
                             w[e] = a;
+                            if (pass == 1) nacc += a * a;
                         }
-                        cl.sync();
+                        if (pass == 0) {
+                            cl.sync();
+                        } else {
+                            ClusterRed::block_part((double)nacc, 0, wred);
+                            cluster_sum(1);
+                        }
                     }
-                    const double hn = sqrt(norm2(w));
+                    const double hn = sqrt(sum[0]);
                     if (hn > 0.0) {
                         const VT ih = (VT)(1.0 / hn);
                         for (int64_t e = ctid; e < n; e += cth) w[e] *= ih;
