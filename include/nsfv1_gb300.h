@@ -335,6 +335,20 @@ typedef struct {
 int nsfv1_newton_solve(nsfv1_disc* h, double* u, const double* u_old, double dt, const nsfv1_newton_params* p,
                        nsfv1_newton_result* r, void* stream);
 
+/* The Newton loop's linear solver on a given system (the core's linear solver
+ * applied to an assembled Jacobian): J x = rhs on the handle's pattern, J =
+ * vals of precision p->jacobian_prec, rhs and x FP64 device vectors, x = 0
+ * start; point-block-Jacobi right-preconditioned BiCGStab or GMRES(m)
+ * (p->linear_solver, p->gmres_restart) to p->lin_rtol relative residual in at
+ * most p->lin_max_iter iterations. Out (host, each may be NULL): iterations,
+ * the final relative residual and the BiCGStab restarts (a zero (r0, v) or
+ * rho, a zero omega or a non-finite coefficient makes the current residual the
+ * new shadow vector; after 20 restarts the solve stops with the last iterate).
+ * NSFV1_ERR_BREAKDOWN: a singular diagonal block or a non-finite residual;
+ * NSFV1_ERR_NOT_CONVERGED: the tolerance was not reached. */
+int nsfv1_linear_solve(nsfv1_disc* h, const void* vals, const double* rhs, double* x, const nsfv1_newton_params* p, int* iterations,
+                       double* relres, int* restarts, void* stream);
+
 /* ---- many independent instances (batched cavities) ------------------------ */
 
 /* Per-element kinematic viscosity (host array [n_elems]), replacing the

@@ -130,6 +130,8 @@ _SIGS = {
     "nsfv1_block_jacobi": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "nsfv1_block_jacobi_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "nsfv1_newton_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, POINTER(NewtonParams), POINTER(NewtonResult), c_void_p]),
+    "nsfv1_linear_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, POINTER(NewtonParams), POINTER(c_int), POINTER(c_double),
+                                   POINTER(c_int), c_void_p]),
     "nsfv1_set_elem_viscosity": (c_int, [c_void_p, c_void_p]),
     "nsfv1_set_instances": (c_int, [c_void_p, c_int, c_void_p]),
     "nsfv1_set_instance_grids": (c_int, [c_void_p, c_void_p]),

@@ -788,7 +788,8 @@ static void bicg_iteration(Disc& D, const MT* J, const MT* Dinv, double* const (
 // an FP32 matrix then only perturbs the operator (relative 6e-8 per entry),
 // while FP32 vectors would let the recursive residual drift from the true one.
 template <typename MT>
-static int bicgstab(Disc& D, const MT* J, const MT* Dinv, const double* rhs, double* x, double rtol, int maxit, double* relres, cudaStream_t s) {
+static int bicgstab(Disc& D, const MT* J, const MT* Dinv, const double* rhs, double* x, double rtol, int maxit, double* relres, cudaStream_t s,
+                    int* restartsOut = nullptr) {
     using VT = double;
     Workspace& W = D.ws;
     const int64_t n = W.n;
@@ -818,6 +819,10 @@ static int bicgstab(Disc& D, const MT* J, const MT* Dinv, const double* rhs, dou
     if (nr0 == 0.0) return 0;
     const int b = D.dim + 1;
     int restarts = 0, it = 0;
+    struct Report {
+        int& n; int* out;
+        ~Report() { if (out) *out = n; }
+    } report{restarts, restartsOut};
     bool needBeta = true;   // rho1 and beta of the first iteration (later ones come from k_bicg_x_end)
     while (it < maxit) {
         const int K = std::min(kBicgBatch, maxit - it);
@@ -1024,6 +1029,47 @@ static int newton_impl(Disc& D, double* u, const double* u_old, double dt, const
     return status;
 }
 
+// J x = rhs on the handle's pattern with the Newton loop's linear solver (x = 0 start)
+template <typename MT>
+static int linear_solve_impl(Disc& D, const MT* J, const double* rhs, double* x, const nsfv1_newton_params& p, int* iterations,
+                             double* relres, int* restarts, cudaStream_t s) {
+    const int prec = std::is_same<MT, double>::value ? NSFV1_F64 : NSFV1_F32;
+    const int m = std::min(std::max(p.gmres_restart, 1), 64);
+    if (!D.ensure_workspace(prec, p.linear_solver == NSFV1_GMRES ? m : 0)) return D.status;
+    Workspace& W = D.ws;
+    MT* Dinv = (MT*)W.Dinv;
+    const int b = D.dim + 1;
+    cudaMemsetAsync(D.d_err, 0, sizeof(int), s);
+    if (b == 4) k_block_inv<MT, MT, 4><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, J, Dinv, D.d_err);
+    else k_block_inv<MT, MT, 3><<<grid_for(D.nNodes, 128), 128, 0, s>>>(D.nNodes, D.d_diagPos, J, Dinv, D.d_err);
+    int herr = 0;
+    cudaMemcpyAsync(&herr, D.d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (!D.cuda_ok(cudaStreamSynchronize(s), "linear solve")) return D.status;
+    if (herr & 2) {
+        cudaMemsetAsync(D.d_err, 0, sizeof(int), s);
+        D.fail(NSFV1_ERR_BREAKDOWN, "singular diagonal block");
+        return D.status;
+    }
+    double rr = 0.0;
+    int rs = 0;
+    const int li = p.linear_solver == NSFV1_GMRES ? gmres<MT>(D, J, Dinv, rhs, x, p.lin_rtol, p.lin_max_iter, m, &rr, s)
+                                                  : bicgstab<MT>(D, J, Dinv, rhs, x, p.lin_rtol, p.lin_max_iter, &rr, s, &rs);
+    if (D.status == NSFV1_ERR_CUDA) return D.status;
+    if (!D.cuda_ok(cudaStreamSynchronize(s), "linear solve")) return D.status;
+    if (iterations) *iterations = li < 0 ? 0 : li;
+    if (relres) *relres = rr;
+    if (restarts) *restarts = rs;
+    if (li < 0) {
+        D.fail(NSFV1_ERR_BREAKDOWN, "linear solver: non-finite residual");
+        return D.status;
+    }
+    if (!(rr < p.lin_rtol)) {
+        D.fail(NSFV1_ERR_NOT_CONVERGED, "linear solver did not reach the tolerance");
+        return D.status;
+    }
+    return NSFV1_OK;
+}
+
 }  // namespace
 
 namespace nsfv1 {
@@ -1101,6 +1147,21 @@ int nsfv1_bsr_mv_split(nsfv1_disc* h, const float* vals, const float* xs, double
         k_bsr_mv_split<3, G><<<grid_for(nR * G), 256, 0, s>>>(nR, D->d_rowPtr, D->d_colIdx, vals, x2, y, nullptr);
     }
     return D->cuda_ok(cudaGetLastError(), "bsr_mv_split") ? NSFV1_OK : D->status;
+}
+
+int nsfv1_linear_solve(nsfv1_disc* h, const void* vals, const double* rhs, double* x, const nsfv1_newton_params* p, int* iterations,
+                       double* relres, int* restarts, void* stream) {
+    Disc* D = reinterpret_cast<Disc*>(h);
+    if (!D) return NSFV1_ERR_ARGUMENT;
+    D->status = NSFV1_OK;
+    if (!D->hasMesh) { D->fail(NSFV1_ERR_STATE, "linear_solve: no mesh"); return D->status; }
+    if (!vals || !rhs || !x || !p) { D->fail(NSFV1_ERR_ARGUMENT, "linear_solve: null pointer"); return D->status; }
+    if (p->lin_max_iter < 1 || !(p->lin_rtol > 0.0)) { D->fail(NSFV1_ERR_ARGUMENT, "linear_solve: lin_max_iter >= 1 and lin_rtol > 0"); return D->status; }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (p->jacobian_prec == NSFV1_F64) return linear_solve_impl<double>(*D, (const double*)vals, rhs, x, *p, iterations, relres, restarts, s);
+    if (p->jacobian_prec == NSFV1_F32) return linear_solve_impl<float>(*D, (const float*)vals, rhs, x, *p, iterations, relres, restarts, s);
+    D->fail(NSFV1_ERR_ARGUMENT, "linear_solve: jacobian_prec must be NSFV1_F64 or NSFV1_F32");
+    return D->status;
 }
 
 int nsfv1_block_jacobi(nsfv1_disc* h, const void* vals, int prec, const double* r, double* z, void* stream) {

@@ -264,6 +264,23 @@ class NavierStokesFV1:
             raise NSFV1Error(st, self._lib.nsfv1_last_error(self._h).decode() + f" {res}")
         return res
 
+    def linear_solve(self, vals, rhs, x, lin_rtol: float = 1e-4, lin_max_iter: int = 2000, linear_solver: str = "bicgstab",
+                     gmres_restart: int = 30, stream=None, raise_on_error: bool = True) -> dict:
+        """J x = rhs with the Newton loop's linear solver (nsfv1_linear_solve); the
+        precision of J follows vals' dtype. Returns status, iterations, relres, restarts."""
+        import torch
+
+        p = _capi.NewtonParams(0.0, 0.0, 1, lin_rtol, lin_max_iter, 0,
+                               _capi.F64 if vals.dtype == torch.float64 else _capi.F32,
+                               _capi.GMRES if linear_solver == "gmres" else _capi.BICGSTAB, gmres_restart)
+        it, rr, rs = ctypes.c_int(0), ctypes.c_double(0.0), ctypes.c_int(0)
+        st = self._lib.nsfv1_linear_solve(self._h, _ptr(vals), _ptr(rhs), _ptr(x), ctypes.byref(p), ctypes.byref(it),
+                                          ctypes.byref(rr), ctypes.byref(rs), _stream_ptr(stream))
+        res = {"status": st, "iterations": it.value, "relres": rr.value, "restarts": rs.value}
+        if st != _capi.OK and raise_on_error:
+            raise NSFV1Error(st, self._lib.nsfv1_last_error(self._h).decode() + f" {res}")
+        return res
+
     def set_elem_viscosity(self, nu) -> None:
         """Per-element kinematic viscosity (None: back to the constant)."""
         if nu is None:

@@ -123,3 +123,49 @@ def test_nonfinite_state_is_reported_and_the_handle_recovers(cuda):
     u.zero_()
     r = d.newton_solve(u, rtol=1e-8, lin_rtol=1e-3, raise_on_error=False)
     assert r["status"] == 0, r
+
+
+@pytest.mark.parametrize("jdtype", ["f64", "f32"])
+def test_bicgstab_breakdown_restarts_and_is_reported(cuda, jdtype):
+    """A planted system on which BiCGStab breaks down at every start: identity
+    diagonal blocks, the block (node 0, node 1) = -2 I, rhs = 1 on nodes 0 and 1.
+    With r0 = rhs, v = J r0 is -1 on node 0 and +1 on node 1, so (r0, v) = 0:
+    alpha breaks down, omega = (t, s) / (t, t) = 0, the residual does not move
+    and every restart (shadow vector := residual) meets the same zero. The solve
+    stops after 20 restarts with NSFV1_ERR_NOT_CONVERGED and x = 0; the handle
+    then solves a well-posed system with the same pattern."""
+    import torch
+    d, roid, X, C = _quads_disc(2)
+    rp, ci = d.pattern()
+    b = 3
+    dt_ = torch.float64 if jdtype == "f64" else torch.float32
+    V = np.zeros((ci.size, b, b))
+    for r in range(X.shape[0]):
+        for q in range(rp[r], rp[r + 1]):
+            if ci[q] == r:
+                V[q] = np.eye(b)
+    q01 = [q for q in range(rp[0], rp[1]) if ci[q] == 1]
+    assert len(q01) == 1
+    V[q01[0]] = -2.0 * np.eye(b)
+    vals = torch.tensor(V.ravel(), dtype=dt_, device=cuda)
+    rhs = torch.zeros(X.shape[0] * b, dtype=torch.float64, device=cuda)
+    rhs[0:2 * b] = 1.0
+    x = torch.full_like(rhs, float("nan"))
+    res = d.linear_solve(vals, rhs, x, lin_rtol=1e-8, lin_max_iter=200, raise_on_error=False)
+    assert res["status"] == _capi.ERR_NOT_CONVERGED, res
+    assert res["restarts"] == 21 and res["iterations"] == 21, res
+    assert res["relres"] == 1.0
+    assert torch.count_nonzero(x).item() == 0
+    # a well-posed system on the same handle: diagonal blocks only, one iteration
+    V2 = np.zeros_like(V)
+    for r in range(X.shape[0]):
+        for q in range(rp[r], rp[r + 1]):
+            if ci[q] == r:
+                V2[q] = 2.0 * np.eye(b)
+    vals2 = torch.tensor(V2.ravel(), dtype=dt_, device=cuda)
+    rhs2 = torch.tensor(mesh.uniform(3, X.shape[0] * b) + 0.5, dtype=torch.float64, device=cuda)
+    for solver in ("bicgstab", "gmres"):
+        x2 = torch.empty_like(rhs2)
+        res2 = d.linear_solve(vals2, rhs2, x2, lin_rtol=1e-10, linear_solver=solver)
+        assert res2["status"] == 0 and res2["restarts"] == 0 and res2["iterations"] == 1, (solver, res2)
+        assert torch.allclose(x2, rhs2 / 2.0, rtol=1e-14, atol=0.0)
