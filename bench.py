@@ -445,6 +445,8 @@ def main():
                      "fp64_inst_per_element": prof["fp64_inst_per_element"], "sm_mhz": sm_mhz,
                      "source": "FP64 instruction count per element from ncu (profiles/k_defect_jacobian_hex_fp64.md)"}
     traffic32 = prof.get("jacobian_f32_bytes_per_assembly")
+    # the colour launches of one assembly (the rooflines' figures are per launch)
+    n_launch = int(d.pattern_info().get("n_colors", prof.get("launches_per_assembly", 8)))
 
     cpu, check = None, None
     if rank == 0:
@@ -475,8 +477,9 @@ def main():
                                                           "roofline": {"bound": "hbm", "kernel": "FP32 Jacobian assembly alone (k_jacobian_lanes, one lane per element corner)",
                                                                        "achieved": alg32 / (jac32_ms * 1e-3) / 1e9, "peak": peak,
                                                                        "unit": "GB/s", "frac": alg32 / (jac32_ms * 1e-3) / 1e9 / peak,
-                                                                       "algorithmic_bytes": alg32,
-                                                                       "traffic": traffic32,
+                                                                       "algorithmic_bytes": alg32 / n_launch,
+                                                                       "traffic": traffic32 / n_launch if traffic32 else None,
+                                                                       "per": f"launch (one colour; {n_launch} per assembly, the time of the assembly / {n_launch})",
                                                                        "traffic_source": prof.get("source_f32")}}}),
             "e2e": {"value": world * n_el / (e2e_ms * 1e-3), "unit": "elems/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
@@ -484,9 +487,11 @@ def main():
                                    "note": "consecutive host-buffer steps: step k's device-to-host copies overlap step k+1's "
                                            "upload and assembly (copy stream, two device buffer sets)"}},
             "roofline": {"bound": "hbm", "kernel": "fused FP64 defect + Jacobian assembly (one launch per colour)",
-                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "traffic_source": prof.get("source_f64"),
-                         "algorithmic_bytes": alg_bytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic / n_launch if traffic else None, "traffic_source": prof.get("source_f64"),
+                         "algorithmic_bytes": alg_bytes / n_launch,
+                         "per": f"launch (one colour; {n_launch} per assembly, the time of the assembly / {n_launch})",
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
                          "fp64_pipe": fp64_pipe,
                          "note": "FP64-pipe bound (GB300: 2 FP64 lanes per clock per SM); HBM traffic runs underneath"},
             "cpu_baseline": cpu,
