@@ -48,6 +48,23 @@ def test_assembly_without_setup_is_a_state_error():
     assert st == _capi.ERR_STATE
 
 
+def test_linear_algebra_entry_points_check_their_arguments_on_the_host():
+    """The linear-solve and split-SpMV entry points refuse a handle without a
+    mesh and invalid arguments before any device work."""
+    d = NavierStokesFV1("u,v,p")
+    lib = _capi.load()
+    p = _capi.NewtonParams(1e-8, 0.0, 10, 1e-4, 100, 0, _capi.F64, _capi.BICGSTAB, 30)
+    it, rr, rs = ctypes.c_int(-1), ctypes.c_double(-1.0), ctypes.c_int(-1)
+    st = lib.nsfv1_linear_solve(d._h, None, None, None, ctypes.byref(p), ctypes.byref(it), ctypes.byref(rr), ctypes.byref(rs), None)
+    assert st == _capi.ERR_STATE and "no mesh" in lib.nsfv1_last_error(d._h).decode()
+    assert it.value == -1 and rs.value == -1   # outputs untouched on refusal
+    assert lib.nsfv1_linear_solve(None, None, None, None, ctypes.byref(p), None, None, None, None) == _capi.ERR_ARGUMENT
+    assert lib.nsfv1_bsr_mv_split(d._h, None, None, None, None) == _capi.ERR_STATE
+    assert lib.nsfv1_split_vector(-1, None, None, None) == _capi.ERR_ARGUMENT
+    assert lib.nsfv1_split_vector(0, None, None, None) == _capi.OK   # nothing to do
+    assert lib.nsfv1_split_vector(4, None, None, None) == _capi.ERR_ARGUMENT
+
+
 @pytest.mark.parametrize("gen", ["quads", "hexes", "tris"])
 def test_pattern_and_coloring_bit_exact_with_oracle(gen):
     roid, X, C = {"quads": lambda: mesh.structured_quads(7), "hexes": lambda: mesh.structured_hexes(4),
