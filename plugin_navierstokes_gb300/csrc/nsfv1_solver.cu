@@ -438,20 +438,40 @@ __device__ __forceinline__ void prec_row(const MT* __restrict__ M, const double 
 }
 
 // the preconditioned vector of a row, and for FP32 matrices its split float pairs
-// (the SpMV's x operand, k_bsr_mv_split)
+// (the SpMV's x operand, k_bsr_mv_split). With FP32 blocks the products run in
+// double-float on the FP32 pipe (x split by integer operations, exact products,
+// TwoSum sums: about 1e-14 of sum |M x|), one conversion to FP64 per entry: GB300's
+// FP64 pipe would otherwise spend 9 conversions and 9 FMAs per row on it.
 template <typename MT, int b>
 __device__ __forceinline__ void prec_row_out(const MT* __restrict__ M, const double (&x)[b], double* __restrict__ out,
                                              float2* __restrict__ outSplit) {
-    double z[b];
-    prec_row<MT, b>(M, x, z);
+    if constexpr (std::is_same<MT, float>::value) {
+        float xh[b], xl[b];
 #pragma unroll
-    for (int i = 0; i < b; ++i) {
-        out[i] = z[i];
-        if constexpr (std::is_same<MT, float>::value) {
+        for (int j = 0; j < b; ++j) split_double(x[j], xh[j], xl[j]);
+#pragma unroll
+        for (int i = 0; i < b; ++i) {
+            float hi = 0.f, lo = 0.f;
+#pragma unroll
+            for (int j = 0; j < b; ++j) {
+                const float a = __ldg(M + i * b + j);
+                const float pr = __fmul_rn(a, xh[j]);
+                const float pe = fmaf(a, xh[j], -pr);   // a xh = pr + pe exactly
+                float e;
+                hi = two_sum(hi, pr, e);
+                lo += e + fmaf(a, xl[j], pe);
+            }
+            const double z = (double)hi + (double)lo;
+            out[i] = z;
             float h, l;
-            split_double(z[i], h, l);
+            split_double(z, h, l);
             outSplit[i] = make_float2(h, l);
         }
+    } else {
+        double z[b];
+        prec_row<MT, b>(M, x, z);
+#pragma unroll
+        for (int i = 0; i < b; ++i) out[i] = z[i];
     }
 }
 
