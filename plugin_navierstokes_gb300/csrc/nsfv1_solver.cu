@@ -440,8 +440,9 @@ __device__ __forceinline__ void prec_row(const MT* __restrict__ M, const double 
 // the preconditioned vector of a row, and for FP32 matrices its split float pairs
 // (the SpMV's x operand, k_bsr_mv_split). With FP32 blocks the products run in
 // double-float on the FP32 pipe (x split by integer operations, exact products,
-// TwoSum sums: about 1e-14 of sum |M x|), one conversion to FP64 per entry: GB300's
-// FP64 pipe would otherwise spend 9 conversions and 9 FMAs per row on it.
+// TwoSum sums: about 1e-14 of sum |M x|) and only the result goes to FP64 (two
+// conversions and an add per entry): GB300's FP64 pipe would otherwise spend b
+// conversions and b FMAs per entry on it.
 template <typename MT, int b>
 __device__ __forceinline__ void prec_row_out(const MT* __restrict__ M, const double (&x)[b], double* __restrict__ out,
                                              float2* __restrict__ outSplit) {
